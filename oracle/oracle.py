@@ -1,0 +1,218 @@
+"""ctypes binding of the C oracle (TEST INFRASTRUCTURE ONLY).
+
+Only tests/, ``__graft_entry__.smoke()`` and bench.py's CPU-baseline leg may import this module:
+it is the checker for the CUDA path, never the thing measured or shipped. ``build()`` compiles
+``hmp_oracle.c`` with gcc (no fused multiply-add, OpenMP) into ``oracle/liboracle.so``.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+LIB_PATH = HERE / "liboracle.so"
+
+KIND_PANON = 1
+KIND_PANO2 = 2
+KIND_PANO3 = 3
+FILTER_REFBOX = 0
+FILTER_BINOMIAL5 = 1
+
+
+def build(force: bool = False) -> Path:
+    src = [HERE / "hmp_oracle.c", HERE / "hmp_oracle_body.h", HERE / "hmp_oracle.h"]
+    if LIB_PATH.exists() and not force and all(LIB_PATH.stat().st_mtime >= s.stat().st_mtime for s in src):
+        return LIB_PATH
+    cmd = ["gcc", "-O2", "-std=c11", "-ffp-contract=off", "-fopenmp", "-fPIC", "-shared", "-Wall",
+           "-o", str(LIB_PATH) + ".tmp", str(HERE / "hmp_oracle.c")]
+    subprocess.run(cmd, check=True)
+    os.replace(str(LIB_PATH) + ".tmp", LIB_PATH)
+    return LIB_PATH
+
+
+class _Config(C.Structure):
+    _fields_ = [
+        ("kind", C.c_int),
+        ("n_images", C.c_int),
+        ("num_levels", C.c_int),
+        ("batch", C.c_int),
+        ("minimize_blend", C.c_int),
+        ("fused3", C.c_int),
+        ("filter", C.c_int),
+        ("map_x", C.POINTER(C.POINTER(C.c_uint16))),
+        ("map_y", C.POINTER(C.POINTER(C.c_uint16))),
+        ("map_w", C.POINTER(C.c_int)),
+        ("map_h", C.POINTER(C.c_int)),
+        ("pos_x", C.POINTER(C.c_int)),
+        ("pos_y", C.POINTER(C.c_int)),
+        ("seam", C.POINTER(C.c_uint8)),
+        ("seam_w", C.c_int),
+        ("seam_h", C.c_int),
+    ]
+
+
+_lib = None
+
+
+def lib() -> C.CDLL:
+    global _lib
+    if _lib is None:
+        if not LIB_PATH.exists():
+            build()
+        L = C.CDLL(str(LIB_PATH))
+        P = C.POINTER
+        L.hmpo_canvas_size.argtypes = [P(_Config), P(C.c_int), P(C.c_int)]
+        L.hmpo_blend_geometry.argtypes = [P(_Config), P(C.c_int)]
+        for name in ("hmpo_stitch_f32", "hmpo_stitch_f64"):
+            getattr(L, name).argtypes = [P(_Config), P(P(C.c_uint8)), P(C.c_int), P(C.c_int), P(C.c_uint8)]
+        L.hmpo_stitch_f64_unpacked.argtypes = [P(_Config), P(P(C.c_uint8)), P(C.c_int), P(C.c_int), P(C.c_double)]
+        L.hmpo_downsample_rgba_f32.argtypes = [P(C.c_float), C.c_int, C.c_int, P(C.c_float)]
+        L.hmpo_laplacian_rgba_f32.argtypes = [P(C.c_float), C.c_int, C.c_int, P(C.c_float), P(C.c_float)]
+        L.hmpo_reconstruct_rgba_f32.argtypes = [P(C.c_float), P(C.c_float), C.c_int, C.c_int, P(C.c_float)]
+        L.hmpo_downsample_mask_f32.argtypes = [P(C.c_float), C.c_int, C.c_int, C.c_int, P(C.c_float)]
+        L.hmpo_set_threads.argtypes = [C.c_int]
+        L.hmpo_get_threads.restype = C.c_int
+        _lib = L
+    return _lib
+
+
+def _ptr(a: np.ndarray, t):
+    return a.ctypes.data_as(C.POINTER(t))
+
+
+class Stitch:
+    """Oracle stitch for one rig description (numpy arrays, kept alive by this object)."""
+
+    def __init__(self, kind: int, map_x, map_y, pos_x, pos_y, seam: np.ndarray, num_levels: int, batch: int = 1,
+                 minimize_blend: bool = True, fused3: bool = True, filter: int = FILTER_REFBOX):
+        n = len(map_x)
+        self.n = n
+        self._mx = [np.ascontiguousarray(m, dtype=np.uint16) for m in map_x]
+        self._my = [np.ascontiguousarray(m, dtype=np.uint16) for m in map_y]
+        self._seam = np.ascontiguousarray(seam, dtype=np.uint8)
+        self._mxp = (C.POINTER(C.c_uint16) * n)(*[_ptr(m, C.c_uint16) for m in self._mx])
+        self._myp = (C.POINTER(C.c_uint16) * n)(*[_ptr(m, C.c_uint16) for m in self._my])
+        self._mw = (C.c_int * n)(*[m.shape[1] for m in self._mx])
+        self._mh = (C.c_int * n)(*[m.shape[0] for m in self._mx])
+        self._px = (C.c_int * n)(*[int(v) for v in pos_x])
+        self._py = (C.c_int * n)(*[int(v) for v in pos_y])
+        self.cfg = _Config(kind, n, num_levels, batch, int(minimize_blend), int(fused3), filter, self._mxp, self._myp,
+                           self._mw, self._mh, self._px, self._py, _ptr(self._seam, C.c_uint8), self._seam.shape[1],
+                           self._seam.shape[0])
+        self.batch = batch
+        w, h = C.c_int(), C.c_int()
+        rc = lib().hmpo_canvas_size(C.byref(self.cfg), C.byref(w), C.byref(h))
+        if rc != 0:
+            raise ValueError(f"oracle: invalid configuration ({rc})")
+        self.canvas_w, self.canvas_h = w.value, h.value
+
+    @classmethod
+    def from_rig(cls, rig, num_levels: int, batch: int = 1, minimize_blend: bool = True, **kw) -> "Stitch":
+        return cls(rig.kind, rig.map_x, rig.map_y, rig.pos_x, rig.pos_y, rig.seam, num_levels, batch,
+                   minimize_blend, **kw)
+
+    def geometry(self) -> dict:
+        out = (C.c_int * 9)()
+        rc = lib().hmpo_blend_geometry(C.byref(self.cfg), out)
+        if rc != 0:
+            raise ValueError(f"oracle: geometry failed ({rc})")
+        v = list(out)
+        return {"blend": tuple(v[0:4]), "write": tuple(v[4:8]), "levels": v[8]}
+
+    def _inputs(self, frames):
+        fr = [np.ascontiguousarray(f, dtype=np.uint8) for f in frames]
+        for f in fr:
+            if f.ndim != 4 or f.shape[0] != self.batch or f.shape[3] != 4:
+                raise ValueError("frames must be [batch, h, w, 4] uint8")
+        ptrs = (C.POINTER(C.c_uint8) * self.n)(*[_ptr(f, C.c_uint8) for f in fr])
+        ws = (C.c_int * self.n)(*[f.shape[2] for f in fr])
+        hs = (C.c_int * self.n)(*[f.shape[1] for f in fr])
+        return fr, ptrs, ws, hs
+
+    def run(self, frames, precision: str = "f32") -> np.ndarray:
+        fr, ptrs, ws, hs = self._inputs(frames)
+        out = np.zeros((self.batch, self.canvas_h, self.canvas_w, 4), dtype=np.uint8)
+        fn = lib().hmpo_stitch_f32 if precision == "f32" else lib().hmpo_stitch_f64
+        rc = fn(C.byref(self.cfg), ptrs, ws, hs, _ptr(out, C.c_uint8))
+        if rc != 0:
+            raise RuntimeError(f"oracle stitch failed ({rc})")
+        return out
+
+    def run_unpacked_f64(self, frames) -> np.ndarray:
+        """Pre-pack FP64 blend result of the write ROI, [batch, wh, ww, 4]."""
+        g = self.geometry()
+        _, _, ww, wh = g["write"]
+        fr, ptrs, ws, hs = self._inputs(frames)
+        out = np.zeros((self.batch, wh, ww, 4), dtype=np.float64)
+        rc = lib().hmpo_stitch_f64_unpacked(C.byref(self.cfg), ptrs, ws, hs, _ptr(out, C.c_double))
+        if rc != 0:
+            raise RuntimeError(f"oracle stitch failed ({rc})")
+        return out
+
+
+def set_threads(n: int) -> None:
+    lib().hmpo_set_threads(int(n))
+
+
+def get_threads() -> int:
+    return int(lib().hmpo_get_threads())
+
+
+def downsample_rgba(img: np.ndarray) -> np.ndarray:
+    img = np.ascontiguousarray(img, dtype=np.float32)
+    h, w = img.shape[-3], img.shape[-2]
+    out = np.zeros(((h + 1) // 2, (w + 1) // 2, 4), dtype=np.float32)
+    lib().hmpo_downsample_rgba_f32(_ptr(img, C.c_float), w, h, _ptr(out, C.c_float))
+    return out
+
+
+def laplacian_rgba(high: np.ndarray, low: np.ndarray) -> np.ndarray:
+    high = np.ascontiguousarray(high, dtype=np.float32)
+    low = np.ascontiguousarray(low, dtype=np.float32)
+    h, w = high.shape[-3], high.shape[-2]
+    out = np.zeros((h, w, 4), dtype=np.float32)
+    lib().hmpo_laplacian_rgba_f32(_ptr(high, C.c_float), w, h, _ptr(low, C.c_float), _ptr(out, C.c_float))
+    return out
+
+
+def reconstruct_rgba(low: np.ndarray, lap: np.ndarray) -> np.ndarray:
+    low = np.ascontiguousarray(low, dtype=np.float32)
+    lap = np.ascontiguousarray(lap, dtype=np.float32)
+    h, w = lap.shape[-3], lap.shape[-2]
+    out = np.zeros((h, w, 4), dtype=np.float32)
+    lib().hmpo_reconstruct_rgba_f32(_ptr(low, C.c_float), _ptr(lap, C.c_float), w, h, _ptr(out, C.c_float))
+    return out
+
+
+def downsample_mask(mask: np.ndarray) -> np.ndarray:
+    mask = np.ascontiguousarray(mask, dtype=np.float32)
+    h, w, k = mask.shape
+    out = np.zeros(((h + 1) // 2, (w + 1) // 2, k), dtype=np.float32)
+    lib().hmpo_downsample_mask_f32(_ptr(mask, C.c_float), w, h, k, _ptr(out, C.c_float))
+    return out
+
+
+def load_golden_case(npz, name: str):
+    """Unpack one golden stitch case into (kind, levels, minimize, batch, maps..., frames, canvas)."""
+    meta = npz[f"{name}/meta"]
+    kind, n, levels, minimize, batch = (int(v) for v in meta[:5])
+    pos = npz[f"{name}/pos"]
+    case = {
+        "kind": kind,
+        "n": n,
+        "levels": levels,
+        "minimize": bool(minimize),
+        "batch": batch,
+        "pos_x": [int(v) for v in pos[0]],
+        "pos_y": [int(v) for v in pos[1]],
+        "seam": npz[f"{name}/seam"],
+        "map_x": [npz[f"{name}/map_x{i}"] for i in range(n)],
+        "map_y": [npz[f"{name}/map_y{i}"] for i in range(n)],
+        "frames": [npz[f"{name}/frame{i}"] for i in range(n)],
+        "canvas": npz[f"{name}/canvas"],
+    }
+    return case
