@@ -1,0 +1,352 @@
+#!/usr/bin/env python
+"""Throughput of the GB300 stitching path on the production two-image workload.
+
+Workload (the reference's headline case, README.md:1-7): two 5120x2880 RGBA frames remapped
+through seeded cylindrical CV_16U tables onto an 8500x3300 canvas, 6-level Laplacian blend,
+FP32 pyramid, uint8 pack; synthetic seeded inputs (no dataset). One step = one process() call
+on one frame. Inputs are larger than L2: three frame/canvas sets rotate between steps.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Prints one JSON line. ``value`` is canvas Mpix/s over all ranks with inputs resident in HBM;
+``e2e`` is the same metric through the public API with pinned host frames copied in and the
+canvas copied out every step; ``roofline`` is the dominant kernel's algorithmic bytes per launch
+over its CUDA-event duration against the measured HBM copy bandwidth; ``cpu_baseline`` is the
+oracle (a C port of the reference's algorithm) on the host cores. ``--impl reference`` times
+that CPU implementation as the reference arm. Multi-GPU runs are independent replicas (weak
+scaling, no collective on the data path).
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+REPO = Path(__file__).resolve().parent
+sys.path.insert(0, str(REPO))
+sys.path.insert(0, str(REPO / "hm-cupano_gb300"))
+
+METRIC = "canvas Mpix/s & fps at 8500x3300 L=6; % HBM peak; p50/p99 serve latency"
+WORKLOAD = "pano2_5120x2880_to_8500x3300"
+N_SETS = 3
+
+
+def _peaks() -> tuple[float, str]:
+    p = REPO / "MEASURED_PEAKS.json"
+    if p.exists():
+        try:
+            d = json.loads(p.read_text())
+            return float(d["hbm_gbs"]), "measured"
+        except Exception:
+            pass
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.samples: list[list[str]] = []
+        self._stop = threading.Event()
+        self._thr = None
+
+    def _run(self):
+        while not self._stop.is_set():
+            try:
+                out = subprocess.run(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}",
+                                      "--format=csv,noheader,nounits"], capture_output=True, text=True, timeout=5)
+                for line in out.stdout.strip().splitlines():
+                    self.samples.append([v.strip() for v in line.split(",")])
+            except Exception:
+                pass
+            self._stop.wait(0.2)
+
+    def __enter__(self):
+        self._thr = threading.Thread(target=self._run, daemon=True)
+        self._thr.start()
+        return self
+
+    def __exit__(self, *exc):
+        self._stop.set()
+        if self._thr:
+            self._thr.join(timeout=6)
+
+    def summary(self) -> dict:
+        sm = [float(s[1]) for s in self.samples if len(s) >= 9 and s[1].replace(".", "").isdigit()]
+        mx = [float(s[2]) for s in self.samples if len(s) >= 9 and s[2].replace(".", "").isdigit()]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for s in self.samples:
+            if len(s) < 9:
+                continue
+            for name, v in zip(names, s[5:9]):
+                if v.strip().lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(self.samples)}
+
+
+def _masks(rig):
+    import hmpano
+
+    pos = [hmpano.SpatialTiff(float(x), float(y)) for x, y in zip(rig.pos_x, rig.pos_y)]
+    return hmpano.ControlMasks(rig.map_x[0], rig.map_y[0], rig.map_x[1], rig.map_y[1], rig.seam, pos)
+
+
+def cpu_baseline(rig, frames, levels: int, frames_sample: int = 2) -> dict:
+    """The oracle (C port of the reference algorithm) on all host cores, bounded sample."""
+    from oracle import oracle
+
+    oracle.build()
+    threads = os.cpu_count() or 1
+    oracle.set_threads(threads)
+    st = oracle.Stitch.from_rig(rig, levels)
+    st.run(frames)  # warm-up
+    t0 = time.perf_counter()
+    for _ in range(frames_sample):
+        st.run(frames)
+    dt = (time.perf_counter() - t0) / frames_sample
+    mpix = rig.canvas_w * rig.canvas_h / 1e6
+    return {"value": round(mpix / dt, 2), "unit": "Mpix/s", "cores": oracle.get_threads(), "kind": "port",
+            "sample": f"{frames_sample} full frames of {WORKLOAD} L={levels} FP32 after 1 warm-up, "
+                      f"{dt * 1e3:.0f} ms/frame", "fps": round(1.0 / dt, 3)}
+
+
+def reference_arm(args) -> None:
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    from hmpano import synth
+    from oracle import oracle
+
+    rig = synth.workload_rig(WORKLOAD, seed=1234)
+    frames = synth.rig_frames(rig, seed=1)
+    oracle.build()
+    threads = os.cpu_count() or 1
+    oracle.set_threads(threads)
+    st = oracle.Stitch.from_rig(rig, args.levels)
+    for _ in range(args.warmup):
+        st.run(frames)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        st.run(frames)
+    dt = (time.perf_counter() - t0) / args.steps
+    mpix = rig.canvas_w * rig.canvas_h / 1e6
+    value = mpix / dt
+    line = {
+        "impl": "reference", "metric": METRIC, "value": round(value, 3), "unit": "Mpix/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(dt * 1e3, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "fps": round(1.0 / dt, 4),
+        "config": {"workload": WORKLOAD, "levels": args.levels, "storage": "f32", "batch": 1,
+                   "canvas": f"{rig.canvas_w}x{rig.canvas_h}"},
+        "cpu_baseline": {"value": round(value, 3), "unit": "Mpix/s", "cores": oracle.get_threads(), "kind": "port",
+                         "sample": f"{args.steps} full frames after {args.warmup} warm-up"},
+        "e2e": {"value": round(value, 3), "unit": "Mpix/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "gpu_launches": 0,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=10)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--levels", type=int, default=6)
+    ap.add_argument("--storage", default="f32")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(3, args.warmup)
+    if args.impl == "reference":
+        reference_arm(args)
+        return
+
+    import numpy as np
+    import torch
+
+    import __graft_entry__
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    __graft_entry__.build()
+    import hmpano
+    from hmpano import _lib, synth
+
+    rig = synth.workload_rig(WORKLOAD, seed=1234)
+    host_frames = synth.rig_frames(rig, seed=1 + rank)
+    pano = hmpano.CudaStitchPano(1, args.levels, _masks(rig), quiet=True, storage=args.storage)
+    if not pano.status.ok():
+        raise SystemExit(f"stitcher: {pano.status}")
+    info = pano.info()
+    W, H = rig.canvas_w, rig.canvas_h
+    dev = torch.device("cuda", local)
+    stream = torch.cuda.Stream(dev)
+    sets = []
+    for i in range(N_SETS):
+        ins = [torch.from_numpy(np.roll(f, i, axis=2)).to(dev) for f in host_frames]
+        canvas = torch.empty((1, H, W, 4), dtype=torch.uint8, device=dev)
+        sets.append((ins, canvas))
+    # Pre-marshalled C-ABI arguments: the timed loop is one C call per step.
+    fn = _lib.lib().hmp_stitcher_process
+    calls = []
+    for ins, canvas in sets:
+        imgs = (_lib.Image * 2)(*[hmpano.pano._image(t) for t in ins])
+        cv = hmpano.pano._image(canvas)
+        calls.append((imgs, cv))
+    sptr = C.c_void_p(stream.cuda_stream)
+
+    def step(i):
+        imgs, cv = calls[i % N_SETS]
+        s = fn(pano._handle, imgs, 2, C.byref(cv), sptr)
+        if s.code:
+            raise RuntimeError(s.message.decode())
+
+    with torch.cuda.stream(stream):
+        for i in range(args.warmup):
+            step(i)
+    torch.cuda.synchronize()
+    pano.set_timing(True)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    sampler = ClockSampler(local) if rank == 0 else None
+    if sampler:
+        sampler.__enter__()
+    e0.record(stream)
+    for i in range(args.steps):
+        step(i)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    if sampler:
+        sampler.__exit__(None, None, None)
+    if dist:
+        dist.barrier()
+    ms = e0.elapsed_time(e1) / args.steps
+    ktimes = pano.kernel_times()
+    pano.set_timing(False)
+    if dist:
+        t = torch.tensor([ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    frames_total = world * args.steps
+    mpix = W * H / 1e6
+    value = frames_total * mpix / (ms * args.steps / 1e3)
+
+    # Untimed, timing-off pass of the same length: event records do not distort the number.
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for i in range(args.steps):
+        step(i)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms_plain = e0.elapsed_time(e1) / args.steps
+
+    # End to end through the public API: pinned host frames in, canvas out, every step.
+    e2e = None
+    if not args.no_e2e:
+        pinned_in = [torch.from_numpy(f).pin_memory() for f in host_frames]
+        pinned_out = torch.empty((1, H, W, 4), dtype=torch.uint8).pin_memory()
+        dins, dcanvas = sets[0]
+        k_e2e = max(10, min(args.steps, 50))
+        for _ in range(3):
+            with torch.cuda.stream(stream):
+                for d, h in zip(dins, pinned_in):
+                    d.copy_(h, non_blocking=True)
+                pano.process(dins[0], dins[1], dcanvas, stream=stream)
+                pinned_out.copy_(dcanvas, non_blocking=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        with torch.cuda.stream(stream):
+            for _ in range(k_e2e):
+                for d, h in zip(dins, pinned_in):
+                    d.copy_(h, non_blocking=True)
+                pano.process(dins[0], dins[1], dcanvas, stream=stream)
+                pinned_out.copy_(dcanvas, non_blocking=True)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms_e2e = e0.elapsed_time(e1) / k_e2e
+        e2e = {"value": round(world * mpix / (ms_e2e / 1e3), 2), "unit": "Mpix/s",
+               "h2d_bytes_per_step": int(sum(f.nbytes for f in host_frames)),
+               "d2h_bytes_per_step": int(W * H * 4), "ms_per_step": round(ms_e2e, 4), "steps": k_e2e}
+
+    peak, peak_kind = _peaks()
+    names = ["canvas_gather", "pyr_down", "pyr_up"]
+    dom = max(names, key=lambda k: ktimes[k][0])
+    tot, cnt = ktimes[dom]
+    per_launch_ms = tot / max(cnt, 1)
+    wr = info["write_rect"]
+    canvas_px = W * H
+    gather_bytes = (canvas_px - wr[2] * wr[3]) * 13.0 if info["levels"] else canvas_px * 13.0
+    dom_bytes = {"canvas_gather": gather_bytes}.get(dom)
+    achieved = dom_bytes / (per_launch_ms / 1e3) / 1e9 if dom_bytes else None
+    traffic = None
+    tp = REPO / "profiles" / "traffic.json"
+    if tp.exists():
+        try:
+            traffic = json.loads(tp.read_text()).get(f"{WORKLOAD}/L{args.levels}/{args.storage}/{dom}")
+        except Exception:
+            traffic = None
+    line = {
+        "metric": METRIC,
+        "value": round(value, 2),
+        "unit": "Mpix/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": round(ms, 5),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32" if args.storage == "f32" else "f16-storage/f32-arith",
+        "data": "synthetic",
+        "fps": round(world * 1e3 / ms, 1),
+        "hbm_frac_frame": round(info["m0_bytes"] / (ms / 1e3) / (peak * 1e9), 4),
+        "m0_bytes_per_frame": int(info["m0_bytes"]),
+        "ms_per_step_timing_off": round(ms_plain, 5),
+        "config": {"workload": WORKLOAD, "levels": args.levels, "storage": args.storage, "batch": 1,
+                   "canvas": f"{W}x{H}", "blend_rect": list(info["blend_rect"]),
+                   "l2": f"inputs larger than L2: {N_SETS} rotating frame/canvas sets",
+                   "parallelism": f"replicas x{world}"},
+        "roofline": {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1) if achieved else None,
+                     "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4) if achieved else None,
+                     "traffic": traffic, "peak_kind": peak_kind,
+                     "bytes_per_launch": int(dom_bytes) if dom_bytes else None,
+                     "ms_per_launch": round(per_launch_ms, 5)},
+        "kernel_ms": {k: round(v[0] / max(v[1], 1), 5) for k, v in ktimes.items()},
+        "gpu_launches": int(sum(v[1] for v in ktimes.values())),
+        "e2e": e2e,
+        "clocks": sampler.summary() if sampler else None,
+    }
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(rig, host_frames, args.levels)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,56 @@
+// hmp_kernels.h -- launch interface of the stitching kernels (host-visible).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "hmp_device.cuh"
+
+namespace hmp {
+
+// Canvas gather: every canvas pixel outside `skip` takes its gather-plane pixel.
+struct GatherArgs {
+  SrcSet S;
+  PlaneDev P;  // canvas plane, rect = whole canvas
+  CanvasDev C;
+  int batch;
+  int skip_x0, skip_y0, skip_x1, skip_y1;  // pixels written by the pyramid (end exclusive)
+  int opaque;
+};
+
+// Shared by the Gaussian-pyramid (down) and blend/reconstruct (up) kernels.
+struct PyrArgs {
+  SrcSet S;
+  PlaneDev slot[kDevMaxImages];
+  int n;
+  int levels;  // effective L >= 1
+  int lw[kDevMaxLevels + 1];
+  int lh[kDevMaxLevels + 1];
+  void* G[kDevMaxImages][kDevMaxLevels];  // level l >= 1 of slot k: [batch][lh][lw] storage pixels
+  const uint8_t* mask0;                   // level-0 weight value (two-image) or label, blend coords
+  int mask0_pitch;
+  const float* maskL[kDevMaxLevels];      // level l >= 1: [lh][lw][K]
+  int K;
+  int opaque;
+  int tile;  // level-0 tile edge
+  int rm_odd, rm_even;  // smem region capacities (pixels) for odd / even levels
+  CanvasDev C;
+  int wx0, wy0, wx1, wy1;  // write rect, blend coordinates, end exclusive
+  int cx_off, cy_off;      // canvas = blend + offset
+  int tx0, ty0;            // first up-tile index
+};
+
+// One-time attribute setup (dynamic shared memory limits). Call before capture.
+cudaError_t kernels_init();
+
+cudaError_t launch_canvas_gather(const GatherArgs& a, bool vec, cudaStream_t stream);
+
+// Gaussian levels 1..L-1 of every slot; grid = tiles over the blend region x batch.
+cudaError_t launch_pyr_down(const PyrArgs& a, int storage, dim3 grid, cudaStream_t stream);
+
+// Blend + reconstruct + pack of the write rect; grid = up-tiles over the write rect x batch.
+cudaError_t launch_pyr_up(const PyrArgs& a, int rule, int storage, dim3 grid, size_t smem, cudaStream_t stream);
+
+size_t pyr_down_smem(int tile);
+size_t pyr_up_smem(int n, int rm_odd, int rm_even);
+
+}  // namespace hmp

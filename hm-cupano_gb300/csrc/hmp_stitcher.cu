@@ -1,0 +1,492 @@
+// hmp_stitcher.cu -- stitcher object and the C ABI (include/hmpano.h).
+//
+// Construction plans the configuration on the host (hmp_plan.cpp), uploads the gather planes and
+// the mask pyramid, and allocates the pyramid levels. process() then launches at most three
+// kernels and allocates nothing:
+//   caller stream : pyr_down (levels >= 2), pyr_up (blend + reconstruct + pack of the write rect)
+//   aux stream    : canvas_gather of everything outside the write rect (forked/joined by events)
+// The hard seam (levels == 0) is a single canvas_gather on the caller stream.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "hmp_kernels.h"
+#include "hmp_plan.h"
+#include "hmpano.h"
+
+namespace {
+
+hmp_status make_status(int code, const std::string& msg) {
+  hmp_status s;
+  s.code = code;
+  std::snprintf(s.message, sizeof(s.message), "%s", msg.c_str());
+  return s;
+}
+
+hmp_status ok_status() { return make_status(HMP_OK, ""); }
+
+hmp_status cuda_status(cudaError_t e, const char* what) {
+  return make_status(int(e), std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+inline int round_up(int v, int a) { return (v + a - 1) / a * a; }
+
+}  // namespace
+
+struct hmp_stitcher {
+  hmp::Plan plan;  // geometry; the large host arrays are released after upload
+  hmp_status status = ok_status();
+  int device = -1;
+  std::vector<void*> allocations;
+  size_t device_bytes = 0;
+  hmp::PlaneDev canvas_plane{};
+  hmp::PlaneDev slot_planes[hmp::kDevMaxImages]{};
+  void* G[hmp::kDevMaxImages][hmp::kDevMaxLevels]{};
+  const float* maskL[hmp::kDevMaxLevels]{};
+  const uint8_t* mask0 = nullptr;
+  int mask0_pitch = 0;
+  int tile_down = 0, tile_up = 0;
+  int rm_odd = 0, rm_even = 0;
+  size_t up_smem = 0;
+  cudaStream_t aux = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  double m0_bytes = 0;
+  int launches = 0;
+  // Optional per-kernel event timing (hmp_stitcher_set_timing).
+  static constexpr int kTimingSlots = 4096;
+  bool timing = false;
+  std::vector<cudaEvent_t> tev;  // [slot][kernel][begin/end]
+  std::vector<unsigned char> tused;
+  int tnext = 0;
+  double tms[3] = {0, 0, 0};
+  long long tcount[3] = {0, 0, 0};
+
+  ~hmp_stitcher() {
+    for (cudaEvent_t e : tev) cudaEventDestroy(e);
+    if (ev_fork) cudaEventDestroy(ev_fork);
+    if (ev_join) cudaEventDestroy(ev_join);
+    if (aux) cudaStreamDestroy(aux);
+    for (void* p : allocations) cudaFree(p);
+  }
+
+  cudaError_t alloc(void** p, size_t bytes) {
+    cudaError_t e = cudaMalloc(p, bytes);
+    if (e == cudaSuccess) {
+      allocations.push_back(*p);
+      device_bytes += bytes;
+    }
+    return e;
+  }
+
+  // Uploads one gather plane with 16-byte aligned rows.
+  cudaError_t upload_plane(const hmp::GatherPlane& g, hmp::PlaneDev& d) {
+    d = hmp::PlaneDev{};
+    d.x0 = g.rect.x;
+    d.y0 = g.rect.y;
+    d.w = g.rect.w;
+    d.h = g.rect.h;
+    d.default_owner = g.default_owner;
+    if (g.rect.empty()) {
+      d.w = d.h = 0;
+      return cudaSuccess;
+    }
+    const int mp = round_up(g.rect.w, 4);
+    void* m = nullptr;
+    cudaError_t e = alloc(&m, size_t(mp) * 4 * g.rect.h);
+    if (e != cudaSuccess) return e;
+    e = cudaMemcpy2D(m, size_t(mp) * 4, g.map.data(), size_t(g.rect.w) * 4, size_t(g.rect.w) * 4, g.rect.h,
+                     cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return e;
+    d.map = static_cast<const uint32_t*>(m);
+    d.map_pitch = mp;
+    if (!g.owner.empty()) {
+      const int op = round_up(g.rect.w, 16);
+      void* o = nullptr;
+      e = alloc(&o, size_t(op) * g.rect.h);
+      if (e != cudaSuccess) return e;
+      e = cudaMemcpy2D(o, op, g.owner.data(), g.rect.w, g.rect.w, g.rect.h, cudaMemcpyHostToDevice);
+      if (e != cudaSuccess) return e;
+      d.owner = static_cast<const uint8_t*>(o);
+      d.owner_pitch = op;
+    }
+    return cudaSuccess;
+  }
+
+  hmp_status setup() {
+    hmp::Plan& p = plan;
+    cudaError_t e = cudaGetDevice(&device);
+    if (e != cudaSuccess) return cuda_status(e, "cudaGetDevice");
+    e = hmp::kernels_init();
+    if (e != cudaSuccess) return cuda_status(e, "kernel setup");
+    if (p.canvas_plane_used) {
+      e = upload_plane(p.canvas, canvas_plane);
+      if (e != cudaSuccess) return cuda_status(e, "canvas plane upload");
+    }
+    launches = p.canvas_plane_used ? 1 : 0;
+    if (p.levels > 0) {
+      const int n = p.n, B = p.batch, L = p.levels;
+      for (int k = 0; k < n; ++k) {
+        e = upload_plane(p.slots[k], slot_planes[k]);
+        if (e != cudaSuccess) return cuda_status(e, "slot plane upload");
+      }
+      // Level-0 mask: weight value (two-image) or label per blend pixel.
+      mask0_pitch = round_up(p.lw[0], 16);
+      void* m0 = nullptr;
+      e = alloc(&m0, size_t(mask0_pitch) * p.lh[0]);
+      if (e != cudaSuccess) return cuda_status(e, "mask allocation");
+      e = cudaMemcpy2D(m0, mask0_pitch, p.mask0.data(), p.lw[0], p.lw[0], p.lh[0], cudaMemcpyHostToDevice);
+      if (e != cudaSuccess) return cuda_status(e, "mask upload");
+      mask0 = static_cast<const uint8_t*>(m0);
+      const size_t px_bytes = p.storage == HMP_STORAGE_F16 ? 8 : 16;
+      for (int l = 1; l < L; ++l) {
+        void* mk = nullptr;
+        const size_t mb = p.mask_levels[l].size() * sizeof(float);
+        e = alloc(&mk, mb);
+        if (e != cudaSuccess) return cuda_status(e, "mask pyramid allocation");
+        e = cudaMemcpy(mk, p.mask_levels[l].data(), mb, cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) return cuda_status(e, "mask pyramid upload");
+        maskL[l] = static_cast<const float*>(mk);
+        for (int k = 0; k < n; ++k) {
+          const size_t gb = size_t(B) * p.lw[l] * p.lh[l] * px_bytes;
+          e = alloc(&G[k][l], gb);
+          if (e != cudaSuccess) return cuda_status(e, "pyramid allocation");
+          // Tiles that miss a slot are never written; their levels must read as zero.
+          e = cudaMemset(G[k][l], 0, gb);
+          if (e != cudaSuccess) return cuda_status(e, "pyramid clear");
+        }
+      }
+      // Tiles: level-0 edge a multiple of 2^(L-1); smaller up-tiles for many images keep the
+      // per-CTA shared memory (n+1 images' worth of two levels) within the SM.
+      const int align = 1 << (L - 1);
+      tile_down = std::max(64, align);
+      tile_up = std::max(n > 4 ? 32 : 64, align);
+      rm_odd = (tile_up / 2 + 2) * (tile_up / 2 + 2);
+      rm_even = (tile_up / 4 + 2) * (tile_up / 4 + 2);
+      up_smem = hmp::pyr_up_smem(n, rm_odd, rm_even);
+      if (up_smem > 227 * 1024)
+        return make_status(HMP_ERR_NOT_SUPPORTED, "pyramid tile does not fit in shared memory");
+      launches += (L > 1 ? 1 : 0) + 1;
+    }
+    if (p.canvas_plane_used && p.levels > 0) {
+      e = cudaStreamCreateWithFlags(&aux, cudaStreamNonBlocking);
+      if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming);
+      if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev_join, cudaEventDisableTiming);
+      if (e != cudaSuccess) return cuda_status(e, "stream setup");
+    }
+    e = cudaDeviceSynchronize();
+    if (e != cudaSuccess) return cuda_status(e, "upload");
+    compute_m0();
+    // Release the large host-side arrays; geometry stays.
+    std::vector<uint8_t>().swap(p.canvas.owner);
+    std::vector<uint32_t>().swap(p.canvas.map);
+    for (auto& s : p.slots) {
+      std::vector<uint8_t>().swap(s.owner);
+      std::vector<uint32_t>().swap(s.map);
+    }
+    std::vector<uint8_t>().swap(p.mask0);
+    for (auto& m : p.mask_levels) std::vector<float>().swap(m);
+    return ok_status();
+  }
+
+  // Compulsory bytes per process(): outside the write rect, 4 (table) + 1 (seam) + 4 (source)
+  // + 4 (canvas) per canvas pixel; inside it, 4 + 4 per mapped slot pixel, 1 (seam) + 4 (canvas)
+  // per pixel. Tables and seam are read once per call, sources and canvas once per frame.
+  void compute_m0() {
+    const hmp::Plan& p = plan;
+    const double B = p.batch;
+    const double canvas_px = double(p.canvas_w) * p.canvas_h;
+    const double a0 = p.levels > 0 ? double(p.write.w) * p.write.h : 0.0;
+    double bytes = (canvas_px - a0) * (5.0 + 8.0 * B);
+    if (p.levels > 0) {
+      double mapped = 0;
+      for (const auto& s : p.slots)
+        for (uint32_t e : s.map) mapped += e != hmp::kNoEntry;
+      bytes += mapped * (4.0 + 4.0 * B) + a0 * (1.0 + 4.0 * B);
+    }
+    m0_bytes = bytes;
+  }
+
+  cudaError_t timing_enable(bool on) {
+    if (on && tev.empty()) {
+      tev.resize(size_t(kTimingSlots) * 3 * 2);
+      for (auto& e : tev) {
+        cudaError_t r = cudaEventCreate(&e);
+        if (r != cudaSuccess) return r;
+      }
+      tused.assign(size_t(kTimingSlots) * 3, 0);
+    }
+    timing = on;
+    tnext = 0;
+    std::fill(tused.begin(), tused.end(), 0);
+    for (int k = 0; k < 3; ++k) tms[k] = 0, tcount[k] = 0;
+    return cudaSuccess;
+  }
+
+  cudaEvent_t tbegin(int kernel, cudaStream_t s) {
+    if (!timing || tnext >= kTimingSlots) return nullptr;
+    cudaEventRecord(tev[(size_t(tnext) * 3 + kernel) * 2], s);
+    return tev[(size_t(tnext) * 3 + kernel) * 2];
+  }
+  void tend(int kernel, cudaStream_t s) {
+    if (!timing || tnext >= kTimingSlots) return;
+    cudaEventRecord(tev[(size_t(tnext) * 3 + kernel) * 2 + 1], s);
+    tused[size_t(tnext) * 3 + kernel] = 1;
+  }
+
+  cudaError_t timing_collect(hmp_kernel_timing* out) {
+    for (int slot = 0; slot < tnext; ++slot)
+      for (int k = 0; k < 3; ++k) {
+        if (!tused[size_t(slot) * 3 + k]) continue;
+        float ms = 0;
+        cudaEvent_t e1 = tev[(size_t(slot) * 3 + k) * 2 + 1];
+        cudaError_t r = cudaEventSynchronize(e1);
+        if (r == cudaSuccess) r = cudaEventElapsedTime(&ms, tev[(size_t(slot) * 3 + k) * 2], e1);
+        if (r != cudaSuccess) return r;
+        tms[k] += ms;
+        tcount[k] += 1;
+      }
+    for (int k = 0; k < 3; ++k) {
+      out->total_ms[k] = tms[k];
+      out->launches[k] = tcount[k];
+      tms[k] = 0;
+      tcount[k] = 0;
+    }
+    tnext = 0;
+    std::fill(tused.begin(), tused.end(), 0);
+    return cudaSuccess;
+  }
+
+  hmp::SrcSet sources(const hmp_image* inputs) const {
+    hmp::SrcSet S{};
+    for (int i = 0; i < plan.n; ++i) {
+      S.ptr[i] = static_cast<const uchar4*>(inputs[i].data);
+      S.pitch[i] = (long long)inputs[i].pitch;
+      S.bstride[i] = (long long)inputs[i].pitch * inputs[i].height;
+      S.w[i] = inputs[i].width;
+      S.h[i] = inputs[i].height;
+    }
+    return S;
+  }
+
+  hmp_status process(const hmp_image* inputs, int n_inputs, const hmp_image* canvas, cudaStream_t s) {
+    const hmp::Plan& p = plan;
+    if (!inputs || n_inputs != p.n) return make_status(HMP_ERR_INVALID_VALUE, "inputs size != N");
+    if (!canvas || !canvas->data) return make_status(HMP_ERR_INVALID_DEVICE_POINTER, "Canvas must be provided");
+    if (canvas->width != p.canvas_w || canvas->height != p.canvas_h || canvas->pitch < size_t(canvas->width) * 4)
+      return make_status(HMP_ERR_INVALID_VALUE, "canvas size does not match the stitcher");
+    for (int i = 0; i < n_inputs; ++i) {
+      const hmp_image& im = inputs[i];
+      if (!im.data) return make_status(HMP_ERR_INVALID_DEVICE_POINTER, "input image is null");
+      if (im.width <= 0 || im.height <= 0 || im.pitch < size_t(im.width) * 4)
+        return make_status(HMP_ERR_INVALID_VALUE, "input image has an invalid size or pitch");
+      if (im.width >= 65535 || im.height >= 65535)
+        return make_status(HMP_ERR_INVALID_VALUE, "input images must be smaller than 65535 pixels per side");
+    }
+    int dev = -1;
+    cudaGetDevice(&dev);
+    if (dev != device) return make_status(HMP_ERR_INVALID_VALUE, "process() called on another device");
+
+    const hmp::SrcSet S = sources(inputs);
+    hmp::CanvasDev C;
+    C.ptr = static_cast<uchar4*>(canvas->data);
+    C.pitch = (long long)canvas->pitch;
+    C.bstride = (long long)canvas->pitch * canvas->height;
+    C.w = canvas->width;
+    C.h = canvas->height;
+    const bool vec = (reinterpret_cast<uintptr_t>(canvas->data) % 16 == 0) && (canvas->pitch % 16 == 0);
+
+    hmp::GatherArgs ga{};
+    if (p.canvas_plane_used) {
+      ga.S = S;
+      ga.P = canvas_plane;
+      ga.C = C;
+      ga.batch = p.batch;
+      ga.opaque = p.canvas_opaque ? 1 : 0;
+      if (p.levels > 0) {
+        ga.skip_x0 = p.write.x;
+        ga.skip_y0 = p.write.y;
+        ga.skip_x1 = p.write.x + p.write.w;
+        ga.skip_y1 = p.write.y + p.write.h;
+      }
+    }
+    cudaError_t e;
+    if (p.levels == 0) {
+      tbegin(0, s);
+      e = hmp::launch_canvas_gather(ga, vec, s);
+      tend(0, s);
+      if (timing && tnext < kTimingSlots) ++tnext;
+      if (e != cudaSuccess) return cuda_status(e, "canvas_gather launch");
+      return ok_status();
+    }
+    const bool fork = p.canvas_plane_used;
+    if (fork) {
+      e = cudaEventRecord(ev_fork, s);
+      if (e == cudaSuccess) e = cudaStreamWaitEvent(aux, ev_fork, 0);
+      tbegin(0, aux);
+      if (e == cudaSuccess) e = hmp::launch_canvas_gather(ga, vec, aux);
+      tend(0, aux);
+      if (e != cudaSuccess) return cuda_status(e, "canvas_gather launch");
+    }
+    hmp::PyrArgs a{};
+    a.S = S;
+    for (int k = 0; k < p.n; ++k) a.slot[k] = slot_planes[k];
+    a.n = p.n;
+    a.levels = p.levels;
+    for (int l = 0; l < p.levels; ++l) {
+      a.lw[l] = p.lw[l];
+      a.lh[l] = p.lh[l];
+      a.maskL[l] = maskL[l];
+      for (int k = 0; k < p.n; ++k) a.G[k][l] = G[k][l];
+    }
+    a.mask0 = mask0;
+    a.mask0_pitch = mask0_pitch;
+    a.K = p.mask_k;
+    a.opaque = p.slot_opaque ? 1 : 0;
+    a.C = C;
+    a.wx0 = p.write.x - p.blend.x;
+    a.wy0 = p.write.y - p.blend.y;
+    a.wx1 = a.wx0 + p.write.w;
+    a.wy1 = a.wy0 + p.write.h;
+    a.cx_off = p.blend.x;
+    a.cy_off = p.blend.y;
+    a.rm_odd = rm_odd;
+    a.rm_even = rm_even;
+    if (p.levels > 1) {
+      a.tile = tile_down;
+      const dim3 grid((p.lw[0] + tile_down - 1) / tile_down, (p.lh[0] + tile_down - 1) / tile_down, p.batch);
+      tbegin(1, s);
+      e = hmp::launch_pyr_down(a, p.storage, grid, s);
+      tend(1, s);
+      if (e != cudaSuccess) return cuda_status(e, "pyr_down launch");
+    }
+    a.tile = tile_up;
+    a.tx0 = a.wx0 / tile_up;
+    a.ty0 = a.wy0 / tile_up;
+    const int tx1 = (a.wx1 + tile_up - 1) / tile_up, ty1 = (a.wy1 + tile_up - 1) / tile_up;
+    const dim3 grid(tx1 - a.tx0, ty1 - a.ty0, p.batch);
+    tbegin(2, s);
+    e = hmp::launch_pyr_up(a, p.rule, p.storage, grid, up_smem, s);
+    tend(2, s);
+    if (timing && tnext < kTimingSlots) ++tnext;
+    if (e != cudaSuccess) return cuda_status(e, "pyr_up launch");
+    if (fork) {
+      e = cudaEventRecord(ev_join, aux);
+      if (e == cudaSuccess) e = cudaStreamWaitEvent(s, ev_join, 0);
+      if (e != cudaSuccess) return cuda_status(e, "stream join");
+    }
+    return ok_status();
+  }
+};
+
+extern "C" {
+
+HMP_API const char* hmp_version(void) { return "hmpano-gb300 0.1 (sm_103a)"; }
+
+HMP_API hmp_status hmp_stitcher_create(const hmp_config* cfg, hmp_stitcher** out) {
+  if (out) *out = nullptr;
+  if (!cfg) return make_status(HMP_ERR_INVALID_VALUE, "config is null");
+  hmp_stitcher* st = new (std::nothrow) hmp_stitcher();
+  if (!st) return make_status(HMP_ERR_MEMORY_ALLOCATION, "out of host memory");
+  std::string msg;
+  int rc = HMP_OK;
+  try {
+    rc = hmp::build_plan(*cfg, st->plan, msg);
+  } catch (const std::bad_alloc&) {
+    rc = HMP_ERR_MEMORY_ALLOCATION;
+    msg = "out of host memory while planning";
+  }
+  if (rc != HMP_OK)
+    st->status = make_status(rc, msg);
+  else
+    st->status = st->setup();
+  if (st->status.code != HMP_OK) {
+    // Release device memory now; keep the object for its sticky status.
+    for (void* p : st->allocations) cudaFree(p);
+    st->allocations.clear();
+  }
+  if (out)
+    *out = st;
+  else if (st->status.code != HMP_OK) {
+    hmp_status s = st->status;
+    delete st;
+    return s;
+  }
+  return st->status;
+}
+
+HMP_API void hmp_stitcher_destroy(hmp_stitcher* st) { delete st; }
+
+HMP_API hmp_status hmp_stitcher_status(const hmp_stitcher* st) {
+  if (!st) return make_status(HMP_ERR_INVALID_VALUE, "stitcher is null");
+  return st->status;
+}
+
+HMP_API int hmp_stitcher_canvas_width(const hmp_stitcher* st) { return st ? st->plan.canvas_w : 0; }
+HMP_API int hmp_stitcher_canvas_height(const hmp_stitcher* st) { return st ? st->plan.canvas_h : 0; }
+HMP_API int hmp_stitcher_batch_size(const hmp_stitcher* st) { return st ? st->plan.batch : 0; }
+
+HMP_API hmp_status hmp_stitcher_get_info(const hmp_stitcher* st, hmp_stitcher_info* info) {
+  if (!st || !info) return make_status(HMP_ERR_INVALID_VALUE, "null argument");
+  const hmp::Plan& p = st->plan;
+  std::memset(info, 0, sizeof(*info));
+  info->canvas_width = p.canvas_w;
+  info->canvas_height = p.canvas_h;
+  info->batch_size = p.batch;
+  info->n_images = p.n;
+  info->levels = p.levels;
+  const int br[4] = {p.blend.x, p.blend.y, p.blend.w, p.blend.h};
+  const int wr[4] = {p.write.x, p.write.y, p.write.w, p.write.h};
+  std::memcpy(info->blend_rect, br, sizeof(br));
+  std::memcpy(info->write_rect, wr, sizeof(wr));
+  info->tile_down = st->tile_down;
+  info->tile_up = st->tile_up;
+  info->launches_per_process = st->launches;
+  info->m0_bytes = st->m0_bytes;
+  info->device_bytes = double(st->device_bytes);
+  return st->status;
+}
+
+HMP_API hmp_status hmp_stitcher_process(hmp_stitcher* st, const hmp_image* inputs, int n_inputs,
+                                        const hmp_image* canvas, void* stream) {
+  if (!st) return make_status(HMP_ERR_INVALID_VALUE, "stitcher is null");
+  if (st->status.code != HMP_OK) return st->status;
+  hmp_status s = st->process(inputs, n_inputs, canvas, static_cast<cudaStream_t>(stream));
+  if (s.code != HMP_OK) st->status = s;
+  return s;
+}
+
+HMP_API hmp_status hmp_stitcher_set_timing(hmp_stitcher* st, int enable) {
+  if (!st) return make_status(HMP_ERR_INVALID_VALUE, "stitcher is null");
+  const cudaError_t e = st->timing_enable(enable != 0);
+  if (e != cudaSuccess) return cuda_status(e, "timing events");
+  return ok_status();
+}
+
+HMP_API hmp_status hmp_stitcher_get_timing(hmp_stitcher* st, hmp_kernel_timing* out) {
+  if (!st || !out) return make_status(HMP_ERR_INVALID_VALUE, "null argument");
+  const cudaError_t e = st->timing_collect(out);
+  if (e != cudaSuccess) return cuda_status(e, "timing events");
+  return ok_status();
+}
+
+HMP_API hmp_status hmp_plan_geometry(const hmp_config* cfg, int* canvas_w, int* canvas_h, int* out9) {
+  if (!cfg) return make_status(HMP_ERR_INVALID_VALUE, "config is null");
+  hmp::Plan p;
+  std::string msg;
+  const int rc = hmp::plan_geometry(*cfg, p, msg);
+  if (rc != HMP_OK) return make_status(rc, msg);
+  if (canvas_w) *canvas_w = p.canvas_w;
+  if (canvas_h) *canvas_h = p.canvas_h;
+  if (out9) {
+    const int v[9] = {p.blend.x, p.blend.y, p.blend.w, p.blend.h, p.write.x, p.write.y, p.write.w, p.write.h, p.levels};
+    std::memcpy(out9, v, sizeof(v));
+  }
+  return ok_status();
+}
+
+}  // extern "C"

@@ -1,0 +1,32 @@
+"""hmpano -- GB300-native (sm_103a) implementation of hm-cupano's per-frame stitching path.
+
+The stitch itself runs in libhmpano.so (CUDA kernels behind the C ABI of include/hmpano.h);
+this package mirrors the reference's Python/C++ stitcher API on top of it.
+"""
+from .pano import (
+    UNMAPPED_POSITION_VALUE,
+    ControlMasks,
+    ControlMasks3,
+    ControlMasksN,
+    CudaStatus,
+    CudaStatusError,
+    CudaStitchPano,
+    CudaStitchPano3,
+    CudaStitchPanoN,
+    SpatialTiff,
+    plan_geometry,
+)
+
+__all__ = [
+    "ControlMasks",
+    "ControlMasks3",
+    "ControlMasksN",
+    "CudaStatus",
+    "CudaStatusError",
+    "CudaStitchPano",
+    "CudaStitchPano3",
+    "CudaStitchPanoN",
+    "SpatialTiff",
+    "UNMAPPED_POSITION_VALUE",
+    "plan_geometry",
+]

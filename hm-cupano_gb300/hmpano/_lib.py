@@ -1,0 +1,113 @@
+"""ctypes declarations of the C ABI in include/hmpano.h (libhmpano.so).
+
+The library is loaded from this package's ``lib/`` directory (built in-tree by build.py). There is
+no fallback: if the library is missing the import of the stitcher classes fails loudly.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from pathlib import Path
+
+PKG_ROOT = Path(__file__).resolve().parents[1]
+LIB_PATH = Path(os.environ.get("HMPANO_LIB", PKG_ROOT / "lib" / "libhmpano.so"))
+
+KIND_PANON = 1
+KIND_PANO2 = 2
+KIND_PANO3 = 3
+STORAGE_F32 = 0
+STORAGE_F16 = 1
+FILTER_REFBOX = 0
+FILTER_BINOMIAL5 = 1
+
+
+class Status(C.Structure):
+    _fields_ = [("code", C.c_int), ("message", C.c_char * 252)]
+
+
+class Remap(C.Structure):
+    _fields_ = [
+        ("map_x", C.POINTER(C.c_uint16)),
+        ("map_y", C.POINTER(C.c_uint16)),
+        ("width", C.c_int),
+        ("height", C.c_int),
+        ("xpos", C.c_int),
+        ("ypos", C.c_int),
+    ]
+
+
+class Config(C.Structure):
+    _fields_ = [
+        ("kind", C.c_int),
+        ("n_images", C.c_int),
+        ("num_levels", C.c_int),
+        ("batch_size", C.c_int),
+        ("channels", C.c_int),
+        ("minimize_blend", C.c_int),
+        ("fused", C.c_int),
+        ("storage", C.c_int),
+        ("filter", C.c_int),
+        ("remaps", C.POINTER(Remap)),
+        ("seam", C.POINTER(C.c_uint8)),
+        ("seam_width", C.c_int),
+        ("seam_height", C.c_int),
+    ]
+
+
+class Image(C.Structure):
+    _fields_ = [("data", C.c_void_p), ("width", C.c_int), ("height", C.c_int), ("pitch", C.c_size_t)]
+
+
+class StitcherInfo(C.Structure):
+    _fields_ = [
+        ("canvas_width", C.c_int),
+        ("canvas_height", C.c_int),
+        ("batch_size", C.c_int),
+        ("n_images", C.c_int),
+        ("levels", C.c_int),
+        ("blend_rect", C.c_int * 4),
+        ("write_rect", C.c_int * 4),
+        ("tile_down", C.c_int),
+        ("tile_up", C.c_int),
+        ("launches_per_process", C.c_int),
+        ("m0_bytes", C.c_double),
+        ("device_bytes", C.c_double),
+    ]
+
+
+class KernelTiming(C.Structure):
+    _fields_ = [("total_ms", C.c_double * 3), ("launches", C.c_longlong * 3)]
+
+
+# Every symbol include/hmpano.h declares, with its signature.
+SIGNATURES = {
+    "hmp_version": ([], C.c_char_p),
+    "hmp_stitcher_create": ([C.POINTER(Config), C.POINTER(C.c_void_p)], Status),
+    "hmp_stitcher_destroy": ([C.c_void_p], None),
+    "hmp_stitcher_status": ([C.c_void_p], Status),
+    "hmp_stitcher_canvas_width": ([C.c_void_p], C.c_int),
+    "hmp_stitcher_canvas_height": ([C.c_void_p], C.c_int),
+    "hmp_stitcher_batch_size": ([C.c_void_p], C.c_int),
+    "hmp_stitcher_get_info": ([C.c_void_p, C.POINTER(StitcherInfo)], Status),
+    "hmp_stitcher_process": ([C.c_void_p, C.POINTER(Image), C.c_int, C.POINTER(Image), C.c_void_p], Status),
+    "hmp_stitcher_set_timing": ([C.c_void_p, C.c_int], Status),
+    "hmp_stitcher_get_timing": ([C.c_void_p, C.POINTER(KernelTiming)], Status),
+    "hmp_plan_geometry": ([C.POINTER(Config), C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)], Status),
+}
+
+_lib = None
+
+
+def lib() -> C.CDLL:
+    """Load libhmpano.so (raises if it has not been built)."""
+    global _lib
+    if _lib is None:
+        if not LIB_PATH.exists():
+            raise ImportError(f"libhmpano.so not found at {LIB_PATH}; run hm-cupano_gb300/build.py")
+        L = C.CDLL(str(LIB_PATH))
+        for name, (args, res) in SIGNATURES.items():
+            fn = getattr(L, name)
+            fn.argtypes = args
+            fn.restype = res
+        _lib = L
+    return _lib

@@ -1,0 +1,352 @@
+"""Python mirror of the reference's stitcher API over the C ABI.
+
+Same class names, constructor arguments, ``process`` signatures and error behaviour as the
+reference's ``cupano`` package (cupano/pano.py:127-911, cupano/masks.py) and its C++ classes
+(src/pano/cudaPano.h, cudaPano3.h, cudaPanoN.h):
+
+* ``ControlMasks`` / ``ControlMasks3`` / ``ControlMasksN`` hold the already-loaded remap tables,
+  positions and seam (two-image seams in the reference's inverted form, 1 = image 1);
+* a stitcher whose masks are invalid keeps an error ``status`` instead of raising at
+  construction, and ``process`` raises ``CudaStatusError`` while the status is not ok;
+* ``process`` takes RGBA uint8 CUDA tensors ``[B, H, W, 4]`` (or ``[H, W, 4]``) and returns the
+  canvas tensor (allocated when not given).
+
+Every stitch runs in libhmpano.so's sm_103a kernels; torch only supplies device memory and the
+current stream.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass, field
+from typing import Iterable, Sequence
+
+import numpy as np
+
+from . import _lib
+from ._lib import Config, Image, Remap, Status, StitcherInfo
+
+UNMAPPED_POSITION_VALUE = np.uint16(65535)
+
+
+@dataclass
+class SpatialTiff:
+    xpos: float
+    ypos: float
+
+
+@dataclass(frozen=True)
+class CudaStatus:
+    code: int = 0
+    message: str = ""
+
+    def ok(self) -> bool:
+        return self.code == 0
+
+
+class CudaStatusError(RuntimeError):
+    def __init__(self, status: CudaStatus):
+        self.status = status
+        super().__init__(status.message or f"CudaStatus(code={status.code})")
+
+
+def _status(s: Status) -> CudaStatus:
+    return CudaStatus(int(s.code), s.message.decode(errors="replace"))
+
+
+def _normalize_positions(positions: Sequence[SpatialTiff]) -> list[tuple[int, int]]:
+    return [(int(p.xpos), int(p.ypos)) for p in positions]
+
+
+@dataclass
+class ControlMasks:
+    """Two-image control data (src/pano/controlMasks.h:30-66)."""
+
+    img1_col: np.ndarray = field(default_factory=lambda: np.empty((0, 0), np.uint16))
+    img1_row: np.ndarray = field(default_factory=lambda: np.empty((0, 0), np.uint16))
+    img2_col: np.ndarray = field(default_factory=lambda: np.empty((0, 0), np.uint16))
+    img2_row: np.ndarray = field(default_factory=lambda: np.empty((0, 0), np.uint16))
+    whole_seam_mask_image: np.ndarray = field(default_factory=lambda: np.empty((0, 0), np.uint8))
+    positions: list = field(default_factory=list)
+
+    def is_valid(self) -> bool:
+        return bool(self.img1_col.size and self.img1_row.size and self.img2_col.size and self.img2_row.size
+                    and self.whole_seam_mask_image.size and len(self.positions) == 2)
+
+    def canvas_width(self) -> int:
+        return int(max(self.positions[0].xpos + self.img1_col.shape[1], self.positions[1].xpos + self.img2_col.shape[1]))
+
+    def canvas_height(self) -> int:
+        return int(max(self.positions[0].ypos + self.img1_col.shape[0], self.positions[1].ypos + self.img2_col.shape[0]))
+
+    def _tables(self):
+        return [self.img1_col, self.img2_col], [self.img1_row, self.img2_row], self.whole_seam_mask_image
+
+
+@dataclass
+class ControlMasks3:
+    """Three-image control data (src/pano/controlMasks3.h); the seam holds labels 0, 1, 2."""
+
+    img0_col: np.ndarray = field(default_factory=lambda: np.empty((0, 0), np.uint16))
+    img0_row: np.ndarray = field(default_factory=lambda: np.empty((0, 0), np.uint16))
+    img1_col: np.ndarray = field(default_factory=lambda: np.empty((0, 0), np.uint16))
+    img1_row: np.ndarray = field(default_factory=lambda: np.empty((0, 0), np.uint16))
+    img2_col: np.ndarray = field(default_factory=lambda: np.empty((0, 0), np.uint16))
+    img2_row: np.ndarray = field(default_factory=lambda: np.empty((0, 0), np.uint16))
+    whole_seam_mask_image: np.ndarray = field(default_factory=lambda: np.empty((0, 0), np.uint8))
+    positions: list = field(default_factory=list)
+
+    def is_valid(self) -> bool:
+        return bool(all(a.size for a in (self.img0_col, self.img0_row, self.img1_col, self.img1_row, self.img2_col,
+                                          self.img2_row, self.whole_seam_mask_image)) and len(self.positions) == 3)
+
+    def _tables(self):
+        return ([self.img0_col, self.img1_col, self.img2_col], [self.img0_row, self.img1_row, self.img2_row],
+                self.whole_seam_mask_image)
+
+
+@dataclass
+class ControlMasksN:
+    """N-image control data (src/pano/controlMasksN.h); the seam holds labels 0..N-1."""
+
+    img_col: list = field(default_factory=list)
+    img_row: list = field(default_factory=list)
+    whole_seam_mask_indexed: np.ndarray = field(default_factory=lambda: np.empty((0, 0), np.uint8))
+    positions: list = field(default_factory=list)
+
+    def is_valid(self) -> bool:
+        return bool(self.img_col and len(self.img_col) == len(self.img_row) and len(self.positions) == len(self.img_col)
+                    and self.whole_seam_mask_indexed.size > 0)
+
+    def canvas_width(self) -> int:
+        return int(max(p.xpos + m.shape[1] for p, m in zip(self.positions, self.img_col)))
+
+    def canvas_height(self) -> int:
+        return int(max(p.ypos + m.shape[0] for p, m in zip(self.positions, self.img_row)))
+
+    @staticmethod
+    def split_to_channels(indexed: np.ndarray, n_images: int) -> np.ndarray:
+        return np.stack([(indexed == i).astype(np.uint8) for i in range(n_images)], axis=-1)
+
+    def _tables(self):
+        return list(self.img_col), list(self.img_row), self.whole_seam_mask_indexed
+
+
+_STORAGE = {"f32": _lib.STORAGE_F32, "fp32": _lib.STORAGE_F32, "f16": _lib.STORAGE_F16, "fp16": _lib.STORAGE_F16}
+_FILTER = {"refbox": _lib.FILTER_REFBOX, "box": _lib.FILTER_REFBOX, "binomial5": _lib.FILTER_BINOMIAL5}
+
+
+def build_config(kind: int, control_masks, num_levels: int, batch_size: int, minimize_blend: bool = True,
+                 fused: bool = True, storage: str = "f32", filter: str = "refbox"):
+    """Marshal control masks into an hmp_config; returns (config, keep-alive list)."""
+    cols, rows, seam = control_masks._tables()
+    positions = _normalize_positions(control_masks.positions)
+    n = len(cols)
+    keep = []
+    remaps = (Remap * n)()
+    for i in range(n):
+        mx = np.ascontiguousarray(cols[i], dtype=np.uint16)
+        my = np.ascontiguousarray(rows[i], dtype=np.uint16)
+        if mx.shape != my.shape:
+            raise ValueError(f"remap x/y tables of image {i} differ in shape")
+        keep += [mx, my]
+        remaps[i] = Remap(mx.ctypes.data_as(C.POINTER(C.c_uint16)), my.ctypes.data_as(C.POINTER(C.c_uint16)),
+                          int(mx.shape[1]), int(mx.shape[0]), positions[i][0], positions[i][1])
+    seam_u8 = np.ascontiguousarray(seam, dtype=np.uint8)
+    keep += [seam_u8, remaps]
+    cfg = Config(kind, n, int(num_levels), int(batch_size), 4, int(bool(minimize_blend)), int(bool(fused)),
+                 _STORAGE[storage.lower()], _FILTER[filter.lower()], remaps,
+                 seam_u8.ctypes.data_as(C.POINTER(C.c_uint8)), int(seam_u8.shape[1]) if seam_u8.ndim == 2 else 0,
+                 int(seam_u8.shape[0]) if seam_u8.ndim == 2 else 0)
+    return cfg, keep
+
+
+def _ensure_batched(t):
+    if t.dim() == 3:
+        return t.unsqueeze(0)
+    if t.dim() != 4:
+        raise ValueError(f"Expected HWC or BHWC tensor, got shape {tuple(t.shape)}")
+    return t
+
+
+def _image(t) -> Image:
+    """hmp_image over a [B, H, W, 4] uint8 CUDA tensor with dense rows and frames."""
+    import torch
+
+    if t.dtype != torch.uint8 or t.shape[-1] != 4:
+        raise ValueError("images must be RGBA uint8 tensors [B, H, W, 4]")
+    if not t.is_cuda:
+        raise ValueError("images must live on a CUDA device")
+    B, H, W, _ = t.shape
+    if t.stride(3) != 1 or t.stride(2) != 4 or t.stride(0) != t.stride(1) * H:
+        raise ValueError("images need dense RGBA rows and frames (row pitch may exceed 4*W)")
+    return Image(C.c_void_p(t.data_ptr()), int(W), int(H), int(t.stride(1)))
+
+
+class _Stitcher:
+    _kind = 0
+
+    def __init__(self, control_masks, num_levels: int, batch_size: int, quiet: bool, minimize_blend: bool,
+                 fused: bool, storage: str, filter: str):
+        self._handle = C.c_void_p()
+        self._status = CudaStatus()
+        self._batch = int(batch_size)
+        if not control_masks.is_valid():
+            self._status = CudaStatus(301, "Stitching masks were not able to be loaded")
+            return
+        cfg, keep = build_config(self._kind, control_masks, num_levels, batch_size, minimize_blend, fused, storage,
+                                 filter)
+        s = _lib.lib().hmp_stitcher_create(C.byref(cfg), C.byref(self._handle))
+        del keep
+        self._status = _status(s)
+        if not quiet and self._status.ok():
+            print(f"Stitched canvas size: {self.canvas_width()} x {self.canvas_height()}")
+
+    def __del__(self):
+        h = getattr(self, "_handle", None)
+        if h:
+            try:
+                _lib.lib().hmp_stitcher_destroy(h)
+            except Exception:
+                pass
+            self._handle = C.c_void_p()
+
+    @property
+    def status(self) -> CudaStatus:
+        if self._handle:
+            return _status(_lib.lib().hmp_stitcher_status(self._handle))
+        return self._status
+
+    def canvas_width(self) -> int:
+        return int(_lib.lib().hmp_stitcher_canvas_width(self._handle)) if self._handle else 0
+
+    def canvas_height(self) -> int:
+        return int(_lib.lib().hmp_stitcher_canvas_height(self._handle)) if self._handle else 0
+
+    def batch_size(self) -> int:
+        return self._batch
+
+    def info(self) -> dict:
+        inf = StitcherInfo()
+        _lib.lib().hmp_stitcher_get_info(self._handle, C.byref(inf))
+        return {
+            "canvas": (inf.canvas_width, inf.canvas_height),
+            "levels": inf.levels,
+            "blend_rect": tuple(inf.blend_rect),
+            "write_rect": tuple(inf.write_rect),
+            "tile_down": inf.tile_down,
+            "tile_up": inf.tile_up,
+            "launches_per_process": inf.launches_per_process,
+            "m0_bytes": inf.m0_bytes,
+            "device_bytes": inf.device_bytes,
+        }
+
+    def set_timing(self, enable: bool) -> None:
+        """Record per-kernel CUDA-event times of subsequent process() calls."""
+        s = _status(_lib.lib().hmp_stitcher_set_timing(self._handle, int(bool(enable))))
+        if not s.ok():
+            raise CudaStatusError(s)
+
+    def kernel_times(self) -> dict:
+        """{kernel: (total_ms, launches)} since timing was enabled or last read."""
+        t = _lib.KernelTiming()
+        s = _status(_lib.lib().hmp_stitcher_get_timing(self._handle, C.byref(t)))
+        if not s.ok():
+            raise CudaStatusError(s)
+        names = ("canvas_gather", "pyr_down", "pyr_up")
+        return {names[i]: (float(t.total_ms[i]), int(t.launches[i])) for i in range(3)}
+
+    def _run(self, inputs: Sequence, canvas=None, stream=None):
+        import torch
+
+        st = self.status
+        if not st.ok():
+            raise CudaStatusError(st)
+        batched = [_ensure_batched(t) for t in inputs]
+        if any(t.shape[0] != self._batch for t in batched):
+            raise ValueError("Input batch size does not match stitcher batch size")
+        if any(t.shape[-1] not in (3, 4) for t in batched):
+            raise ValueError("Only 3- and 4-channel inputs are supported")
+        device = batched[0].device
+        if canvas is None:
+            canvas = torch.empty((self._batch, self.canvas_height(), self.canvas_width(), 4), dtype=torch.uint8,
+                                 device=device)
+        else:
+            canvas = _ensure_batched(canvas)
+            if canvas.shape[0] != self._batch:
+                raise ValueError("Canvas batch size does not match stitcher batch size")
+        imgs = (Image * len(batched))(*[_image(t) for t in batched])
+        cv = _image(canvas)
+        if stream is None:
+            stream = torch.cuda.current_stream(device).cuda_stream
+        elif hasattr(stream, "cuda_stream"):
+            stream = stream.cuda_stream
+        s = _lib.lib().hmp_stitcher_process(self._handle, imgs, len(batched), C.byref(cv), C.c_void_p(stream))
+        status = _status(s)
+        if not status.ok():
+            raise CudaStatusError(status)
+        return canvas
+
+
+class CudaStitchPano(_Stitcher):
+    """Two-image stitcher (src/pano/cudaPano.h:68-115, cupano/pano.py:127-551)."""
+
+    _kind = _lib.KIND_PANO2
+
+    def __init__(self, batch_size: int, num_levels: int, control_masks: ControlMasks, quiet: bool = False,
+                 minimize_blend: bool = True, max_output_width: int = 0, *, storage: str = "f32",
+                 filter: str = "refbox"):
+        del max_output_width
+        super().__init__(control_masks, num_levels, batch_size, quiet, minimize_blend, True, storage, filter)
+
+    def process(self, input_image_1, input_image_2, canvas=None, stream=None):
+        return self._run([input_image_1, input_image_2], canvas, stream)
+
+
+class CudaStitchPano3(_Stitcher):
+    """Three-image stitcher (src/pano/cudaPano3.h:64-182). ``fused`` picks the reference's fused
+    remap (invalid table entries leave pixels transparent) or its legacy remap+copy path."""
+
+    _kind = _lib.KIND_PANO3
+
+    def __init__(self, batch_size: int, num_levels: int, control_masks: ControlMasks3, quiet: bool = False,
+                 fused: bool = True, *, storage: str = "f32", filter: str = "refbox"):
+        super().__init__(control_masks, num_levels, batch_size, quiet, True, fused, storage, filter)
+
+    def process(self, input_image_0, input_image_1, input_image_2, canvas=None, stream=None):
+        return self._run([input_image_0, input_image_1, input_image_2], canvas, stream)
+
+
+class CudaStitchPanoN(_Stitcher):
+    """N-image stitcher, N in [2, 8] (src/pano/cudaPanoN.h:80-146, cupano/pano.py:553-911)."""
+
+    _kind = _lib.KIND_PANON
+
+    def __init__(self, batch_size: int, num_levels: int, control_masks: ControlMasksN, quiet: bool = False,
+                 minimize_blend: bool = True, *, storage: str = "f32", filter: str = "refbox"):
+        self._n = len(control_masks.img_col)
+        if control_masks.is_valid() and not 2 <= self._n <= 8:
+            self._handle = C.c_void_p()
+            self._batch = int(batch_size)
+            self._status = CudaStatus(1, "Unsupported N for blend (supported 2..8)")
+            return
+        super().__init__(control_masks, num_levels, batch_size, quiet, minimize_blend, True, storage, filter)
+
+    def process(self, inputs: Iterable, canvas=None, stream=None):
+        inputs = list(inputs)
+        if len(inputs) != self._n:
+            raise ValueError("inputs size != N")
+        return self._run(inputs, canvas, stream)
+
+
+def plan_geometry(kind: int, control_masks, num_levels: int, minimize_blend: bool = True) -> dict:
+    """Host-only geometry of a configuration (no GPU needed)."""
+    cfg, keep = build_config(kind, control_masks, num_levels, 1, minimize_blend)
+    cw, ch = C.c_int(), C.c_int()
+    out = (C.c_int * 9)()
+    s = _lib.lib().hmp_plan_geometry(C.byref(cfg), C.byref(cw), C.byref(ch), out)
+    del keep
+    st = _status(s)
+    if not st.ok():
+        raise CudaStatusError(st)
+    v = list(out)
+    return {"canvas": (cw.value, ch.value), "blend": tuple(v[0:4]), "write": tuple(v[4:8]), "levels": v[8]}

@@ -1,0 +1,180 @@
+/*
+ * hmpano.h -- C ABI of the GB300-native stitching path (libhmpano.so).
+ *
+ * This is the boundary a host program binds to (ctypes, cgo, JNI, N-API or plain C/C++). It
+ * replaces the per-frame stitcher objects of hm-cupano:
+ *
+ *   hmp_stitcher_create   <- hm::pano::cuda::CudaStitchPano<T,T>::CudaStitchPano(batch, levels,
+ *                            masks, quiet, minimize_blend)          src/pano/cudaPano.h:71-77
+ *                            CudaStitchPano3(batch, levels, masks)   src/pano/cudaPano3.h:70-75
+ *                            CudaStitchPanoN(batch, levels, masks, minimize_blend)
+ *                                                                    src/pano/cudaPanoN.h:83-88
+ *   hmp_stitcher_process  <- CudaStitchPano::process(in1, in2, stream, canvas)
+ *                                                                    src/pano/cudaPano.h:95-99
+ *                            CudaStitchPano3::process(in0, in1, in2, stream, canvas, fused)
+ *                                                                    src/pano/cudaPano3.h:99-107
+ *                            CudaStitchPanoN::process(inputs, stream, canvas)
+ *                                                                    src/pano/cudaPanoN.h:97-101
+ *   hmp_stitcher_status   <- CudaStitchPano*::status()               src/pano/cudaPano.h:101-103
+ *   hmp_stitcher_canvas_* <- canvas_width() / canvas_height()        src/pano/cudaPano.h:105-111
+ *   hmp_stitcher_destroy  <- ~CudaStitchPano*()
+ *
+ * Error convention (src/cuda/cudaStatus.h:12-75): every call returns an hmp_status whose code is
+ * a cudaError_t value (0 = success) with a message. Construction errors are also kept as the
+ * stitcher's sticky status; process() first returns the sticky status, then the per-call error,
+ * and a per-call error becomes sticky (src/pano/cudaPano.inl:460-472).
+ *
+ * Data: images are RGBA8 (uchar4), device memory, frame b of a batch at data + b*pitch*height.
+ * Remap tables, positions and the seam are host data consumed at create time (the ControlMasks
+ * of the reference, already loaded: the two-image seam is in its inverted form, 1 = image 1;
+ * the three/N-image seam holds labels 0..n-1). Positions are normalised (minimum 0).
+ *
+ * All device memory a stitcher needs is allocated by hmp_stitcher_create; process() allocates
+ * nothing, so it can be captured in a CUDA graph. One process() may be in flight per stitcher.
+ */
+#ifndef HMPANO_H
+#define HMPANO_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(__GNUC__)
+#define HMP_API __attribute__((visibility("default")))
+#else
+#define HMP_API
+#endif
+
+/* Stitcher kinds. */
+#define HMP_KIND_PANON 1 /* CudaStitchPanoN: 2..8 images, N-way blend */
+#define HMP_KIND_PANO2 2 /* CudaStitchPano: 2 images, two-image blend */
+#define HMP_KIND_PANO3 3 /* CudaStitchPano3: 3 images, three-way blend */
+
+/* Pyramid storage precision for levels >= 1 (arithmetic is always FP32). */
+#define HMP_STORAGE_F32 0
+#define HMP_STORAGE_F16 1
+
+/* Pyramid filter. */
+#define HMP_FILTER_REFBOX 0    /* the reference's 2x2 box downsample / bilinear upsample */
+#define HMP_FILTER_BINOMIAL5 1 /* 5-tap [1,4,6,4,1]/16, reflect-101 (no reference counterpart) */
+
+/* Status codes are cudaError_t values; these are the ones the library produces itself. */
+#define HMP_OK 0
+#define HMP_ERR_INVALID_VALUE 1        /* cudaErrorInvalidValue */
+#define HMP_ERR_MEMORY_ALLOCATION 2    /* cudaErrorMemoryAllocation */
+#define HMP_ERR_INVALID_DEVICE_POINTER 17 /* cudaErrorInvalidDevicePointer */
+#define HMP_ERR_FILE_NOT_FOUND 301     /* cudaErrorFileNotFound: masks not loaded (cudaPano.inl:28-31) */
+#define HMP_ERR_NOT_SUPPORTED 801      /* cudaErrorNotSupported */
+#define HMP_ERR_TIMEOUT 909            /* cudaErrorTimeout: a bounded wait gave up */
+
+typedef struct hmp_status {
+  int code;          /* cudaError_t value, 0 = success */
+  char message[252]; /* NUL-terminated */
+} hmp_status;
+
+typedef struct hmp_remap {
+  const uint16_t* map_x; /* host, row-major height x width, CV_16U; 65535 = unmapped */
+  const uint16_t* map_y;
+  int width;
+  int height;
+  int xpos; /* canvas position of the table's top-left corner */
+  int ypos;
+} hmp_remap;
+
+typedef struct hmp_config {
+  int kind;           /* HMP_KIND_* */
+  int n_images;       /* 2 (PANO2), 3 (PANO3), 2..8 (PANON) */
+  int num_levels;     /* 0 = hard seam; pyramid levels otherwise */
+  int batch_size;     /* frames per process() call */
+  int channels;       /* 4 (RGBA) */
+  int minimize_blend; /* PANO2 / PANON: blend only the seam region (reference default: 1) */
+  int fused;          /* PANO3: 1 = fused remap (reference default), 0 = legacy remap+copy */
+  int storage;        /* HMP_STORAGE_* */
+  int filter;         /* HMP_FILTER_* */
+  const hmp_remap* remaps; /* n_images entries */
+  const uint8_t* seam;     /* host, seam_height x seam_width */
+  int seam_width;
+  int seam_height;
+} hmp_config;
+
+typedef struct hmp_image {
+  void* data; /* device pointer, RGBA8 */
+  int width;
+  int height;
+  size_t pitch; /* bytes per row (>= 4*width); frame stride = pitch*height */
+} hmp_image;
+
+typedef struct hmp_stitcher hmp_stitcher;
+
+/* Geometry and cost model of a stitcher (for reports and tests). Rectangles are x, y, w, h in
+ * canvas pixels. */
+typedef struct hmp_stitcher_info {
+  int canvas_width;
+  int canvas_height;
+  int batch_size;
+  int n_images;
+  int levels;        /* effective pyramid levels (0 = hard seam) */
+  int blend_rect[4]; /* pyramid domain */
+  int write_rect[4]; /* region the pyramid writes back to the canvas */
+  int tile_down;     /* level-0 tile edge of the Gaussian-pyramid kernel */
+  int tile_up;       /* level-0 tile edge of the blend/reconstruct kernel */
+  int launches_per_process; /* kernels one process() launches */
+  double m0_bytes;   /* compulsory bytes per frame (maps, seam, sources, canvas) */
+  double device_bytes; /* device memory held by the stitcher */
+} hmp_stitcher_info;
+
+/* Library version string. */
+HMP_API const char* hmp_version(void);
+
+/* Construct a stitcher: validates the configuration, plans the per-pixel gather tables and
+ * allocates every device buffer. On failure *out is still set (unless NULL) to a stitcher
+ * object carrying the sticky error status, like the reference's constructors; pass it to
+ * hmp_stitcher_destroy. */
+HMP_API hmp_status hmp_stitcher_create(const hmp_config* cfg, hmp_stitcher** out);
+
+HMP_API void hmp_stitcher_destroy(hmp_stitcher* st);
+
+/* Sticky status (construction error or the first failed process()). */
+HMP_API hmp_status hmp_stitcher_status(const hmp_stitcher* st);
+
+HMP_API int hmp_stitcher_canvas_width(const hmp_stitcher* st);
+HMP_API int hmp_stitcher_canvas_height(const hmp_stitcher* st);
+HMP_API int hmp_stitcher_batch_size(const hmp_stitcher* st);
+HMP_API hmp_status hmp_stitcher_get_info(const hmp_stitcher* st, hmp_stitcher_info* info);
+
+/* Stitch one batch: inputs[0..n_inputs) -> canvas, enqueued on `stream` (a cudaStream_t; NULL =
+ * legacy default stream). Every canvas pixel is written, so the canvas needs no clearing. */
+HMP_API hmp_status hmp_stitcher_process(hmp_stitcher* st, const hmp_image* inputs, int n_inputs,
+                                        const hmp_image* canvas, void* stream);
+
+/* Per-kernel device time of process() calls made while timing is enabled, measured with CUDA
+ * events recorded on the stream each kernel is launched on (the canvas gather runs on the
+ * stitcher's auxiliary stream). Index 0 = canvas_gather, 1 = pyr_down, 2 = pyr_up. */
+typedef struct hmp_kernel_timing {
+  double total_ms[3];
+  long long launches[3];
+} hmp_kernel_timing;
+
+/* Enable (1) or disable (0) per-kernel event timing; enabling clears the accumulated times.
+ * At most 4096 process() calls are recorded between two hmp_stitcher_get_timing() calls. */
+HMP_API hmp_status hmp_stitcher_set_timing(hmp_stitcher* st, int enable);
+
+/* Accumulated kernel times since timing was enabled or last read; waits for the recorded
+ * events, then resets the accumulators. No counterpart in the reference (its benchmark times
+ * whole frames with a host clock, tests/testCudaBlend.cpp:224-241). */
+HMP_API hmp_status hmp_stitcher_get_timing(hmp_stitcher* st, hmp_kernel_timing* out);
+
+/* Geometry of a configuration computed on the host only (no device work): blend rect, write
+ * rect and effective levels, out9 = {bx, by, bw, bh, wx, wy, ww, wh, levels}; also the canvas
+ * size. Mirrors CanvasManager::updateMinimizeBlend / convertMaskMat (src/pano/canvasManager.cpp:
+ * 16-101) and the N-image ROI logic (src/pano/cudaPanoN.inl:156-190). */
+HMP_API hmp_status hmp_plan_geometry(const hmp_config* cfg, int* canvas_w, int* canvas_h, int* out9);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* HMPANO_H */

@@ -1,0 +1,155 @@
+"""Host-side checks of libhmpano.so that need no GPU: exported symbols, planning geometry
+against the oracle, and configuration errors (which are rejected before any device work)."""
+from __future__ import annotations
+
+import ctypes as C
+import re
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from helpers import masks_for_case, masks_for_rig
+
+REPO = Path(__file__).resolve().parents[1]
+
+
+@pytest.fixture(scope="module")
+def lib():
+    import sys
+
+    sys.path.insert(0, str(REPO / "hm-cupano_gb300"))
+    import build as hmp_build
+    from hmpano import _lib
+
+    hmp_build.build()
+    return _lib.lib()
+
+
+def _declared_symbols():
+    text = (REPO / "include" / "hmpano.h").read_text()
+    return sorted(set(re.findall(r"HMP_API\s+[\w\s\*]+?\b(hmp_\w+)\s*\(", text)))
+
+
+def test_library_exports_every_declared_symbol(lib):
+    names = _declared_symbols()
+    assert len(names) >= 10
+    from hmpano import _lib
+
+    for name in names:
+        assert hasattr(lib, name), name
+        assert name in _lib.SIGNATURES, f"{name} has no ctypes signature"
+
+
+def test_version(lib):
+    assert b"sm_103a" in lib.hmp_version()
+
+
+def test_plan_geometry_matches_oracle(golden, oracle_lib):
+    import hmpano
+
+    for name in [str(n) for n in golden["names"]]:
+        c = oracle_lib.load_golden_case(golden, name)
+        g = hmpano.plan_geometry(c["kind"], masks_for_case(c), c["levels"], c["minimize"])
+        st = oracle_lib.Stitch(c["kind"], c["map_x"], c["map_y"], c["pos_x"], c["pos_y"], c["seam"], c["levels"],
+                               c["batch"], c["minimize"])
+        assert g["canvas"] == (st.canvas_w, st.canvas_h), name
+        if c["levels"] > 0:
+            og = st.geometry()
+            assert g["blend"] == og["blend"] and g["write"] == og["write"] and g["levels"] == og["levels"], name
+
+
+@pytest.mark.parametrize("workload,kind,levels", [
+    ("pano2_1280x720_to_2200x800", 2, 0),
+    ("pano2_1280x720_to_2200x800", 2, 6),
+    ("panon8_2000x1500_to_9000x2400", 1, 6),
+    ("panon8_2000x1500_to_9000x2400", 1, 3),
+    ("pano3_2704x1520_to_6000x1800", 3, 6),
+])
+def test_plan_geometry_matches_oracle_on_workloads(oracle_lib, workload, kind, levels):
+    import hmpano
+    from hmpano import synth
+
+    rig = synth.workload_rig(workload, scale=0.25, kind=kind)
+    g = hmpano.plan_geometry(kind, masks_for_rig(rig), levels)
+    st = oracle_lib.Stitch.from_rig(rig, levels)
+    assert g["canvas"] == (st.canvas_w, st.canvas_h)
+    if levels:
+        og = st.geometry()
+        assert (g["blend"], g["write"], g["levels"]) == (og["blend"], og["write"], og["levels"])
+
+
+def _create(lib, masks, kind, levels, batch=1, **kw):
+    from hmpano import _lib
+    from hmpano.pano import build_config
+
+    cfg, keep = build_config(kind, masks, levels, batch, **kw)
+    h = C.c_void_p()
+    s = lib.hmp_stitcher_create(C.byref(cfg), C.byref(h))
+    st = lib.hmp_stitcher_status(h)
+    code = s.code
+    assert st.code == code  # the error is also the stitcher's sticky status
+    lib.hmp_stitcher_destroy(h)
+    return code, s.message.decode()
+
+
+def _two_image_masks(x2=200):
+    import hmpano
+
+    w, h = 400, 16
+    mx = np.tile(np.arange(w, dtype=np.uint16), (h, 1))
+    my = np.tile(np.arange(h, dtype=np.uint16)[:, None], (1, w))
+    m = hmpano.ControlMasks(mx, my, mx, my, np.ones((h, w + x2), np.uint8),
+                            [hmpano.SpatialTiff(0, 0), hmpano.SpatialTiff(x2, 0)])
+    return m
+
+
+def test_create_rejects_invalid_configurations(lib):
+    from hmpano import _lib
+
+    # no overlap between the two footprints (CanvasManager::updateMinimizeBlend)
+    code, msg = _create(lib, _two_image_masks(x2=400), _lib.KIND_PANO2, 0)
+    assert code == 1 and "overlap" in msg
+    # blend strip of +/-128 px does not fit the canvas (x2 - 128 < 0)
+    code, msg = _create(lib, _two_image_masks(x2=100), _lib.KIND_PANO2, 3)
+    assert code == 1 and "strip" in msg
+    # wrong image count for the two-image stitcher
+    import hmpano
+
+    m3 = hmpano.ControlMasksN([np.zeros((4, 4), np.uint16)] * 3, [np.zeros((4, 4), np.uint16)] * 3,
+                              np.zeros((4, 4), np.uint8), [hmpano.SpatialTiff(0, 0)] * 3)
+    code, _ = _create(lib, m3, _lib.KIND_PANO2, 0)
+    assert code == 1
+    # empty seam: masks not loaded (the reference's cudaErrorFileNotFound)
+    m = _two_image_masks()
+    m.whole_seam_mask_image = np.zeros((0, 0), np.uint8)
+    code, msg = _create(lib, m, _lib.KIND_PANO2, 0)
+    assert code == 301 and "masks" in msg
+    # seam larger than the canvas
+    m = _two_image_masks()
+    m.whole_seam_mask_image = np.ones((64, 2000), np.uint8)
+    code, _ = _create(lib, m, _lib.KIND_PANO2, 0)
+    assert code == 1
+    # too many images
+    m9 = hmpano.ControlMasksN([np.zeros((4, 4), np.uint16)] * 9, [np.zeros((4, 4), np.uint16)] * 9,
+                              np.zeros((4, 4), np.uint8), [hmpano.SpatialTiff(0, 0)] * 9)
+    code, msg = _create(lib, m9, _lib.KIND_PANON, 0)
+    assert code == 1 and "2..8" in msg
+    # more pyramid levels than one fused pass supports
+    w, h = 2048, 1024
+    mx = np.tile(np.arange(w, dtype=np.uint16), (h, 1))
+    my = np.tile(np.arange(h, dtype=np.uint16)[:, None], (1, w))
+    mN = hmpano.ControlMasksN([mx, mx], [my, my], np.zeros((h, w), np.uint8), [hmpano.SpatialTiff(0, 0)] * 2)
+    code, msg = _create(lib, mN, _lib.KIND_PANON, 9, minimize_blend=False)
+    assert code == 801 and "levels" in msg
+
+
+def test_python_mirror_keeps_invalid_masks_as_status():
+    import hmpano
+
+    pano = hmpano.CudaStitchPano(1, 0, hmpano.ControlMasks(), quiet=True)
+    assert not pano.status.ok() and pano.status.code == 301
+    with pytest.raises(hmpano.CudaStatusError):
+        pano.process(None, None)
+    panoN = hmpano.CudaStitchPanoN(1, 0, hmpano.ControlMasksN(), quiet=True)
+    assert not panoN.status.ok()
