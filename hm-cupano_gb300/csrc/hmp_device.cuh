@@ -63,6 +63,52 @@ __device__ __forceinline__ void store_level(half4* p, const float4 v) {
   *reinterpret_cast<uint2*>(p) = raw;
 }
 
+// Owner and packed table entry of one plane pixel (domain coordinates); owner 0xFF and entry
+// 0xFFFFFFFF outside the plane.
+__device__ __forceinline__ void plane_lookup(const PlaneDev& P, int x, int y, int& owner, uint32_t& entry) {
+  const int rx = x - P.x0, ry = y - P.y0;
+  owner = 0xFF;
+  entry = 0xFFFFFFFFu;
+  if ((unsigned)rx >= (unsigned)P.w || (unsigned)ry >= (unsigned)P.h) return;
+  owner = P.owner ? int(__ldg(P.owner + (long long)ry * P.owner_pitch + rx)) : P.default_owner;
+  entry = __ldg(P.map + (long long)ry * P.map_pitch + rx);
+}
+
+// Source pixel for (owner, entry): the source pixel when the entry lies inside the source;
+// otherwise zero, with alpha 255 under the soft-seam ("opaque") rule when the x entry is not the
+// 65535 sentinel (src/cuda/cudaRemap.cu:60-123).
+__device__ __forceinline__ uchar4 fetch_src(const SrcSet& S, int o, uint32_t e, int b, bool opaque) {
+  uchar4 out = make_uchar4(0, 0, 0, 0);
+  if (o >= kDevMaxImages) return out;
+  const int sx = int(e & 0xFFFFu), sy = int(e >> 16);
+  if (sx < S.w[o] && sy < S.h[o]) {
+    const char* base = reinterpret_cast<const char*>(S.ptr[o]) + b * S.bstride[o] + sy * S.pitch[o];
+    return __ldg(reinterpret_cast<const uchar4*>(base) + sx);
+  }
+  if (opaque && sx != 0xFFFF) out.w = 255;
+  return out;
+}
+
+// Source pixel of (owner, entry) with the owner resolved by a static select, so that the frame
+// table in the kernel parameters is only ever indexed by constants.
+template <int NMAX>
+__device__ __forceinline__ uchar4 fetch_sel(const SrcSet& S, int o, uint32_t e, int b, bool opaque) {
+  const int sx = int(e & 0xFFFFu), sy = int(e >> 16);
+  uchar4 out = make_uchar4(0, 0, 0, 0);
+#pragma unroll
+  for (int q = 0; q < NMAX; ++q) {
+    if (o == q) {
+      if (sx < S.w[q] && sy < S.h[q]) {
+        const char* base = reinterpret_cast<const char*>(S.ptr[q]) + b * S.bstride[q] + sy * S.pitch[q];
+        out = __ldg(reinterpret_cast<const uchar4*>(base) + sx);
+      } else if (opaque && sx != 0xFFFF) {
+        out.w = 255;
+      }
+    }
+  }
+  return out;
+}
+
 // Level-0 value of one plane pixel (domain coordinates), the reference's remap rule
 // (src/cuda/cudaRemap.cu:60-123): an entry inside the source gives the source pixel; otherwise
 // zero, with alpha 255 under the soft-seam ("opaque") rule when the x entry is not the 65535

@@ -15,6 +15,7 @@ struct GatherArgs {
   int batch;
   int skip_x0, skip_y0, skip_x1, skip_y1;  // pixels written by the pyramid (end exclusive)
   int opaque;
+  int n_owners;  // images the plane can select (owners are < n_owners)
 };
 
 // Shared by the Gaussian-pyramid (down) and blend/reconstruct (up) kernels.
@@ -31,8 +32,8 @@ struct PyrArgs {
   const float* maskL[kDevMaxLevels];      // level l >= 1: [lh][lw][K]
   int K;
   int opaque;
-  int tile;  // level-0 tile edge
-  int rm_odd, rm_even;  // smem region capacities (pixels) for odd / even levels
+  int tile;  // tile edge (level 0 for pyr_down, level 1 for pyr_coarse)
+  float4* R1;  // level-1 reconstruction [batch][lh1][lw1] (levels >= 2)
   CanvasDev C;
   int wx0, wy0, wx1, wy1;  // write rect, blend coordinates, end exclusive
   int cx_off, cy_off;      // canvas = blend + offset
@@ -42,15 +43,18 @@ struct PyrArgs {
 // One-time attribute setup (dynamic shared memory limits). Call before capture.
 cudaError_t kernels_init();
 
-cudaError_t launch_canvas_gather(const GatherArgs& a, bool vec, cudaStream_t stream);
+cudaError_t launch_canvas_gather(const GatherArgs& a, cudaStream_t stream);
 
 // Gaussian levels 1..L-1 of every slot; grid = tiles over the blend region x batch.
 cudaError_t launch_pyr_down(const PyrArgs& a, int storage, dim3 grid, cudaStream_t stream);
 
-// Blend + reconstruct + pack of the write rect; grid = up-tiles over the write rect x batch.
-cudaError_t launch_pyr_up(const PyrArgs& a, int rule, int storage, dim3 grid, size_t smem, cudaStream_t stream);
+// R^1 over the level-1 tiles the write rect needs; grid = level-1 tiles x batch (levels >= 2).
+cudaError_t launch_pyr_coarse(const PyrArgs& a, int rule, int storage, dim3 grid, size_t smem, cudaStream_t stream);
 
-size_t pyr_down_smem(int tile);
-size_t pyr_up_smem(int n, int rm_odd, int rm_even);
+// Level 0 of the write rect: blend + reconstruct + pack; grid = 64 x 16 pixel blocks x batch.
+cudaError_t launch_pyr_fine(const PyrArgs& a, int rule, int storage, dim3 grid, cudaStream_t stream);
+
+size_t pyr_down_smem(int n, int tile);
+size_t pyr_coarse_smem(int n, int k, int tile1, int levels);
 
 }  // namespace hmp

@@ -116,8 +116,10 @@ int validate(const hmp_config& c, std::string& m) {
 }
 
 // Crops a full-domain plane (dw x dh) to the bounding box of mapped pixels and drops the owner
-// array when all mapped pixels share one owner.
-GatherPlane crop_plane(std::vector<uint8_t>& owner, std::vector<uint32_t>& map, int dw, int dh) {
+// array when all mapped pixels share one owner equal to `implied_owner` (the owner the kernels
+// assume for a plane without an owner array).
+GatherPlane crop_plane(std::vector<uint8_t>& owner, std::vector<uint32_t>& map, int dw, int dh,
+                       int implied_owner) {
   GatherPlane p;
   int x0 = dw, y0 = dh, x1 = -1, y1 = -1;
   int first_owner = -1;
@@ -137,6 +139,7 @@ GatherPlane crop_plane(std::vector<uint8_t>& owner, std::vector<uint32_t>& map, 
         uniform = false;
     }
   if (x1 < 0) return p;  // nothing mapped
+  if (first_owner != implied_owner) uniform = false;
   p.rect = Rect{x0, y0, x1 - x0 + 1, y1 - y0 + 1};
   p.default_owner = first_owner;
   p.map.resize(size_t(p.rect.w) * p.rect.h);
@@ -346,7 +349,7 @@ int build_plan(const hmp_config& c, Plan& p, std::string& m) {
           map[d] = table_at(c, k, x, y);
         }
     }
-    p.slots[k] = crop_plane(owner, map, bw, bh);
+    p.slots[k] = crop_plane(owner, map, bw, bh, k);
     if (p.slots[k].rect.empty()) p.slots[k].default_owner = k;
   }
 

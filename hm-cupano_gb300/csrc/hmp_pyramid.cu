@@ -3,18 +3,23 @@
 // The reference runs ~6L launches per frame: a downsample and a mask downsample per level, a
 // Laplacian per image and level, a blend per level, a reconstruct per level, plus device copies
 // (src/cuda/cudaBlend.cu:847-1049, cudaBlend3.cu:881-1206, cudaBlendN.cu:649-828). Here the whole
-// pyramid is two launches:
+// pyramid is three launches:
 //
 //  * pyr_down: the 2x2 box downsample has no halo, so a CTA that owns an aligned T x T level-0
 //    tile (T a multiple of 2^(L-1)) builds every Gaussian level of that tile in shared memory,
 //    gathering level 0 straight from the sources through the slot planes (remap + level-0
 //    downsample fused). Levels >= 1 go to HBM (FP32 or FP16 storage).
-//  * pyr_up: a CTA that owns a level-0 tile of the write region walks from the coarsest level
-//    down. At level l it needs its tile plus a 1-2 pixel halo (the bilinear upsample reads
-//    floor(x/2) and floor(x/2)+1), so it loads G_k^l of every image for that region, forms the
-//    Laplacians G_k^l - up(G_k^{l+1}), blends them with the mask pyramid, adds up(R^{l+1}) and
-//    keeps R^l in shared memory. At level 0 it packs straight into the canvas. Laplacians,
-//    blended levels and reconstructions never touch HBM.
+//  * pyr_coarse: a CTA that owns a tile of level-1 pixels loads, all at once, every coarser level
+//    it needs (its tile plus a 1-2 pixel halo per level: the bilinear upsample reads floor(x/2)
+//    and floor(x/2)+1) into shared memory and walks from the coarsest level down: Laplacians
+//    G_k^l - up(G_k^{l+1}), the seam-weighted blend, R^l = up(R^{l+1}) + blend. It writes R^1.
+//  * pyr_fine: level 0 (three quarters of the pixels) as a streaming kernel: gather the level-0
+//    pixels through the slot planes, Laplacians against up(G_k^1), blend, add up(R^1), pack
+//    into the canvas. Laplacians and blended levels never touch HBM.
+//
+// Tile edges are template parameters and level loops are unrolled, so shared-memory strides and
+// per-level geometry are compile-time constants or registers (no local memory, no integer
+// division by runtime values).
 //
 // Arithmetic follows the reference order exactly (this file is compiled with -fmad=false so no
 // product is fused into a sum): downsample sums in (0,0),(1,0),(0,1),(1,1) order divided by the
@@ -26,6 +31,17 @@ namespace hmp {
 namespace {
 
 constexpr int kRuleNway = 1, kRuleTwo = 2, kRuleThree = 3;
+constexpr int kL = kDevMaxLevels;
+
+// Table lookup of slot k at (x, y); the owner is k unless the slot has an owner plane.
+__device__ __forceinline__ void slot_lookup(const PlaneDev& P, int k, int x, int y, int& owner, uint32_t& entry) {
+  const int rx = x - P.x0, ry = y - P.y0;
+  owner = 0xFF;
+  entry = 0xFFFFFFFFu;
+  if ((unsigned)rx >= (unsigned)P.w || (unsigned)ry >= (unsigned)P.h) return;
+  owner = P.owner ? int(__ldg(P.owner + (long long)ry * P.owner_pitch + rx)) : k;
+  entry = __ldg(P.map + (long long)ry * P.map_pitch + rx);
+}
 
 // Alpha-aware 2x2 mean of four level-l pixels (src/cuda/cudaBlend.cu:46-144).
 struct DownAcc {
@@ -47,114 +63,152 @@ struct DownAcc {
   }
 };
 
-template <typename Store>
+// Gaussian levels 1..L-1 of every slot for one TD x TD level-0 tile. Level 1 is gathered straight
+// from the sources (all slots' table lookups first, then all source loads, then the reductions);
+// deeper levels reduce the previous level in shared memory. A slot whose plane misses the tile
+// produces zeros, which its level buffers already hold, so it is skipped entirely.
+template <int NMAX, typename Store, int TD>
 __global__ void __launch_bounds__(256) pyr_down_kernel(const __grid_constant__ PyrArgs a) {
+  constexpr int T1 = TD / 2, T2 = TD / 4;
   extern __shared__ float4 sm[];
-  const int TD = a.tile, T1 = TD >> 1;
-  float4* bufA = sm;
-  float4* bufB = sm + T1 * T1;
+  const int n = a.n;
+  float4* bufA = sm;                // levels 1, 3, 5: [n][T1*T1]
+  float4* bufB = sm + n * T1 * T1;  // levels 2, 4, 6: [n][T2*T2]
   const int b = blockIdx.z;
   const int X0 = blockIdx.x * TD, Y0 = blockIdx.y * TD;
   const bool opaque = a.opaque != 0;
   const int L = a.levels;
-  for (int k = 0; k < a.n; ++k) {
+  bool active[NMAX];
+#pragma unroll
+  for (int k = 0; k < NMAX; ++k) {
     const PlaneDev& P = a.slot[k];
-    // A tile that misses the slot's rect only produces zeros, which the buffers already hold.
-    if (X0 >= P.x0 + P.w || Y0 >= P.y0 + P.h || X0 + TD <= P.x0 || Y0 + TD <= P.y0) continue;
-    // Level 1 straight from the sources.
-    {
-      Store* G1 = static_cast<Store*>(a.G[k][1]) + (long long)b * a.lw[1] * a.lh[1];
-      for (int i = threadIdx.x; i < T1 * T1; i += blockDim.x) {
-        const int tx = i % T1, ty = i / T1;
-        const int gx = (X0 >> 1) + tx, gy = (Y0 >> 1) + ty;
-        float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-        if (gx < a.lw[1] && gy < a.lh[1]) {
-          DownAcc acc;
+    active[k] = k < n && !(X0 >= P.x0 + P.w || Y0 >= P.y0 + P.h || X0 + TD <= P.x0 || Y0 + TD <= P.y0);
+  }
+  const int lw0 = a.lw[0], lh0 = a.lh[0], lw1 = a.lw[1], lh1 = a.lh[1];
+#pragma unroll 1
+  for (int i = threadIdx.x; i < T1 * T1; i += blockDim.x) {
+    const int tx = i % T1, ty = i / T1;
+    const int gx = (X0 >> 1) + tx, gy = (Y0 >> 1) + ty;
+    const bool inside = gx < lw1 && gy < lh1;
+    int own[NMAX][4];
+    uint32_t ent[NMAX][4];
 #pragma unroll
-          for (int dy = 0; dy < 2; ++dy)
+    for (int k = 0; k < NMAX; ++k)
 #pragma unroll
-            for (int dx = 0; dx < 2; ++dx) {
-              const int ix = 2 * gx + dx, iy = 2 * gy + dy;
-              if (ix < a.lw[0] && iy < a.lh[0]) acc.add(to_f4(plane_pixel(a.S, P, ix, iy, b, opaque)));
-            }
-          v = acc.result();
-          store_level(G1 + (long long)gy * a.lw[1] + gx, v);
+      for (int q = 0; q < 4; ++q) {
+        const int ix = 2 * gx + (q & 1), iy = 2 * gy + (q >> 1);
+        own[k][q] = 0xFF;
+        ent[k][q] = 0xFFFFFFFFu;
+        if (active[k] && inside && ix < lw0 && iy < lh0) slot_lookup(a.slot[k], k, ix, iy, own[k][q], ent[k][q]);
+      }
+    uchar4 px[NMAX][4];
+#pragma unroll
+    for (int k = 0; k < NMAX; ++k)
+#pragma unroll
+      for (int q = 0; q < 4; ++q) px[k][q] = fetch_sel<NMAX>(a.S, own[k][q], ent[k][q], b, opaque);
+#pragma unroll
+    for (int k = 0; k < NMAX; ++k) {
+      if (!active[k]) continue;
+      float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (inside) {
+        DownAcc acc;
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          const int ix = 2 * gx + (q & 1), iy = 2 * gy + (q >> 1);
+          if (ix < lw0 && iy < lh0) acc.add(to_f4(px[k][q]));
         }
-        bufA[i] = v;
+        v = acc.result();
+        Store* G1 = static_cast<Store*>(a.G[k][1]) + (long long)b * lw1 * lh1;
+        store_level(G1 + (long long)gy * lw1 + gx, v);
+      }
+      bufA[k * T1 * T1 + i] = v;
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int l = 2; l < kL; ++l) {
+    if (l >= L) break;
+    const int Tp = TD >> (l - 1), Tn = TD >> l;
+    const int area = Tn * Tn;
+    const float4* src = (l & 1) ? bufB : bufA;
+    float4* dst = (l & 1) ? bufA : bufB;
+    const int sstride = (l & 1) ? T2 * T2 : T1 * T1;
+    const int dstride = (l & 1) ? T1 * T1 : T2 * T2;
+    const int lwl = a.lw[l], lhl = a.lh[l], lwp = a.lw[l - 1], lhp = a.lh[l - 1];
+#pragma unroll
+    for (int k = 0; k < NMAX; ++k) {
+      if (!active[k]) continue;
+      for (int j = threadIdx.x; j < area; j += blockDim.x) {
+        const int tx = j % Tn, ty = j / Tn;
+        const int gx = (X0 >> l) + tx, gy = (Y0 >> l) + ty;
+        float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (gx < lwl && gy < lhl) {
+          DownAcc acc;
+          const float4* sk = src + k * sstride;
+#pragma unroll
+          for (int q = 0; q < 4; ++q) {
+            const int dx = q & 1, dy = q >> 1;
+            if (2 * gx + dx < lwp && 2 * gy + dy < lhp) acc.add(sk[(2 * ty + dy) * Tp + 2 * tx + dx]);
+          }
+          v = acc.result();
+          Store* Gl = static_cast<Store*>(a.G[k][l]) + (long long)b * lwl * lhl;
+          store_level(Gl + (long long)gy * lwl + gx, v);
+        }
+        dst[k * dstride + j] = v;
       }
     }
     __syncthreads();
-    float4* src = bufA;
-    float4* dst = bufB;
-    int T = T1;
-    for (int l = 2; l < L; ++l) {
-      const int Tn = T >> 1;
-      Store* Gl = static_cast<Store*>(a.G[k][l]) + (long long)b * a.lw[l] * a.lh[l];
-      for (int i = threadIdx.x; i < Tn * Tn; i += blockDim.x) {
-        const int tx = i % Tn, ty = i / Tn;
-        const int gx = (X0 >> l) + tx, gy = (Y0 >> l) + ty;
-        float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-        if (gx < a.lw[l] && gy < a.lh[l]) {
-          DownAcc acc;
-#pragma unroll
-          for (int dy = 0; dy < 2; ++dy)
-#pragma unroll
-            for (int dx = 0; dx < 2; ++dx) {
-              if (2 * gx + dx < a.lw[l - 1] && 2 * gy + dy < a.lh[l - 1])
-                acc.add(src[(2 * ty + dy) * T + 2 * tx + dx]);
-            }
-          v = acc.result();
-          store_level(Gl + (long long)gy * a.lw[l] + gx, v);
-        }
-        dst[i] = v;
-      }
-      __syncthreads();
-      float4* t = src;
-      src = dst;
-      dst = t;
-      T = Tn;
-    }
   }
 }
 
-// Alpha-aware bilinear upsample of a shared-memory region (origin ax, ay; row width rw) of a
+// Alpha-aware bilinear upsample of a shared-memory region (origin ax, ay; row stride cw) of a
 // level of size lw x lh, sampled for high-res pixel (x, y): top-left aligned, gx = x/2, taps
 // floor and floor+1 clamped to the level, only taps with alpha != 0, renormalised
-// (src/cuda/cudaBlend.cu:389-455, 581-672).
-__device__ __forceinline__ float3 up_alpha(const float4* buf, int rw, int ax, int ay, int lw, int lh, int x, int y) {
+// (src/cuda/cudaBlend.cu:389-455, 581-672). Callers order pixels so that the parity of (x, y) is
+// the same across a warp, which keeps the branches below uniform.
+//
+// Same bits as the reference, with less work. The weights are products of {1, 0.5}, so a tap of
+// weight 0 adds an exact zero and is skipped (the remaining taps keep their order; skipping can
+// only turn a -0 sum into +0, and the uint8 pack maps both to 0). Every other product v*w is
+// exact. The weight sum is 1, 0.5, 0.25 or 0.75; dividing by the first three is an exact scaling
+// by 1, 2 or 4, so only a 0.75 sum (three of four taps valid) needs a division.
+__device__ __forceinline__ float3 up_alpha(const float4* buf, int cw, int ax, int ay, int lw, int lh, int x, int y) {
   const int gxi = x >> 1, gyi = y >> 1;
+  const float4* r0 = buf + (gyi - ay) * cw - ax;
+  const float4 p00 = r0[gxi];
+  const bool ox = (x & 1) != 0, oy = (y & 1) != 0;
+  if (!ox && !oy) {
+    if (p00.w != 0.f) return make_float3(p00.x, p00.y, p00.z);
+    return make_float3(0.f, 0.f, 0.f);
+  }
+  if (ox != oy) {
+    // Two taps of weight 0.5: (00, 10) for odd x, (00, 01) for odd y.
+    const float4 p1 = ox ? r0[min(gxi + 1, lw - 1)] : buf[(min(gyi + 1, lh - 1) - ay) * cw + (gxi - ax)];
+    const bool v0 = p00.w != 0.f, v1 = p1.w != 0.f;
+    if (v0 && v1)  // (p00*0.5 + p1*0.5) / 1
+      return make_float3(p00.x * 0.5f + p1.x * 0.5f, p00.y * 0.5f + p1.y * 0.5f, p00.z * 0.5f + p1.z * 0.5f);
+    // (p*0.5) / 0.5: dividing by 0.5 is an exact doubling (kept explicit for subnormal p)
+    if (v0) return make_float3((p00.x * 0.5f) * 2.f, (p00.y * 0.5f) * 2.f, (p00.z * 0.5f) * 2.f);
+    if (v1) return make_float3((p1.x * 0.5f) * 2.f, (p1.y * 0.5f) * 2.f, (p1.z * 0.5f) * 2.f);
+    return make_float3(0.f, 0.f, 0.f);
+  }
+  // Four taps of weight 0.25.
   const int gxi1 = min(gxi + 1, lw - 1), gyi1 = min(gyi + 1, lh - 1);
-  const float dx = (x & 1) ? 0.5f : 0.f, dy = (y & 1) ? 0.5f : 0.f;
-  const float w00 = (1.f - dx) * (1.f - dy), w10 = dx * (1.f - dy), w01 = (1.f - dx) * dy, w11 = dx * dy;
-  const float4 p00 = buf[(gyi - ay) * rw + (gxi - ax)];
-  const float4 p10 = buf[(gyi - ay) * rw + (gxi1 - ax)];
-  const float4 p01 = buf[(gyi1 - ay) * rw + (gxi - ax)];
-  const float4 p11 = buf[(gyi1 - ay) * rw + (gxi1 - ax)];
+  const float4* r1 = buf + (gyi1 - ay) * cw - ax;
+  const float4 q[4] = {p00, r0[gxi1], r1[gxi], r1[gxi1]};
   float sw = 0.f, s0 = 0.f, s1 = 0.f, s2 = 0.f;
-  if (p00.w != 0.f) {
-    sw += w00;
-    s0 += p00.x * w00;
-    s1 += p00.y * w00;
-    s2 += p00.z * w00;
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    if (q[i].w != 0.f) {
+      sw += 0.25f;
+      s0 += q[i].x * 0.25f;
+      s1 += q[i].y * 0.25f;
+      s2 += q[i].z * 0.25f;
+    }
   }
-  if (p10.w != 0.f) {
-    sw += w10;
-    s0 += p10.x * w10;
-    s1 += p10.y * w10;
-    s2 += p10.z * w10;
-  }
-  if (p01.w != 0.f) {
-    sw += w01;
-    s0 += p01.x * w01;
-    s1 += p01.y * w01;
-    s2 += p01.z * w01;
-  }
-  if (p11.w != 0.f) {
-    sw += w11;
-    s0 += p11.x * w11;
-    s1 += p11.y * w11;
-    s2 += p11.z * w11;
-  }
+  if (sw == 1.f) return make_float3(s0, s1, s2);
+  if (sw == 0.5f) return make_float3(s0 * 2.f, s1 * 2.f, s2 * 2.f);
+  if (sw == 0.25f) return make_float3(s0 * 4.f, s1 * 4.f, s2 * 4.f);
   if (sw > 0.f) return make_float3(s0 / sw, s1 / sw, s2 / sw);
   return make_float3(0.f, 0.f, 0.f);
 }
@@ -174,15 +228,15 @@ __device__ __forceinline__ float4 blend_three(const float4* L, float m0, float m
   if (L[2].w == 0.f) m2 = 0.f;
   const float sum = (m0 + m1) + m2;
   if (!(sum > 0.f)) {
-    int src = -1;
+    float4 r = make_float4(0.f, 0.f, 0.f, 0.f);
     float amax = 0.f;
 #pragma unroll
     for (int k = 0; k < 3; ++k)
       if (L[k].w > amax) {
         amax = L[k].w;
-        src = k;
+        r = L[k];
       }
-    return src < 0 ? make_float4(0.f, 0.f, 0.f, 0.f) : L[src];
+    return r;
   }
   m0 /= sum;
   m1 /= sum;
@@ -244,100 +298,179 @@ __device__ __forceinline__ float4 blend_nway(const float4* L, int n, float* w) {
   return acc;
 }
 
+// Blend of one pixel at level l >= 1 with mask values m[0..K).
 template <int RULE, int NMAX>
-__device__ __forceinline__ float4 blend_pixel(const PyrArgs& a, const float4* lap, int l, int px, int py) {
-  if (RULE == kRuleTwo) {
-    float m;
-    if (l == 0)
-      m = float(a.mask0[(long long)py * a.mask0_pitch + px]);
-    else
-      m = a.maskL[l][(long long)py * a.lw[l] + px];
-    return blend_two(lap[0], lap[1], m);
-  } else if (RULE == kRuleThree) {
-    float m[3];
-    if (l == 0) {
-      const int label = a.mask0[(long long)py * a.mask0_pitch + px];
+__device__ __forceinline__ float4 blend_level(int n, const float4* lap, const float* m) {
+  if (RULE == kRuleTwo) return blend_two(lap[0], lap[1], m[0]);
+  if (RULE == kRuleThree) return blend_three(lap, m[0], m[1], m[2]);
+  float w[NMAX];
 #pragma unroll
-      for (int k = 0; k < 3; ++k) m[k] = label == k ? 1.f : 0.f;
-    } else {
-      const float* mp = a.maskL[l] + ((long long)py * a.lw[l] + px) * 3;
-#pragma unroll
-      for (int k = 0; k < 3; ++k) m[k] = mp[k];
-    }
-    return blend_three(lap, m[0], m[1], m[2]);
-  } else {
-    float w[NMAX];
-    if (l == 0) {
-      const int label = a.mask0[(long long)py * a.mask0_pitch + px];
-#pragma unroll
-      for (int k = 0; k < NMAX; ++k) w[k] = label == k ? 1.f : 0.f;
-    } else {
-      const float* mp = a.maskL[l] + ((long long)py * a.lw[l] + px) * a.K;
-#pragma unroll
-      for (int k = 0; k < NMAX; ++k) w[k] = k < a.n ? mp[k] : 0.f;
-    }
-    return blend_nway<NMAX>(lap, a.n, w);
-  }
+  for (int k = 0; k < NMAX; ++k) w[k] = k < n ? m[k] : 0.f;
+  return blend_nway<NMAX>(lap, n, w);
 }
 
-template <int RULE, int NMAX, typename Store>
-__global__ void __launch_bounds__(256) pyr_up_kernel(const __grid_constant__ PyrArgs a) {
-  extern __shared__ float4 sm[];
-  const int n = a.n;
-  // Shared memory: G for odd levels [n][rm_odd], G for even levels [n][rm_even], then R for odd
-  // and even levels. Level 0 is never stored.
-  float4* g_odd = sm;
-  float4* g_even = g_odd + n * a.rm_odd;
-  float4* r_odd = g_even + n * a.rm_even;
-  float4* r_even = r_odd + a.rm_odd;
-  const int TU = a.tile;
-  const int b = blockIdx.z;
-  const int X0 = (a.tx0 + blockIdx.x) * TU, Y0 = (a.ty0 + blockIdx.y) * TU;
-  const int L = a.levels, c = L - 1;
-  int ax[kDevMaxLevels], ay[kDevMaxLevels], bx[kDevMaxLevels], by[kDevMaxLevels];
-  ax[0] = X0;
-  ay[0] = Y0;
-  bx[0] = min(X0 + TU, a.lw[0]);
-  by[0] = min(Y0 + TU, a.lh[0]);
+// Blend of one level-0 pixel from its seam value (two-image weight) or label (one-hot).
+template <int RULE, int NMAX>
+__device__ __forceinline__ float4 blend_level0(int n, const float4* lap, int v) {
+  if (RULE == kRuleTwo) return blend_two(lap[0], lap[1], float(v));
+  if (RULE == kRuleThree) return blend_three(lap, v == 0 ? 1.f : 0.f, v == 1 ? 1.f : 0.f, v == 2 ? 1.f : 0.f);
+  float w[NMAX];
 #pragma unroll
-  for (int l = 1; l < kDevMaxLevels; ++l) {
-    if (l < L) {
-      ax[l] = ax[l - 1] >> 1;
-      ay[l] = ay[l - 1] >> 1;
-      bx[l] = min(((bx[l - 1] - 1) >> 1) + 2, a.lw[l]);
-      by[l] = min(((by[l - 1] - 1) >> 1) + 2, a.lh[l]);
+  for (int k = 0; k < NMAX; ++k) w[k] = v == k ? 1.f : 0.f;
+  return blend_nway<NMAX>(lap, n, w);
+}
+
+// Shared-memory row stride and capacity (pixels) of level l >= 1 for an up-tile of edge TU: the
+// tile's footprint at that level plus the upsample halo.
+__host__ __device__ constexpr int up_cw(int tile, int l) { return (tile >> l) + 2; }
+__host__ __device__ constexpr int up_cap(int tile, int l) { return up_cw(tile, l) * up_cw(tile, l); }
+
+// Read-only loads of a level buffer in HBM (through the non-coherent cache).
+__device__ __forceinline__ float4 ldg_level(const float4* p) { return __ldg(p); }
+__device__ __forceinline__ float4 ldg_level(const half4* p) {
+  const uint2 raw = __ldg(reinterpret_cast<const uint2*>(p));
+  const __half2 a = *reinterpret_cast<const __half2*>(&raw.x);
+  const __half2 b = *reinterpret_cast<const __half2*>(&raw.y);
+  const float2 fa = __half22float2(a), fb = __half22float2(b);
+  return make_float4(fa.x, fa.y, fb.x, fb.y);
+}
+
+// up_alpha over a full level buffer in HBM (row stride lw): same taps, order and exactness
+// argument as up_alpha above.
+template <typename T>
+__device__ __forceinline__ float3 up_alpha_g(const T* buf, int lw, int lh, int x, int y) {
+  const int gxi = x >> 1, gyi = y >> 1;
+  const T* r0 = buf + (long long)gyi * lw;
+  const float4 p00 = ldg_level(r0 + gxi);
+  const bool ox = (x & 1) != 0, oy = (y & 1) != 0;
+  if (!ox && !oy) {
+    if (p00.w != 0.f) return make_float3(p00.x, p00.y, p00.z);
+    return make_float3(0.f, 0.f, 0.f);
+  }
+  if (ox != oy) {
+    const float4 p1 = ox ? ldg_level(r0 + min(gxi + 1, lw - 1)) : ldg_level(buf + (long long)min(gyi + 1, lh - 1) * lw + gxi);
+    const bool v0 = p00.w != 0.f, v1 = p1.w != 0.f;
+    if (v0 && v1)
+      return make_float3(p00.x * 0.5f + p1.x * 0.5f, p00.y * 0.5f + p1.y * 0.5f, p00.z * 0.5f + p1.z * 0.5f);
+    if (v0) return make_float3((p00.x * 0.5f) * 2.f, (p00.y * 0.5f) * 2.f, (p00.z * 0.5f) * 2.f);
+    if (v1) return make_float3((p1.x * 0.5f) * 2.f, (p1.y * 0.5f) * 2.f, (p1.z * 0.5f) * 2.f);
+    return make_float3(0.f, 0.f, 0.f);
+  }
+  const int gxi1 = min(gxi + 1, lw - 1), gyi1 = min(gyi + 1, lh - 1);
+  const T* r1 = buf + (long long)gyi1 * lw;
+  const float4 q[4] = {p00, ldg_level(r0 + gxi1), ldg_level(r1 + gxi), ldg_level(r1 + gxi1)};
+  float sw = 0.f, s0 = 0.f, s1 = 0.f, s2 = 0.f;
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    if (q[i].w != 0.f) {
+      sw += 0.25f;
+      s0 += q[i].x * 0.25f;
+      s1 += q[i].y * 0.25f;
+      s2 += q[i].z * 0.25f;
     }
   }
-  const bool opaque = a.opaque != 0;
-  for (int l = c; l >= 0; --l) {
-    const int rw = bx[l] - ax[l], rh = by[l] - ay[l];
-    float4* gcur = (l & 1) ? g_odd : g_even;
-    float4* gprev = (l & 1) ? g_even : g_odd;
-    const int rm_cur = (l & 1) ? a.rm_odd : a.rm_even;
-    const int rm_prev = (l & 1) ? a.rm_even : a.rm_odd;
-    float4* rcur = (l & 1) ? r_odd : r_even;
-    const float4* rprev = (l & 1) ? r_even : r_odd;
-    if (l >= 1) {
-      const int npx = rw * rh;
-      for (int i = threadIdx.x; i < n * npx; i += blockDim.x) {
-        const int k = i / npx, j = i - k * npx;
-        const int py = ay[l] + j / rw, px = ax[l] + j % rw;
-        const Store* Gl = static_cast<const Store*>(a.G[k][l]) + (long long)b * a.lw[l] * a.lh[l];
-        gcur[k * rm_cur + j] = load_level(Gl + (long long)py * a.lw[l] + px);
+  if (sw == 1.f) return make_float3(s0, s1, s2);
+  if (sw == 0.5f) return make_float3(s0 * 2.f, s1 * 2.f, s2 * 2.f);
+  if (sw == 0.25f) return make_float3(s0 * 4.f, s1 * 4.f, s2 * 4.f);
+  if (sw > 0.f) return make_float3(s0 / sw, s1 / sw, s2 / sw);
+  return make_float3(0.f, 0.f, 0.f);
+}
+
+// pyr_coarse: R^1 (the reconstruction at level 1) for one T1 x T1 tile of level-1 pixels.
+// Levels 2..L-1 of the tile plus the upsample halo are loaded into shared memory up front (one
+// wait on memory), blended and reconstructed from the coarsest level down; level 1 reads G^1 and
+// the level-1 mask straight from HBM and writes R^1 to HBM for pyr_fine. Pixels are processed
+// parity-class-major so that the upsample branches stay uniform across a warp.
+template <int RULE, int NMAX, typename Store, int T1>
+__global__ void __launch_bounds__(256) pyr_coarse_kernel(const __grid_constant__ PyrArgs a) {
+  extern __shared__ float4 sm[];
+  const int n = RULE == kRuleNway ? a.n : NMAX;
+  const int K = RULE == kRuleTwo ? 1 : (RULE == kRuleThree ? 3 : a.K);
+  const int b = blockIdx.z;
+  const int X1 = (a.tx0 + blockIdx.x) * T1, Y1 = (a.ty0 + blockIdx.y) * T1;
+  const int L = a.levels, c = L - 1;
+  const int tid = threadIdx.x;
+  // Regions: level 1 is the tile itself; level l >= 2 adds the halo read by level l-1's
+  // upsample. Shared memory holds levels 2..c (G of every slot, R, mask values).
+  int rax[kL], ray[kL], rbx[kL], rby[kL], gofs[kL], rofs[kL], mofs[kL];
+  int f4_total = 0, mtotal = 0;
+  {
+    int ax = X1, ay = Y1, bx = min(X1 + T1, a.lw[1]), by = min(Y1 + T1, a.lh[1]);
+#pragma unroll
+    for (int l = 1; l < kL; ++l) {
+      if (l > 1 && l < L) {
+        ax >>= 1;
+        ay >>= 1;
+        bx = min(((bx - 1) >> 1) + 2, a.lw[l]);
+        by = min(((by - 1) >> 1) + 2, a.lh[l]);
       }
-      __syncthreads();
+      rax[l] = ax;
+      ray[l] = ay;
+      rbx[l] = bx;
+      rby[l] = by;
+      const int cap = (l > 1 && l < L) ? up_cap(T1, l - 1) : 0;
+      gofs[l] = f4_total;
+      rofs[l] = f4_total + n * cap;
+      f4_total = rofs[l] + cap;
+      mofs[l] = mtotal;
+      mtotal += cap * K;
     }
-    const int rw1 = l < c ? bx[l + 1] - ax[l + 1] : 0;
-    for (int i = threadIdx.x; i < rw * rh; i += blockDim.x) {
-      const int py = ay[l] + i / rw, px = ax[l] + i % rw;
-      if (l == 0 && (px < a.wx0 || px >= a.wx1 || py < a.wy0 || py >= a.wy1)) continue;
+  }
+  float* mbuf = reinterpret_cast<float*>(sm + f4_total);
+#pragma unroll
+  for (int l = 2; l < kL; ++l) {
+    if (l >= L) break;
+    const int CW = up_cw(T1, l - 1), CAP = CW * CW;
+    const int lax = rax[l], lay = ray[l], rw = rbx[l] - lax, rh = rby[l] - lay;
+    const int lw = a.lw[l], lh = a.lh[l];
+#pragma unroll
+    for (int k = 0; k < NMAX; ++k) {
+      if (k >= n) break;
+      const Store* Gl = static_cast<const Store*>(a.G[k][l]) + (long long)b * lw * lh;
+      float4* gl = sm + gofs[l] + k * CAP;
+      for (int i = tid; i < CAP; i += 256) {
+        const int x = i % CW, y = i / CW;
+        if (x < rw && y < rh) gl[i] = ldg_level(Gl + (long long)(lay + y) * lw + (lax + x));
+      }
+    }
+    const float* ml = a.maskL[l];
+    float* mb = mbuf + mofs[l];
+    for (int i = tid; i < CAP * K; i += 256) {
+      const int p = i / K, q = i - p * K;
+      const int x = p % CW, y = p / CW;
+      if (x < rw && y < rh) mb[i] = __ldg(ml + ((long long)(lay + y) * lw + (lax + x)) * K + q);
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int l = kL - 1; l >= 2; --l) {
+    if (l > c) continue;
+    const int CW = up_cw(T1, l - 1), CAP = CW * CW;
+    const int QW = (CW + 1) / 2, QC = QW * QW;
+    const int lax = rax[l], lay = ray[l], rw = rbx[l] - lax, rh = rby[l] - lay;
+    const float4* gcur = sm + gofs[l];
+    float4* rcur = sm + rofs[l];
+    const float* mb = mbuf + mofs[l];
+    const bool has_next = l < c;
+    const int nl = l + 1 < kL ? l + 1 : l;
+    const int CWN = up_cw(T1, nl - 1), CAPN = CWN * CWN;
+    const int nax = rax[nl], nay = ray[nl];
+    const int lwn = a.lw[nl], lhn = a.lh[nl];
+    const float4* gnext = sm + gofs[nl];
+    const float4* rnext = sm + rofs[nl];
+    for (int t = tid; t < 4 * QC; t += 256) {
+      const int cls = t / QC, j = t - cls * QC;
+      const int x = 2 * (j % QW) + (cls & 1), y = 2 * (j / QW) + (cls >> 1);
+      if (x >= rw || y >= rh) continue;
+      const int i = y * CW + x;
+      const int px = lax + x, py = lay + y;
       float4 lap[NMAX];
 #pragma unroll
       for (int k = 0; k < NMAX; ++k) {
         if (k < n) {
-          float4 g = l == 0 ? to_f4(plane_pixel(a.S, a.slot[k], px, py, b, opaque)) : gcur[k * rm_cur + i];
-          if (l < c) {
-            const float3 up = up_alpha(gprev + k * rm_prev, rw1, ax[l + 1], ay[l + 1], a.lw[l + 1], a.lh[l + 1], px, py);
+          float4 g = gcur[k * CAP + i];
+          if (has_next) {
+            const float3 up = up_alpha(gnext + k * CAPN, CWN, nax, nay, lwn, lhn, px, py);
             g.x = g.x - up.x;
             g.y = g.y - up.y;
             g.z = g.z - up.z;
@@ -347,80 +480,246 @@ __global__ void __launch_bounds__(256) pyr_up_kernel(const __grid_constant__ Pyr
           lap[k] = make_float4(0.f, 0.f, 0.f, 0.f);
         }
       }
-      float4 r = blend_pixel<RULE, NMAX>(a, lap, l, px, py);
-      if (l < c) {
-        const float3 up = up_alpha(rprev, rw1, ax[l + 1], ay[l + 1], a.lw[l + 1], a.lh[l + 1], px, py);
+      float4 r = blend_level<RULE, NMAX>(n, lap, mb + i * K);
+      if (has_next) {
+        const float3 up = up_alpha(rnext, CWN, nax, nay, lwn, lhn, px, py);
         r.x = up.x + r.x;
         r.y = up.y + r.y;
         r.z = up.z + r.z;
       }
-      if (l > 0) {
-        rcur[i] = r;
-      } else {
-        uchar4* crow = reinterpret_cast<uchar4*>(reinterpret_cast<char*>(a.C.ptr) + b * a.C.bstride +
-                                                 (long long)(py + a.cy_off) * a.C.pitch);
-        crow[px + a.cx_off] = pack_rgba(r);
-      }
+      rcur[i] = r;
     }
     __syncthreads();
   }
+  // Level 1: the tile's own pixels, G^1 and mask^1 from HBM, R^1 to HBM.
+  constexpr int HALF = T1 / 2, CLS = HALF * HALF, PER = T1 * T1 / 256;
+  static_assert(CLS % 32 == 0 && PER >= 1, "tile");
+  const int lw1 = a.lw[1], lh1 = a.lh[1];
+  const bool has2 = c >= 2;
+  const int CW2 = up_cw(T1, 1), CAP2 = CW2 * CW2;
+  const int nax = rax[2], nay = ray[2];
+  const int lw2 = a.lw[2 < kL ? 2 : 1], lh2 = a.lh[2 < kL ? 2 : 1];
+  const float4* g2 = sm + gofs[2];
+  const float4* r2 = sm + rofs[2];
+  float4* R1 = a.R1 + (long long)b * lw1 * lh1;
+#pragma unroll 2
+  for (int p = 0; p < PER; ++p) {
+    const int i = p * 256 + tid;
+    const int px = X1 + 2 * ((i % CLS) % HALF) + ((i / CLS) & 1);
+    const int py = Y1 + 2 * ((i % CLS) / HALF) + ((i / CLS) >> 1);
+    if (px >= lw1 || py >= lh1) continue;
+    const long long o1 = (long long)py * lw1 + px;
+    float m[NMAX];
+#pragma unroll
+    for (int q = 0; q < NMAX; ++q) m[q] = q < K ? __ldg(a.maskL[1] + o1 * K + q) : 0.f;
+    float4 lap[NMAX];
+#pragma unroll
+    for (int k = 0; k < NMAX; ++k) {
+      if (k < n) {
+        float4 g = ldg_level(static_cast<const Store*>(a.G[k][1]) + (long long)b * lw1 * lh1 + o1);
+        if (has2) {
+          const float3 up = up_alpha(g2 + k * CAP2, CW2, nax, nay, lw2, lh2, px, py);
+          g.x = g.x - up.x;
+          g.y = g.y - up.y;
+          g.z = g.z - up.z;
+        }
+        lap[k] = g;
+      } else {
+        lap[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+      }
+    }
+    float4 r = blend_level<RULE, NMAX>(n, lap, m);
+    if (has2) {
+      const float3 up = up_alpha(r2, CW2, nax, nay, lw2, lh2, px, py);
+      r.x = up.x + r.x;
+      r.y = up.y + r.y;
+      r.z = up.z + r.z;
+    }
+    R1[o1] = r;
+  }
 }
 
+// pyr_fine: level 0 of the write region. Each warp owns a 64 x 2 pixel block, each lane the 2x2
+// pixels (X, Y)..(X+1, Y+1), processed in the four parity passes so the upsample branches are
+// uniform across the warp. All table lookups, then all source gathers, are issued before any
+// arithmetic; G^1 and R^1 taps come from HBM through the cache (neighbouring lanes and passes
+// share them). Lap_k = G^0_k - up(G^1_k), blend with the level-0 seam value, R^0 = up(R^1) +
+// blend, truncating pack into the canvas. No shared memory, no barriers.
 template <int RULE, int NMAX, typename Store>
+__global__ void __launch_bounds__(256) pyr_fine_kernel(const __grid_constant__ PyrArgs a) {
+  const int n = RULE == kRuleNway ? a.n : NMAX;
+  const int b = blockIdx.z;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int X = (a.wx0 & ~1) + blockIdx.x * 64 + 2 * lane;
+  const int Y = (a.wy0 & ~1) + blockIdx.y * 16 + 2 * warp;
+  const bool opaque = a.opaque != 0;
+  const int lw0 = a.lw[0], lh0 = a.lh[0];
+  int own[4][NMAX], mv[4];
+  uint32_t ent[4][NMAX];
+  bool live[4];
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    const int x = X + (q & 1), y = Y + (q >> 1);
+    live[q] = x < lw0 && y < lh0 && x >= a.wx0 && x < a.wx1 && y >= a.wy0 && y < a.wy1;
+    mv[q] = live[q] ? int(__ldg(a.mask0 + (long long)y * a.mask0_pitch + x)) : 0;
+#pragma unroll
+    for (int k = 0; k < NMAX; ++k) {
+      own[q][k] = 0xFF;
+      ent[q][k] = 0xFFFFFFFFu;
+      if (live[q] && k < n) slot_lookup(a.slot[k], k, x, y, own[q][k], ent[q][k]);
+    }
+  }
+  uchar4 src[4][NMAX];
+#pragma unroll
+  for (int q = 0; q < 4; ++q)
+#pragma unroll
+    for (int k = 0; k < NMAX; ++k) src[q][k] = fetch_sel<NMAX>(a.S, own[q][k], ent[q][k], b, opaque);
+  const bool has1 = a.levels > 1;
+  const int lw1 = a.lw[1], lh1 = a.lh[1];
+  const float4* R1 = a.R1 + (long long)b * lw1 * lh1;
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    if (!live[q]) continue;
+    const int px = X + (q & 1), py = Y + (q >> 1);
+    float4 lap[NMAX];
+#pragma unroll
+    for (int k = 0; k < NMAX; ++k) {
+      float4 g = to_f4(src[q][k]);
+      if (has1 && k < n) {
+        const float3 up =
+            up_alpha_g(static_cast<const Store*>(a.G[k][1]) + (long long)b * lw1 * lh1, lw1, lh1, px, py);
+        g.x = g.x - up.x;
+        g.y = g.y - up.y;
+        g.z = g.z - up.z;
+      }
+      lap[k] = g;
+    }
+    float4 r = blend_level0<RULE, NMAX>(n, lap, mv[q]);
+    if (has1) {
+      const float3 up = up_alpha_g(R1, lw1, lh1, px, py);
+      r.x = up.x + r.x;
+      r.y = up.y + r.y;
+      r.z = up.z + r.z;
+    }
+    uchar4* crow = reinterpret_cast<uchar4*>(reinterpret_cast<char*>(a.C.ptr) + b * a.C.bstride +
+                                             (long long)(py + a.cy_off) * a.C.pitch);
+    crow[px + a.cx_off] = pack_rgba(r);
+  }
+}
+
+template <int NMAX, typename Store, int T>
+void set_down_attr() {
+  cudaFuncSetAttribute(pyr_down_kernel<NMAX, Store, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+}
+
+template <int RULE, int NMAX, typename Store, int T>
 void set_up_attr() {
-  cudaFuncSetAttribute(pyr_up_kernel<RULE, NMAX, Store>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+  cudaFuncSetAttribute(pyr_coarse_kernel<RULE, NMAX, Store, T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       227 * 1024);
+}
+
+template <typename Store, int T>
+void set_attrs() {
+  set_down_attr<2, Store, T>();
+  set_down_attr<3, Store, T>();
+  set_down_attr<8, Store, T>();
+  set_up_attr<kRuleTwo, 2, Store, T>();
+  set_up_attr<kRuleThree, 3, Store, T>();
+  set_up_attr<kRuleNway, 8, Store, T>();
+}
+
+template <typename Store, int T>
+void down_dispatch(const PyrArgs& a, dim3 grid, size_t smem, cudaStream_t stream) {
+  if (a.n <= 2)
+    pyr_down_kernel<2, Store, T><<<grid, 256, smem, stream>>>(a);
+  else if (a.n == 3)
+    pyr_down_kernel<3, Store, T><<<grid, 256, smem, stream>>>(a);
+  else
+    pyr_down_kernel<8, Store, T><<<grid, 256, smem, stream>>>(a);
+}
+
+template <typename Store, int T>
+void coarse_dispatch(const PyrArgs& a, int rule, dim3 grid, size_t smem, cudaStream_t stream) {
+  if (rule == kRuleTwo)
+    pyr_coarse_kernel<kRuleTwo, 2, Store, T><<<grid, 256, smem, stream>>>(a);
+  else if (rule == kRuleThree)
+    pyr_coarse_kernel<kRuleThree, 3, Store, T><<<grid, 256, smem, stream>>>(a);
+  else
+    pyr_coarse_kernel<kRuleNway, 8, Store, T><<<grid, 256, smem, stream>>>(a);
+}
+
+template <typename Store>
+void fine_dispatch(const PyrArgs& a, int rule, dim3 grid, cudaStream_t stream) {
+  if (rule == kRuleTwo)
+    pyr_fine_kernel<kRuleTwo, 2, Store><<<grid, 256, 0, stream>>>(a);
+  else if (rule == kRuleThree)
+    pyr_fine_kernel<kRuleThree, 3, Store><<<grid, 256, 0, stream>>>(a);
+  else
+    pyr_fine_kernel<kRuleNway, 8, Store><<<grid, 256, 0, stream>>>(a);
 }
 
 }  // namespace
 
-size_t pyr_down_smem(int tile) {
+size_t pyr_down_smem(int n, int tile) {
   const int t1 = tile / 2, t2 = tile / 4;
-  return size_t(t1 * t1 + t2 * t2) * sizeof(float4);
+  return size_t(n) * size_t(t1 * t1 + t2 * t2) * sizeof(float4);
 }
 
-size_t pyr_up_smem(int n, int rm_odd, int rm_even) {
-  return size_t((n + 1) * (rm_odd + rm_even)) * sizeof(float4);
+size_t pyr_coarse_smem(int n, int k, int tile1, int levels) {
+  size_t bytes = 0;
+  for (int l = 2; l < levels; ++l)
+    bytes += size_t(up_cap(tile1, l - 1)) * ((n + 1) * sizeof(float4) + k * sizeof(float));
+  return bytes;
 }
 
 cudaError_t kernels_init() {
-  cudaFuncSetAttribute(pyr_down_kernel<float4>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
-  cudaFuncSetAttribute(pyr_down_kernel<half4>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
-  set_up_attr<kRuleTwo, 2, float4>();
-  set_up_attr<kRuleTwo, 2, half4>();
-  set_up_attr<kRuleThree, 3, float4>();
-  set_up_attr<kRuleThree, 3, half4>();
-  set_up_attr<kRuleNway, 8, float4>();
-  set_up_attr<kRuleNway, 8, half4>();
+  set_attrs<float4, 32>();
+  set_attrs<half4, 32>();
+  set_attrs<float4, 64>();
+  set_attrs<half4, 64>();
   return cudaGetLastError();
 }
 
 cudaError_t launch_pyr_down(const PyrArgs& a, int storage, dim3 grid, cudaStream_t stream) {
-  const size_t smem = pyr_down_smem(a.tile);
-  if (storage == 1)
-    pyr_down_kernel<half4><<<grid, 256, smem, stream>>>(a);
-  else
-    pyr_down_kernel<float4><<<grid, 256, smem, stream>>>(a);
+  const size_t smem = pyr_down_smem(a.n, a.tile);
+  if (a.tile == 32) {
+    if (storage == 1)
+      down_dispatch<half4, 32>(a, grid, smem, stream);
+    else
+      down_dispatch<float4, 32>(a, grid, smem, stream);
+  } else if (a.tile == 64) {
+    if (storage == 1)
+      down_dispatch<half4, 64>(a, grid, smem, stream);
+    else
+      down_dispatch<float4, 64>(a, grid, smem, stream);
+  } else {
+    return cudaErrorInvalidValue;
+  }
   return cudaGetLastError();
 }
 
-cudaError_t launch_pyr_up(const PyrArgs& a, int rule, int storage, dim3 grid, size_t smem, cudaStream_t stream) {
-  const bool h = storage == 1;
-  if (rule == kRuleTwo) {
-    if (h)
-      pyr_up_kernel<kRuleTwo, 2, half4><<<grid, 256, smem, stream>>>(a);
+cudaError_t launch_pyr_coarse(const PyrArgs& a, int rule, int storage, dim3 grid, size_t smem, cudaStream_t stream) {
+  if (a.tile == 32) {
+    if (storage == 1)
+      coarse_dispatch<half4, 32>(a, rule, grid, smem, stream);
     else
-      pyr_up_kernel<kRuleTwo, 2, float4><<<grid, 256, smem, stream>>>(a);
-  } else if (rule == kRuleThree) {
-    if (h)
-      pyr_up_kernel<kRuleThree, 3, half4><<<grid, 256, smem, stream>>>(a);
+      coarse_dispatch<float4, 32>(a, rule, grid, smem, stream);
+  } else if (a.tile == 64) {
+    if (storage == 1)
+      coarse_dispatch<half4, 64>(a, rule, grid, smem, stream);
     else
-      pyr_up_kernel<kRuleThree, 3, float4><<<grid, 256, smem, stream>>>(a);
+      coarse_dispatch<float4, 64>(a, rule, grid, smem, stream);
   } else {
-    if (h)
-      pyr_up_kernel<kRuleNway, 8, half4><<<grid, 256, smem, stream>>>(a);
-    else
-      pyr_up_kernel<kRuleNway, 8, float4><<<grid, 256, smem, stream>>>(a);
+    return cudaErrorInvalidValue;
   }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_pyr_fine(const PyrArgs& a, int rule, int storage, dim3 grid, cudaStream_t stream) {
+  if (storage == 1)
+    fine_dispatch<half4>(a, rule, grid, stream);
+  else
+    fine_dispatch<float4>(a, rule, grid, stream);
   return cudaGetLastError();
 }
 

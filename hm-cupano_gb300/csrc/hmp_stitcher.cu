@@ -3,8 +3,10 @@
 // Construction plans the configuration on the host (hmp_plan.cpp), uploads the gather planes and
 // the mask pyramid, and allocates the pyramid levels. process() then launches at most three
 // kernels and allocates nothing:
-//   caller stream : pyr_down (levels >= 2), pyr_up (blend + reconstruct + pack of the write rect)
-//   aux stream    : canvas_gather of everything outside the write rect (forked/joined by events)
+//   aux stream (high priority) : pyr_down (Gaussian levels), pyr_coarse (reconstruction down to
+//                                level 1), pyr_fine (level 0: blend + reconstruct + pack of the
+//                                write rect), forked from and joined back to the caller stream
+//   caller stream              : canvas_gather of everything outside the write rect
 // The hard seam (levels == 0) is a single canvas_gather on the caller stream.
 #include <cuda_runtime.h>
 
@@ -50,21 +52,22 @@ struct hmp_stitcher {
   const float* maskL[hmp::kDevMaxLevels]{};
   const uint8_t* mask0 = nullptr;
   int mask0_pitch = 0;
-  int tile_down = 0, tile_up = 0;
-  int rm_odd = 0, rm_even = 0;
-  size_t up_smem = 0;
+  int tile_down = 0, tile_coarse = 0;
+  size_t coarse_smem = 0;
+  float4* R1 = nullptr;
   cudaStream_t aux = nullptr;
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   double m0_bytes = 0;
   int launches = 0;
   // Optional per-kernel event timing (hmp_stitcher_set_timing).
   static constexpr int kTimingSlots = 4096;
+  static constexpr int kTimed = 4;
   bool timing = false;
-  std::vector<cudaEvent_t> tev;  // [slot][kernel][begin/end]
+  std::vector<cudaEvent_t> tev;  // [slot][kernel][begin/end], kernels: gather, down, coarse, fine
   std::vector<unsigned char> tused;
   int tnext = 0;
-  double tms[3] = {0, 0, 0};
-  long long tcount[3] = {0, 0, 0};
+  double tms[4] = {0, 0, 0, 0};
+  long long tcount[4] = {0, 0, 0, 0};
 
   ~hmp_stitcher() {
     for (cudaEvent_t e : tev) cudaEventDestroy(e);
@@ -95,7 +98,7 @@ struct hmp_stitcher {
       d.w = d.h = 0;
       return cudaSuccess;
     }
-    const int mp = round_up(g.rect.w, 4);
+    const int mp = round_up(g.rect.w, 8);
     void* m = nullptr;
     cudaError_t e = alloc(&m, size_t(mp) * 4 * g.rect.h);
     if (e != cudaSuccess) return e;
@@ -163,17 +166,30 @@ struct hmp_stitcher {
       // Tiles: level-0 edge a multiple of 2^(L-1); smaller up-tiles for many images keep the
       // per-CTA shared memory (n+1 images' worth of two levels) within the SM.
       const int align = 1 << (L - 1);
-      tile_down = std::max(64, align);
-      tile_up = std::max(n > 4 ? 32 : 64, align);
-      rm_odd = (tile_up / 2 + 2) * (tile_up / 2 + 2);
-      rm_even = (tile_up / 4 + 2) * (tile_up / 4 + 2);
-      up_smem = hmp::pyr_up_smem(n, rm_odd, rm_even);
-      if (up_smem > 227 * 1024)
+      // Down tiles: 64 level-0 pixels amortise the per-CTA level walk; with more than three images
+      // the per-tile shared memory calls for 32. Coarse tiles: 32 level-1 pixels (a multiple of
+      // 2^(L-2) for every supported L).
+      tile_down = std::max(n <= 3 ? 64 : 32, align);
+      tile_coarse = std::max(32, align / 2);
+      coarse_smem = hmp::pyr_coarse_smem(n, p.mask_k, tile_coarse, L);
+      if (L > 1) {
+        void* r = nullptr;
+        e = alloc(&r, size_t(B) * p.lw[1] * p.lh[1] * sizeof(float4));
+        if (e != cudaSuccess) return cuda_status(e, "reconstruction buffer");
+        R1 = static_cast<float4*>(r);
+      }
+      if (hmp::pyr_down_smem(n, tile_down) > 227 * 1024)
         return make_status(HMP_ERR_NOT_SUPPORTED, "pyramid tile does not fit in shared memory");
-      launches += (L > 1 ? 1 : 0) + 1;
+      if (coarse_smem > 227 * 1024)
+        return make_status(HMP_ERR_NOT_SUPPORTED, "pyramid tile does not fit in shared memory");
+      launches += (L > 1 ? 2 : 0) + 1;
     }
     if (p.canvas_plane_used && p.levels > 0) {
-      e = cudaStreamCreateWithFlags(&aux, cudaStreamNonBlocking);
+      // The pyramid chain (latency-bound, few CTAs) runs on a high-priority stream so that its
+      // CTAs are dispatched ahead of the bandwidth-bound canvas gather sharing the SMs.
+      int least = 0, greatest = 0;
+      cudaDeviceGetStreamPriorityRange(&least, &greatest);
+      e = cudaStreamCreateWithPriority(&aux, cudaStreamNonBlocking, greatest);
       if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming);
       if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev_join, cudaEventDisableTiming);
       if (e != cudaSuccess) return cuda_status(e, "stream setup");
@@ -213,44 +229,44 @@ struct hmp_stitcher {
 
   cudaError_t timing_enable(bool on) {
     if (on && tev.empty()) {
-      tev.resize(size_t(kTimingSlots) * 3 * 2);
+      tev.resize(size_t(kTimingSlots) * kTimed * 2);
       for (auto& e : tev) {
         cudaError_t r = cudaEventCreate(&e);
         if (r != cudaSuccess) return r;
       }
-      tused.assign(size_t(kTimingSlots) * 3, 0);
+      tused.assign(size_t(kTimingSlots) * kTimed, 0);
     }
     timing = on;
     tnext = 0;
     std::fill(tused.begin(), tused.end(), 0);
-    for (int k = 0; k < 3; ++k) tms[k] = 0, tcount[k] = 0;
+    for (int k = 0; k < kTimed; ++k) tms[k] = 0, tcount[k] = 0;
     return cudaSuccess;
   }
 
   cudaEvent_t tbegin(int kernel, cudaStream_t s) {
     if (!timing || tnext >= kTimingSlots) return nullptr;
-    cudaEventRecord(tev[(size_t(tnext) * 3 + kernel) * 2], s);
-    return tev[(size_t(tnext) * 3 + kernel) * 2];
+    cudaEventRecord(tev[(size_t(tnext) * kTimed + kernel) * 2], s);
+    return tev[(size_t(tnext) * kTimed + kernel) * 2];
   }
   void tend(int kernel, cudaStream_t s) {
     if (!timing || tnext >= kTimingSlots) return;
-    cudaEventRecord(tev[(size_t(tnext) * 3 + kernel) * 2 + 1], s);
-    tused[size_t(tnext) * 3 + kernel] = 1;
+    cudaEventRecord(tev[(size_t(tnext) * kTimed + kernel) * 2 + 1], s);
+    tused[size_t(tnext) * kTimed + kernel] = 1;
   }
 
   cudaError_t timing_collect(hmp_kernel_timing* out) {
     for (int slot = 0; slot < tnext; ++slot)
-      for (int k = 0; k < 3; ++k) {
-        if (!tused[size_t(slot) * 3 + k]) continue;
+      for (int k = 0; k < kTimed; ++k) {
+        if (!tused[size_t(slot) * kTimed + k]) continue;
         float ms = 0;
-        cudaEvent_t e1 = tev[(size_t(slot) * 3 + k) * 2 + 1];
+        cudaEvent_t e1 = tev[(size_t(slot) * kTimed + k) * 2 + 1];
         cudaError_t r = cudaEventSynchronize(e1);
-        if (r == cudaSuccess) r = cudaEventElapsedTime(&ms, tev[(size_t(slot) * 3 + k) * 2], e1);
+        if (r == cudaSuccess) r = cudaEventElapsedTime(&ms, tev[(size_t(slot) * kTimed + k) * 2], e1);
         if (r != cudaSuccess) return r;
         tms[k] += ms;
         tcount[k] += 1;
       }
-    for (int k = 0; k < 3; ++k) {
+    for (int k = 0; k < kTimed; ++k) {
       out->total_ms[k] = tms[k];
       out->launches[k] = tcount[k];
       tms[k] = 0;
@@ -298,7 +314,6 @@ struct hmp_stitcher {
     C.bstride = (long long)canvas->pitch * canvas->height;
     C.w = canvas->width;
     C.h = canvas->height;
-    const bool vec = (reinterpret_cast<uintptr_t>(canvas->data) % 16 == 0) && (canvas->pitch % 16 == 0);
 
     hmp::GatherArgs ga{};
     if (p.canvas_plane_used) {
@@ -307,6 +322,7 @@ struct hmp_stitcher {
       ga.C = C;
       ga.batch = p.batch;
       ga.opaque = p.canvas_opaque ? 1 : 0;
+      ga.n_owners = p.n;
       if (p.levels > 0) {
         ga.skip_x0 = p.write.x;
         ga.skip_y0 = p.write.y;
@@ -317,20 +333,21 @@ struct hmp_stitcher {
     cudaError_t e;
     if (p.levels == 0) {
       tbegin(0, s);
-      e = hmp::launch_canvas_gather(ga, vec, s);
+      e = hmp::launch_canvas_gather(ga, s);
       tend(0, s);
       if (timing && tnext < kTimingSlots) ++tnext;
       if (e != cudaSuccess) return cuda_status(e, "canvas_gather launch");
       return ok_status();
     }
+    // Fork: the pyramid goes to the high-priority stream `aux` when the canvas gather also
+    // runs; the gather is launched on the caller stream after the pyramid kernels.
     const bool fork = p.canvas_plane_used;
+    cudaStream_t ps = s;
     if (fork) {
       e = cudaEventRecord(ev_fork, s);
       if (e == cudaSuccess) e = cudaStreamWaitEvent(aux, ev_fork, 0);
-      tbegin(0, aux);
-      if (e == cudaSuccess) e = hmp::launch_canvas_gather(ga, vec, aux);
-      tend(0, aux);
-      if (e != cudaSuccess) return cuda_status(e, "canvas_gather launch");
+      if (e != cudaSuccess) return cuda_status(e, "stream fork");
+      ps = aux;
     }
     hmp::PyrArgs a{};
     a.S = S;
@@ -354,31 +371,47 @@ struct hmp_stitcher {
     a.wy1 = a.wy0 + p.write.h;
     a.cx_off = p.blend.x;
     a.cy_off = p.blend.y;
-    a.rm_odd = rm_odd;
-    a.rm_even = rm_even;
     if (p.levels > 1) {
       a.tile = tile_down;
       const dim3 grid((p.lw[0] + tile_down - 1) / tile_down, (p.lh[0] + tile_down - 1) / tile_down, p.batch);
-      tbegin(1, s);
-      e = hmp::launch_pyr_down(a, p.storage, grid, s);
-      tend(1, s);
+      tbegin(1, ps);
+      e = hmp::launch_pyr_down(a, p.storage, grid, ps);
+      tend(1, ps);
       if (e != cudaSuccess) return cuda_status(e, "pyr_down launch");
     }
-    a.tile = tile_up;
-    a.tx0 = a.wx0 / tile_up;
-    a.ty0 = a.wy0 / tile_up;
-    const int tx1 = (a.wx1 + tile_up - 1) / tile_up, ty1 = (a.wy1 + tile_up - 1) / tile_up;
-    const dim3 grid(tx1 - a.tx0, ty1 - a.ty0, p.batch);
-    tbegin(2, s);
-    e = hmp::launch_pyr_up(a, p.rule, p.storage, grid, up_smem, s);
-    tend(2, s);
-    if (timing && tnext < kTimingSlots) ++tnext;
-    if (e != cudaSuccess) return cuda_status(e, "pyr_up launch");
+    a.R1 = R1;
+    if (p.levels > 1) {
+      // Level-1 pixels the fine pass reads: floor(x/2) and floor(x/2)+1 of the write rect.
+      const int x1lo = a.wx0 >> 1, x1hi = std::min(((a.wx1 - 1) >> 1) + 2, p.lw[1]);
+      const int y1lo = a.wy0 >> 1, y1hi = std::min(((a.wy1 - 1) >> 1) + 2, p.lh[1]);
+      a.tile = tile_coarse;
+      a.tx0 = x1lo / tile_coarse;
+      a.ty0 = y1lo / tile_coarse;
+      const dim3 cgrid((x1hi + tile_coarse - 1) / tile_coarse - a.tx0, (y1hi + tile_coarse - 1) / tile_coarse - a.ty0,
+                       p.batch);
+      tbegin(2, ps);
+      e = hmp::launch_pyr_coarse(a, p.rule, p.storage, cgrid, coarse_smem, ps);
+      tend(2, ps);
+      if (e != cudaSuccess) return cuda_status(e, "pyr_coarse launch");
+    }
+    {
+      const int fx0 = a.wx0 & ~1, fy0 = a.wy0 & ~1;
+      const dim3 fgrid((a.wx1 - fx0 + 63) / 64, (a.wy1 - fy0 + 15) / 16, p.batch);
+      tbegin(3, ps);
+      e = hmp::launch_pyr_fine(a, p.rule, p.storage, fgrid, ps);
+      tend(3, ps);
+      if (e != cudaSuccess) return cuda_status(e, "pyr_fine launch");
+    }
     if (fork) {
+      tbegin(0, s);
+      e = hmp::launch_canvas_gather(ga, s);
+      tend(0, s);
+      if (e != cudaSuccess) return cuda_status(e, "canvas_gather launch");
       e = cudaEventRecord(ev_join, aux);
       if (e == cudaSuccess) e = cudaStreamWaitEvent(s, ev_join, 0);
       if (e != cudaSuccess) return cuda_status(e, "stream join");
     }
+    if (timing && tnext < kTimingSlots) ++tnext;
     return ok_status();
   }
 };
@@ -444,7 +477,7 @@ HMP_API hmp_status hmp_stitcher_get_info(const hmp_stitcher* st, hmp_stitcher_in
   std::memcpy(info->blend_rect, br, sizeof(br));
   std::memcpy(info->write_rect, wr, sizeof(wr));
   info->tile_down = st->tile_down;
-  info->tile_up = st->tile_up;
+  info->tile_coarse = st->tile_coarse;
   info->launches_per_process = st->launches;
   info->m0_bytes = st->m0_bytes;
   info->device_bytes = double(st->device_bytes);

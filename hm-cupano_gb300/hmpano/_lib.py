@@ -68,7 +68,7 @@ class StitcherInfo(C.Structure):
         ("blend_rect", C.c_int * 4),
         ("write_rect", C.c_int * 4),
         ("tile_down", C.c_int),
-        ("tile_up", C.c_int),
+        ("tile_coarse", C.c_int),
         ("launches_per_process", C.c_int),
         ("m0_bytes", C.c_double),
         ("device_bytes", C.c_double),
@@ -76,7 +76,7 @@ class StitcherInfo(C.Structure):
 
 
 class KernelTiming(C.Structure):
-    _fields_ = [("total_ms", C.c_double * 3), ("launches", C.c_longlong * 3)]
+    _fields_ = [("total_ms", C.c_double * 4), ("launches", C.c_longlong * 4)]
 
 
 # Every symbol include/hmpano.h declares, with its signature.

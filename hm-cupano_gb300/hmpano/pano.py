@@ -234,7 +234,7 @@ class _Stitcher:
             "blend_rect": tuple(inf.blend_rect),
             "write_rect": tuple(inf.write_rect),
             "tile_down": inf.tile_down,
-            "tile_up": inf.tile_up,
+            "tile_coarse": inf.tile_coarse,
             "launches_per_process": inf.launches_per_process,
             "m0_bytes": inf.m0_bytes,
             "device_bytes": inf.device_bytes,
@@ -252,8 +252,8 @@ class _Stitcher:
         s = _status(_lib.lib().hmp_stitcher_get_timing(self._handle, C.byref(t)))
         if not s.ok():
             raise CudaStatusError(s)
-        names = ("canvas_gather", "pyr_down", "pyr_up")
-        return {names[i]: (float(t.total_ms[i]), int(t.launches[i])) for i in range(3)}
+        names = ("canvas_gather", "pyr_down", "pyr_coarse", "pyr_fine")
+        return {names[i]: (float(t.total_ms[i]), int(t.launches[i])) for i in range(4)}
 
     def _run(self, inputs: Sequence, canvas=None, stream=None):
         import torch

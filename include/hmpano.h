@@ -120,7 +120,7 @@ typedef struct hmp_stitcher_info {
   int blend_rect[4]; /* pyramid domain */
   int write_rect[4]; /* region the pyramid writes back to the canvas */
   int tile_down;     /* level-0 tile edge of the Gaussian-pyramid kernel */
-  int tile_up;       /* level-0 tile edge of the blend/reconstruct kernel */
+  int tile_coarse;   /* level-1 tile edge of the coarse reconstruction kernel */
   int launches_per_process; /* kernels one process() launches */
   double m0_bytes;   /* compulsory bytes per frame (maps, seam, sources, canvas) */
   double device_bytes; /* device memory held by the stitcher */
@@ -151,11 +151,12 @@ HMP_API hmp_status hmp_stitcher_process(hmp_stitcher* st, const hmp_image* input
                                         const hmp_image* canvas, void* stream);
 
 /* Per-kernel device time of process() calls made while timing is enabled, measured with CUDA
- * events recorded on the stream each kernel is launched on (the canvas gather runs on the
- * stitcher's auxiliary stream). Index 0 = canvas_gather, 1 = pyr_down, 2 = pyr_up. */
+ * events recorded on the stream each kernel is launched on (the pyramid kernels run on the
+ * stitcher's auxiliary stream). Index 0 = canvas_gather, 1 = pyr_down, 2 = pyr_coarse,
+ * 3 = pyr_fine. */
 typedef struct hmp_kernel_timing {
-  double total_ms[3];
-  long long launches[3];
+  double total_ms[4];
+  long long launches[4];
 } hmp_kernel_timing;
 
 /* Enable (1) or disable (0) per-kernel event timing; enabling clears the accumulated times.
