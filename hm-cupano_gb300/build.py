@@ -30,6 +30,7 @@ UNITS = {
     "hmp_gather.cu": [],
     "hmp_pyramid.cu": ["-fmad=false"],
     "hmp_stitcher.cu": [],
+    "hmp_noalloc.cu": ["-fmad=false"],
 }
 HEADERS = ["hmp_plan.h", "hmp_device.cuh", "hmp_kernels.h"]
 

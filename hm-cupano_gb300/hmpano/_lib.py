@@ -93,7 +93,11 @@ SIGNATURES = {
     "hmp_stitcher_set_timing": ([C.c_void_p, C.c_int], Status),
     "hmp_stitcher_get_timing": ([C.c_void_p, C.POINTER(KernelTiming)], Status),
     "hmp_plan_geometry": ([C.POINTER(Config), C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)], Status),
+    "hmp_blend2_noalloc": ([C.POINTER(Image), C.POINTER(Image), C.c_void_p, C.c_size_t, C.c_int, C.c_int,
+                            C.POINTER(Image), C.c_void_p], Status),
 }
+
+NOALLOC_SCRATCH_BYTES = 48 * 1024 * 1024  # HMP_NOALLOC_SCRATCH_BYTES
 
 _lib = None
 

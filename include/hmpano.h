@@ -168,6 +168,36 @@ HMP_API hmp_status hmp_stitcher_set_timing(hmp_stitcher* st, int enable);
  * whole frames with a host clock, tests/testCudaBlend.cpp:224-241). */
 HMP_API hmp_status hmp_stitcher_get_timing(hmp_stitcher* st, hmp_kernel_timing* out);
 
+/* Size of the static device array hmp_blend2_noalloc works in: 48 MiB, about 2.3 million pixels
+ * per frame at batch 1 (e.g. 1920 x 1080). */
+#define HMP_NOALLOC_SCRATCH_BYTES (48u * 1024u * 1024u)
+
+/* Two-image Laplacian pyramid blend that allocates no device memory. No counterpart in the
+ * reference.
+ *
+ * For callers that cannot call cudaMalloc, and so cannot create a stitcher: a plugin inside a
+ * host application that owns all device memory through its own pool (a raw cudaMalloc escapes
+ * the host's budget and accounting), or code on a real-time frame path, where cudaMalloc and
+ * cudaFree may synchronise the device and stall every stream. The caller passes the inputs and
+ * the output; every intermediate lives in one file-scope device array of
+ * HMP_NOALLOC_SCRATCH_BYTES, which every GPU that loads the library holds until the process exits.
+ * The call allocates nothing (no cudaMalloc, cudaFree or allocating library routine).
+ *
+ * image1, image2: already-remapped RGBA8 frames of the same size (device, batch_size frames each
+ * at data + b*pitch*height); seam: device, height rows of seam_pitch bytes, 1 = image 1, 0 =
+ * image 2 (the two-image seam in its inverted form); out: same size as the images. The result
+ * equals hmp_stitcher_process of a two-image stitcher whose tables are the identity, with both
+ * images at (0, 0) and minimize_blend = 0. Work is enqueued on `stream`.
+ *
+ * Sizes whose scratch exceeds HMP_NOALLOC_SCRATCH_BYTES are rejected with HMP_ERR_INVALID_VALUE
+ * and a message giving the bytes needed. The first call on a device does the set-up (it looks up
+ * the array's device address and sets kernel attributes), so make it before any stream capture.
+ * Every call shares the one array, which keeps the last call's contents; calls whose work
+ * overlaps on the GPU (other streams, other host threads) race on it and must be serialised. */
+HMP_API hmp_status hmp_blend2_noalloc(const hmp_image* image1, const hmp_image* image2, const uint8_t* seam,
+                                      size_t seam_pitch, int num_levels, int batch_size, const hmp_image* out,
+                                      void* stream);
+
 /* Geometry of a configuration computed on the host only (no device work): blend rect, write
  * rect and effective levels, out9 = {bx, by, bw, bh, wx, wy, ww, wh, levels}; also the canvas
  * size. Mirrors CanvasManager::updateMinimizeBlend / convertMaskMat (src/pano/canvasManager.cpp:
