@@ -56,12 +56,119 @@ struct DownAcc {
       ++cnt;
     }
   }
+  // s / count. Division by 1, 2 or 4 equals the (correctly rounded) product with 1, 0.5 or 0.25,
+  // so only a count of 3 needs a division.
   __device__ __forceinline__ float4 result() const {
+    if (cnt == 4) return make_float4(s0 * 0.25f, s1 * 0.25f, s2 * 0.25f, amax);
     if (cnt == 0) return make_float4(0.f, 0.f, 0.f, amax);
-    const float c = float(cnt);
-    return make_float4(s0 / c, s1 / c, s2 / c, amax);
+    if (cnt == 2) return make_float4(s0 * 0.5f, s1 * 0.5f, s2 * 0.5f, amax);
+    if (cnt == 1) return make_float4(s0, s1, s2, amax);
+    return make_float4(s0 / 3.f, s1 / 3.f, s2 / 3.f, amax);
   }
 };
+
+// Source pixel of slot k for a looked-up (owner, entry). A slot without an owner plane only ever
+// reads image k (outside its plane the entry is the sentinel, which reads as zero), so it skips
+// the owner select.
+template <int NMAX>
+__device__ __forceinline__ uchar4 slot_fetch(const PyrArgs& a, int k, int own, uint32_t e, int b, bool opaque) {
+  if (a.slot[k].owner != nullptr) return fetch_sel<NMAX>(a.S, own, e, b, opaque);
+  const int sx = int(e & 0xFFFFu), sy = int(e >> 16);
+  uchar4 out = make_uchar4(0, 0, 0, 0);
+  if (sx < a.S.w[k] && sy < a.S.h[k]) {
+    const char* base = reinterpret_cast<const char*>(a.S.ptr[k]) + b * a.S.bstride[k];
+    out = __ldg(reinterpret_cast<const uchar4*>(base + (long long)sy * int(a.S.pitch[k])) + sx);
+  } else if (opaque && sx != 0xFFFF) {
+    out.w = 255;
+  }
+  return out;
+}
+
+// Blends whose weights are one-hot need a single Laplacian. With weight 1 on image s and 0 on
+// the others, every rule below returns Lap_s's colour up to the sign of a zero (1*x + 0*y = x
+// unless x is a zero) and an alpha known from the alphas alone; a zero's sign never changes a
+// later non-zero sum, product or alpha test, and the uint8 pack maps both zeros to 0. So the
+// up-pass computes the Laplacian of the picked image only:
+//   pick >= 0 : the result is Lap_pick's colour with the alpha of blend_alpha();
+//   kPickNone : the result is (0, 0, 0, 0);
+//   kPickAll  : fractional weights, the full blend of every Laplacian.
+constexpr int kPickNone = -1, kPickAll = -2;
+
+// First image of strictly largest non-zero alpha (the rules' fallback when no weighted image has
+// alpha), or kPickNone.
+template <int NMAX>
+__device__ __forceinline__ int pick_max_alpha(int n, const float* al) {
+  float amax = 0.f;
+  int idx = kPickNone;
+#pragma unroll
+  for (int k = 0; k < NMAX; ++k)
+    if (k < n && al[k] > amax) {
+      amax = al[k];
+      idx = k;
+    }
+  return idx;
+}
+
+// Level 0: the seam value v is the two-image weight of image 1, or the label (one-hot weights).
+template <int RULE, int NMAX>
+__device__ __forceinline__ int blend_pick0(int n, const float* al, int v) {
+  if (RULE == kRuleTwo) {
+    if (al[0] == 0.f) return 1;  // blend_two returns b
+    if (al[1] == 0.f) return 0;  // blend_two returns a
+    if (v == 1) return 0;
+    if (v == 0) return 1;
+    return kPickAll;
+  }
+  float alv = 0.f;
+#pragma unroll
+  for (int k = 0; k < NMAX; ++k)
+    if (k == v) alv = al[k];
+  if (v < n && alv != 0.f) return v;
+  return pick_max_alpha<NMAX>(n, al);
+}
+
+// Levels >= 1: mask values m[0..K).
+template <int RULE, int NMAX>
+__device__ __forceinline__ int blend_pick(int n, const float* al, const float* m) {
+  if (RULE == kRuleTwo) {
+    if (al[0] == 0.f) return 1;
+    if (al[1] == 0.f) return 0;
+    if (m[0] == 1.f) return 0;
+    if (m[0] == 0.f) return 1;
+    return kPickAll;
+  }
+  int hot = kPickNone;
+  bool onehot = true;
+#pragma unroll
+  for (int k = 0; k < NMAX; ++k) {
+    if (k >= n) break;
+    if (m[k] == 1.f) {
+      if (hot != kPickNone) onehot = false;
+      hot = k;
+    } else if (m[k] != 0.f) {
+      onehot = false;
+    }
+  }
+  if (!onehot) return kPickAll;
+  float alh = 0.f;
+#pragma unroll
+  for (int k = 0; k < NMAX; ++k)
+    if (k == hot) alh = al[k];
+  if (hot != kPickNone && alh != 0.f) return hot;
+  return pick_max_alpha<NMAX>(n, al);
+}
+
+// Alpha of a picked blend: the two-image rule keeps b's alpha unless b has none; the others
+// keep the picked image's.
+template <int RULE, int NMAX>
+__device__ __forceinline__ float blend_alpha(const float* al, int pick) {
+  if (RULE == kRuleTwo) return al[1] == 0.f ? al[0] : al[1];
+  float r = 0.f;
+#pragma unroll
+  for (int k = 0; k < NMAX; ++k)
+    if (k == pick) r = al[k];
+  return r;
+}
 
 // Gaussian levels 1..L-1 of every slot for one TD x TD level-0 tile. Level 1 is gathered straight
 // from the sources (all slots' table lookups first, then all source loads, then the reductions);
@@ -85,7 +192,7 @@ __global__ void __launch_bounds__(256) pyr_down_kernel(const __grid_constant__ P
     active[k] = k < n && !(X0 >= P.x0 + P.w || Y0 >= P.y0 + P.h || X0 + TD <= P.x0 || Y0 + TD <= P.y0);
   }
   const int lw0 = a.lw[0], lh0 = a.lh[0], lw1 = a.lw[1], lh1 = a.lh[1];
-#pragma unroll 1
+#pragma unroll 2
   for (int i = threadIdx.x; i < T1 * T1; i += blockDim.x) {
     const int tx = i % T1, ty = i / T1;
     const int gx = (X0 >> 1) + tx, gy = (Y0 >> 1) + ty;
@@ -105,7 +212,7 @@ __global__ void __launch_bounds__(256) pyr_down_kernel(const __grid_constant__ P
 #pragma unroll
     for (int k = 0; k < NMAX; ++k)
 #pragma unroll
-      for (int q = 0; q < 4; ++q) px[k][q] = fetch_sel<NMAX>(a.S, own[k][q], ent[k][q], b, opaque);
+      for (int q = 0; q < 4; ++q) px[k][q] = slot_fetch<NMAX>(a, k, own[k][q], ent[k][q], b, opaque);
 #pragma unroll
     for (int k = 0; k < NMAX; ++k) {
       if (!active[k]) continue;
@@ -335,47 +442,6 @@ __device__ __forceinline__ float4 ldg_level(const half4* p) {
   return make_float4(fa.x, fa.y, fb.x, fb.y);
 }
 
-// up_alpha over a full level buffer in HBM (row stride lw): same taps, order and exactness
-// argument as up_alpha above.
-template <typename T>
-__device__ __forceinline__ float3 up_alpha_g(const T* buf, int lw, int lh, int x, int y) {
-  const int gxi = x >> 1, gyi = y >> 1;
-  const T* r0 = buf + (long long)gyi * lw;
-  const float4 p00 = ldg_level(r0 + gxi);
-  const bool ox = (x & 1) != 0, oy = (y & 1) != 0;
-  if (!ox && !oy) {
-    if (p00.w != 0.f) return make_float3(p00.x, p00.y, p00.z);
-    return make_float3(0.f, 0.f, 0.f);
-  }
-  if (ox != oy) {
-    const float4 p1 = ox ? ldg_level(r0 + min(gxi + 1, lw - 1)) : ldg_level(buf + (long long)min(gyi + 1, lh - 1) * lw + gxi);
-    const bool v0 = p00.w != 0.f, v1 = p1.w != 0.f;
-    if (v0 && v1)
-      return make_float3(p00.x * 0.5f + p1.x * 0.5f, p00.y * 0.5f + p1.y * 0.5f, p00.z * 0.5f + p1.z * 0.5f);
-    if (v0) return make_float3((p00.x * 0.5f) * 2.f, (p00.y * 0.5f) * 2.f, (p00.z * 0.5f) * 2.f);
-    if (v1) return make_float3((p1.x * 0.5f) * 2.f, (p1.y * 0.5f) * 2.f, (p1.z * 0.5f) * 2.f);
-    return make_float3(0.f, 0.f, 0.f);
-  }
-  const int gxi1 = min(gxi + 1, lw - 1), gyi1 = min(gyi + 1, lh - 1);
-  const T* r1 = buf + (long long)gyi1 * lw;
-  const float4 q[4] = {p00, ldg_level(r0 + gxi1), ldg_level(r1 + gxi), ldg_level(r1 + gxi1)};
-  float sw = 0.f, s0 = 0.f, s1 = 0.f, s2 = 0.f;
-#pragma unroll
-  for (int i = 0; i < 4; ++i) {
-    if (q[i].w != 0.f) {
-      sw += 0.25f;
-      s0 += q[i].x * 0.25f;
-      s1 += q[i].y * 0.25f;
-      s2 += q[i].z * 0.25f;
-    }
-  }
-  if (sw == 1.f) return make_float3(s0, s1, s2);
-  if (sw == 0.5f) return make_float3(s0 * 2.f, s1 * 2.f, s2 * 2.f);
-  if (sw == 0.25f) return make_float3(s0 * 4.f, s1 * 4.f, s2 * 4.f);
-  if (sw > 0.f) return make_float3(s0 / sw, s1 / sw, s2 / sw);
-  return make_float3(0.f, 0.f, 0.f);
-}
-
 // pyr_coarse: R^1 (the reconstruction at level 1) for one T1 x T1 tile of level-1 pixels.
 // Levels 2..L-1 of the tile plus the upsample halo are loaded into shared memory up front (one
 // wait on memory), blended and reconstructed from the coarsest level down; level 1 reads G^1 and
@@ -464,23 +530,39 @@ __global__ void __launch_bounds__(256) pyr_coarse_kernel(const __grid_constant__
       if (x >= rw || y >= rh) continue;
       const int i = y * CW + x;
       const int px = lax + x, py = lay + y;
-      float4 lap[NMAX];
+      float al[NMAX];
 #pragma unroll
-      for (int k = 0; k < NMAX; ++k) {
-        if (k < n) {
-          float4 g = gcur[k * CAP + i];
-          if (has_next) {
-            const float3 up = up_alpha(gnext + k * CAPN, CWN, nax, nay, lwn, lhn, px, py);
-            g.x = g.x - up.x;
-            g.y = g.y - up.y;
-            g.z = g.z - up.z;
-          }
-          lap[k] = g;
-        } else {
-          lap[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+      for (int k = 0; k < NMAX; ++k) al[k] = k < n ? gcur[k * CAP + i].w : 0.f;
+      const int pk = blend_pick<RULE, NMAX>(n, al, mb + i * K);
+      float4 r = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (pk >= 0) {
+        float4 g = gcur[pk * CAP + i];
+        if (has_next) {
+          const float3 up = up_alpha(gnext + pk * CAPN, CWN, nax, nay, lwn, lhn, px, py);
+          g.x = g.x - up.x;
+          g.y = g.y - up.y;
+          g.z = g.z - up.z;
         }
+        r = make_float4(g.x, g.y, g.z, blend_alpha<RULE, NMAX>(al, pk));
+      } else if (pk == kPickAll) {
+        float4 lap[NMAX];
+#pragma unroll
+        for (int k = 0; k < NMAX; ++k) {
+          if (k < n) {
+            float4 g = gcur[k * CAP + i];
+            if (has_next) {
+              const float3 up = up_alpha(gnext + k * CAPN, CWN, nax, nay, lwn, lhn, px, py);
+              g.x = g.x - up.x;
+              g.y = g.y - up.y;
+              g.z = g.z - up.z;
+            }
+            lap[k] = g;
+          } else {
+            lap[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+          }
+        }
+        r = blend_level<RULE, NMAX>(n, lap, mb + i * K);
       }
-      float4 r = blend_level<RULE, NMAX>(n, lap, mb + i * K);
       if (has_next) {
         const float3 up = up_alpha(rnext, CWN, nax, nay, lwn, lhn, px, py);
         r.x = up.x + r.x;
@@ -512,23 +594,40 @@ __global__ void __launch_bounds__(256) pyr_coarse_kernel(const __grid_constant__
     float m[NMAX];
 #pragma unroll
     for (int q = 0; q < NMAX; ++q) m[q] = q < K ? __ldg(a.maskL[1] + o1 * K + q) : 0.f;
-    float4 lap[NMAX];
+    float4 g1[NMAX];
+    float al[NMAX];
 #pragma unroll
     for (int k = 0; k < NMAX; ++k) {
-      if (k < n) {
-        float4 g = ldg_level(static_cast<const Store*>(a.G[k][1]) + (long long)b * lw1 * lh1 + o1);
-        if (has2) {
-          const float3 up = up_alpha(g2 + k * CAP2, CW2, nax, nay, lw2, lh2, px, py);
-          g.x = g.x - up.x;
-          g.y = g.y - up.y;
-          g.z = g.z - up.z;
-        }
-        lap[k] = g;
-      } else {
-        lap[k] = make_float4(0.f, 0.f, 0.f, 0.f);
-      }
+      g1[k] = k < n ? ldg_level(static_cast<const Store*>(a.G[k][1]) + (long long)b * lw1 * lh1 + o1)
+                    : make_float4(0.f, 0.f, 0.f, 0.f);
+      al[k] = g1[k].w;
     }
-    float4 r = blend_level<RULE, NMAX>(n, lap, m);
+    const int pk = blend_pick<RULE, NMAX>(n, al, m);
+    float4 r = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (pk >= 0) {
+      float4 g = g1[0];
+#pragma unroll
+      for (int k = 1; k < NMAX; ++k)
+        if (k == pk) g = g1[k];
+      if (has2) {
+        const float3 up = up_alpha(g2 + pk * CAP2, CW2, nax, nay, lw2, lh2, px, py);
+        g.x = g.x - up.x;
+        g.y = g.y - up.y;
+        g.z = g.z - up.z;
+      }
+      r = make_float4(g.x, g.y, g.z, blend_alpha<RULE, NMAX>(al, pk));
+    } else if (pk == kPickAll) {
+#pragma unroll
+      for (int k = 0; k < NMAX; ++k) {
+        if (k < n && has2) {
+          const float3 up = up_alpha(g2 + k * CAP2, CW2, nax, nay, lw2, lh2, px, py);
+          g1[k].x = g1[k].x - up.x;
+          g1[k].y = g1[k].y - up.y;
+          g1[k].z = g1[k].z - up.z;
+        }
+      }
+      r = blend_level<RULE, NMAX>(n, g1, m);
+    }
     if (has2) {
       const float3 up = up_alpha(r2, CW2, nax, nay, lw2, lh2, px, py);
       r.x = up.x + r.x;
@@ -539,21 +638,98 @@ __global__ void __launch_bounds__(256) pyr_coarse_kernel(const __grid_constant__
   }
 }
 
-// pyr_fine: level 0 of the write region. Each warp owns a 64 x 2 pixel block, each lane the 2x2
-// pixels (X, Y)..(X+1, Y+1), processed in the four parity passes so the upsample branches are
-// uniform across the warp. All table lookups, then all source gathers, are issued before any
-// arithmetic; G^1 and R^1 taps come from HBM through the cache (neighbouring lanes and passes
-// share them). Lap_k = G^0_k - up(G^1_k), blend with the level-0 seam value, R^0 = up(R^1) +
-// blend, truncating pack into the canvas. No shared memory, no barriers.
+// Level-1 tile of a pyr_fine CTA: the 32 x 8 level-1 pixels under its 64 x 16 level-0 block
+// plus the +1 column and row the bilinear upsample reads, with coordinates clamped to the level
+// (so the tile holds the clamped taps and the upsample needs no bounds checks).
+constexpr int kFineTW = 33, kFineTH = 9, kFineTA = kFineTW * kFineTH;
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+template <int BYTES>
+__device__ __forceinline__ void cp_async(void* dst, const void* src) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], %2;\n" ::"r"(smem_u32(dst)), "l"(src), "n"(BYTES));
+}
+
+// G^1 buffer of slot k, frame b (k selected at run time among the NMAX slots).
+template <int NMAX, typename Store>
+__device__ __forceinline__ const Store* g1_of(const PyrArgs& a, int k, int b) {
+  const void* p = a.G[0][1];
+#pragma unroll
+  for (int j = 1; j < NMAX; ++j)
+    if (j == k) p = a.G[j][1];
+  return static_cast<const Store*>(p) + (long long)b * a.lw[1] * a.lh[1];
+}
+
+// up_alpha from a pyr_fine tile: tap (0,0) at t[i]; (1,0) at t[i+1], (0,1) at t[i+TW]. Same
+// taps, order and exact shortcuts as up_alpha.
+template <typename T>
+__device__ __forceinline__ float3 up_tile(const T* t, int i, bool ox, bool oy) {
+  const float4 p00 = load_level(t + i);
+  if (!ox && !oy) {
+    if (p00.w != 0.f) return make_float3(p00.x, p00.y, p00.z);
+    return make_float3(0.f, 0.f, 0.f);
+  }
+  if (ox != oy) {
+    const float4 p1 = load_level(t + i + (ox ? 1 : kFineTW));
+    const bool v0 = p00.w != 0.f, v1 = p1.w != 0.f;
+    if (v0 && v1)
+      return make_float3(p00.x * 0.5f + p1.x * 0.5f, p00.y * 0.5f + p1.y * 0.5f, p00.z * 0.5f + p1.z * 0.5f);
+    if (v0) return make_float3((p00.x * 0.5f) * 2.f, (p00.y * 0.5f) * 2.f, (p00.z * 0.5f) * 2.f);
+    if (v1) return make_float3((p1.x * 0.5f) * 2.f, (p1.y * 0.5f) * 2.f, (p1.z * 0.5f) * 2.f);
+    return make_float3(0.f, 0.f, 0.f);
+  }
+  const float4 q[4] = {p00, load_level(t + i + 1), load_level(t + i + kFineTW), load_level(t + i + kFineTW + 1)};
+  float sw = 0.f, s0 = 0.f, s1 = 0.f, s2 = 0.f;
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    if (q[j].w != 0.f) {
+      sw += 0.25f;
+      s0 += q[j].x * 0.25f;
+      s1 += q[j].y * 0.25f;
+      s2 += q[j].z * 0.25f;
+    }
+  }
+  if (sw == 1.f) return make_float3(s0, s1, s2);
+  if (sw == 0.5f) return make_float3(s0 * 2.f, s1 * 2.f, s2 * 2.f);
+  if (sw == 0.25f) return make_float3(s0 * 4.f, s1 * 4.f, s2 * 4.f);
+  if (sw > 0.f) return make_float3(s0 / sw, s1 / sw, s2 / sw);
+  return make_float3(0.f, 0.f, 0.f);
+}
+
+// pyr_fine: level 0 of the write region. A CTA owns a 64 x 16 pixel block, each warp 64 x 2 of
+// it, each lane the 2x2 quad (X, Y)..(X+1, Y+1). The CTA first copies its level-1 tiles (G^1 of
+// every slot, R^1) into shared memory with cp.async, then issues all its table lookups and
+// source gathers, and waits for the tiles only after that. Per pixel: Lap = G^0 - up(G^1) of the
+// picked image (of every image where the weights are fractional), blend, add up(R^1), truncating
+// pack into the canvas.
 template <int RULE, int NMAX, typename Store>
 __global__ void __launch_bounds__(256) pyr_fine_kernel(const __grid_constant__ PyrArgs a) {
+  extern __shared__ float4 fsm[];  // R^1 tile, then G^1 tiles of slots 0..n-1 (Store)
   const int n = RULE == kRuleNway ? a.n : NMAX;
   const int b = blockIdx.z;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int X = (a.wx0 & ~1) + blockIdx.x * 64 + 2 * lane;
-  const int Y = (a.wy0 & ~1) + blockIdx.y * 16 + 2 * warp;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int bx0 = (a.wx0 & ~1) + blockIdx.x * 64, by0 = (a.wy0 & ~1) + blockIdx.y * 16;
+  const int X = bx0 + 2 * lane, Y = by0 + 2 * warp;
   const bool opaque = a.opaque != 0;
-  const int lw0 = a.lw[0], lh0 = a.lh[0];
+  const bool has1 = a.levels > 1;
+  const int lw0 = a.lw[0], lh0 = a.lh[0], lw1 = a.lw[1], lh1 = a.lh[1];
+  float4* rs = fsm;
+  Store* gs = reinterpret_cast<Store*>(fsm + kFineTA);
+  if (has1) {
+    const int tx0 = bx0 >> 1, ty0 = by0 >> 1;
+    const long long fo = (long long)b * lw1 * lh1;
+    for (int i = tid; i < (n + 1) * kFineTA; i += 256) {
+      const int s = i / kFineTA, j = i - s * kFineTA;
+      const int y = min(ty0 + j / kFineTW, lh1 - 1), x = min(tx0 + j % kFineTW, lw1 - 1);
+      const long long o = fo + (long long)y * lw1 + x;
+      if (s == 0)
+        cp_async<16>(rs + j, a.R1 + o);
+      else
+        cp_async<int(sizeof(Store))>(gs + (s - 1) * kFineTA + j, g1_of<NMAX, Store>(a, s - 1, 0) + o);
+    }
+    asm volatile("cp.async.commit_group;\n" ::: "memory");
+  }
   int own[4][NMAX], mv[4];
   uint32_t ent[4][NMAX];
   bool live[4];
@@ -573,34 +749,56 @@ __global__ void __launch_bounds__(256) pyr_fine_kernel(const __grid_constant__ P
 #pragma unroll
   for (int q = 0; q < 4; ++q)
 #pragma unroll
-    for (int k = 0; k < NMAX; ++k) src[q][k] = fetch_sel<NMAX>(a.S, own[q][k], ent[q][k], b, opaque);
-  const bool has1 = a.levels > 1;
-  const int lw1 = a.lw[1], lh1 = a.lh[1];
-  const float4* R1 = a.R1 + (long long)b * lw1 * lh1;
+    for (int k = 0; k < NMAX; ++k) src[q][k] = slot_fetch<NMAX>(a, k, own[q][k], ent[q][k], b, opaque);
+  if (has1) {
+    asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+    __syncthreads();
+  }
+  const int ti = warp * kFineTW + lane;  // tap (0,0) of the quad in the tiles
 #pragma unroll
   for (int q = 0; q < 4; ++q) {
     if (!live[q]) continue;
-    const int px = X + (q & 1), py = Y + (q >> 1);
-    float4 lap[NMAX];
+    const bool ox = (q & 1) != 0, oy = (q >> 1) != 0;
+    float al[NMAX];
 #pragma unroll
-    for (int k = 0; k < NMAX; ++k) {
-      float4 g = to_f4(src[q][k]);
-      if (has1 && k < n) {
-        const float3 up =
-            up_alpha_g(static_cast<const Store*>(a.G[k][1]) + (long long)b * lw1 * lh1, lw1, lh1, px, py);
+    for (int k = 0; k < NMAX; ++k) al[k] = float(src[q][k].w);
+    const int pk = blend_pick0<RULE, NMAX>(n, al, mv[q]);
+    float4 r = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (pk >= 0) {
+      uchar4 sp = src[q][0];
+#pragma unroll
+      for (int k = 1; k < NMAX; ++k)
+        if (k == pk) sp = src[q][k];
+      float4 g = to_f4(sp);
+      if (has1) {
+        const float3 up = up_tile(gs + pk * kFineTA, ti, ox, oy);
         g.x = g.x - up.x;
         g.y = g.y - up.y;
         g.z = g.z - up.z;
       }
-      lap[k] = g;
+      r = make_float4(g.x, g.y, g.z, blend_alpha<RULE, NMAX>(al, pk));
+    } else if (pk == kPickAll) {
+      float4 lap[NMAX];
+#pragma unroll
+      for (int k = 0; k < NMAX; ++k) {
+        float4 g = to_f4(src[q][k]);
+        if (has1 && k < n) {
+          const float3 up = up_tile(gs + k * kFineTA, ti, ox, oy);
+          g.x = g.x - up.x;
+          g.y = g.y - up.y;
+          g.z = g.z - up.z;
+        }
+        lap[k] = g;
+      }
+      r = blend_level0<RULE, NMAX>(n, lap, mv[q]);
     }
-    float4 r = blend_level0<RULE, NMAX>(n, lap, mv[q]);
     if (has1) {
-      const float3 up = up_alpha_g(R1, lw1, lh1, px, py);
+      const float3 up = up_tile(rs, ti, ox, oy);
       r.x = up.x + r.x;
       r.y = up.y + r.y;
       r.z = up.z + r.z;
     }
+    const int px = X + (q & 1), py = Y + (q >> 1);
     uchar4* crow = reinterpret_cast<uchar4*>(reinterpret_cast<char*>(a.C.ptr) + b * a.C.bstride +
                                              (long long)(py + a.cy_off) * a.C.pitch);
     crow[px + a.cx_off] = pack_rgba(r);
@@ -650,12 +848,13 @@ void coarse_dispatch(const PyrArgs& a, int rule, dim3 grid, size_t smem, cudaStr
 
 template <typename Store>
 void fine_dispatch(const PyrArgs& a, int rule, dim3 grid, cudaStream_t stream) {
+  const size_t smem = a.levels > 1 ? size_t(kFineTA) * (sizeof(float4) + size_t(a.n) * sizeof(Store)) : 0;
   if (rule == kRuleTwo)
-    pyr_fine_kernel<kRuleTwo, 2, Store><<<grid, 256, 0, stream>>>(a);
+    pyr_fine_kernel<kRuleTwo, 2, Store><<<grid, 256, smem, stream>>>(a);
   else if (rule == kRuleThree)
-    pyr_fine_kernel<kRuleThree, 3, Store><<<grid, 256, 0, stream>>>(a);
+    pyr_fine_kernel<kRuleThree, 3, Store><<<grid, 256, smem, stream>>>(a);
   else
-    pyr_fine_kernel<kRuleNway, 8, Store><<<grid, 256, 0, stream>>>(a);
+    pyr_fine_kernel<kRuleNway, 8, Store><<<grid, 256, smem, stream>>>(a);
 }
 
 }  // namespace

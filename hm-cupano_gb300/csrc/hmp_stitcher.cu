@@ -131,6 +131,8 @@ struct hmp_stitcher {
       if (e != cudaSuccess) return cuda_status(e, "canvas plane upload");
     }
     launches = p.canvas_plane_used ? 1 : 0;
+    if (p.levels > 0 && p.filter != HMP_FILTER_REFBOX)
+      return make_status(HMP_ERR_NOT_SUPPORTED, "the Binomial5 pyramid filter has no GPU kernels in this build");
     if (p.levels > 0) {
       const int n = p.n, B = p.batch, L = p.levels;
       for (int k = 0; k < n; ++k) {
