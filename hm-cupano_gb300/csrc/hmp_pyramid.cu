@@ -33,6 +33,18 @@ namespace {
 constexpr int kRuleNway = 1, kRuleTwo = 2, kRuleThree = 3;
 constexpr int kL = kDevMaxLevels;
 
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+template <int BYTES>
+__device__ __forceinline__ void cp_async(void* dst, const void* src) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], %2;\n" ::"r"(smem_u32(dst)), "l"(src), "n"(BYTES));
+}
+__device__ __forceinline__ void cp_async_commit_wait_all() {
+  asm volatile("cp.async.commit_group;\n" ::: "memory");
+  asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+}
+
 // Table lookup of slot k at (x, y); the owner is k unless the slot has an owner plane.
 __device__ __forceinline__ void slot_lookup(const PlaneDev& P, int k, int x, int y, int& owner, uint32_t& entry) {
   const int rx = x - P.x0, ry = y - P.y0;
@@ -170,70 +182,167 @@ __device__ __forceinline__ float blend_alpha(const float* al, int pick) {
   return r;
 }
 
-// Gaussian levels 1..L-1 of every slot for one TD x TD level-0 tile. Level 1 is gathered straight
-// from the sources (all slots' table lookups first, then all source loads, then the reductions);
-// deeper levels reduce the previous level in shared memory. A slot whose plane misses the tile
-// produces zeros, which its level buffers already hold, so it is skipped entirely.
+// Source pixel address of slot k for table entry e (owner o when the slot has an owner plane),
+// or nullptr with the pixel to store instead: zero, or alpha 255 under the soft-seam ("opaque")
+// rule for an out-of-range entry that is not the 65535 sentinel (src/cuda/cudaRemap.cu:60-123).
+template <int NMAX>
+__device__ __forceinline__ const uchar4* slot_src(const PyrArgs& a, int k, int o, uint32_t e, int b, bool opaque,
+                                                  uint32_t& fill) {
+  const int sx = int(e & 0xFFFFu), sy = int(e >> 16);
+  fill = 0u;
+  if (a.slot[k].owner == nullptr) o = k;
+  const uchar4* p = nullptr;
+  bool known = false;
+#pragma unroll
+  for (int q = 0; q < NMAX; ++q) {
+    if (o == q) {
+      known = true;
+      if (sx < a.S.w[q] && sy < a.S.h[q])
+        p = reinterpret_cast<const uchar4*>(reinterpret_cast<const char*>(a.S.ptr[q]) + b * a.S.bstride[q] +
+                                            (long long)sy * int(a.S.pitch[q])) + sx;
+    }
+  }
+  if (!p && known && opaque && sx != 0xFFFF) fill = 0xFF000000u;
+  return p;
+}
+
+__device__ __forceinline__ float4 u32_to_f4(uint32_t v) {
+  return make_float4(float(v & 0xFFu), float((v >> 8) & 0xFFu), float((v >> 16) & 0xFFu), float(v >> 24));
+}
+
+// Level-l buffer of slot k, frame b (k selected at run time among the NMAX slots).
+template <int NMAX, typename Store>
+__device__ __forceinline__ Store* level_of(const PyrArgs& a, int k, int l, int b) {
+  void* p = a.G[0][l];
+#pragma unroll
+  for (int j = 1; j < NMAX; ++j)
+    if (j == k) p = a.G[j][l];
+  return static_cast<Store*>(p) + (long long)b * a.lw[l] * a.lh[l];
+}
+
+// Gaussian levels 1..L-1 of every slot for one TD x TD level-0 tile (TD a multiple of 2^(L-1),
+// so no level needs a neighbouring tile). Level 0 is gathered like the canvas: each warp owns
+// tile rows, copies their table entries into shared memory (cp.async, 32 consecutive entries
+// per instruction), then replaces every entry by its source pixel (one 4-byte cp.async each, all
+// in flight together). One pass then reduces each 4x4 pixel block to its four level-1 pixels
+// (kept in registers and stored to HBM) and their level-2 pixel; deeper levels reduce the
+// previous level in shared memory (levels 3, 5 reuse the level-0 buffer). Every level >= 1 goes
+// to HBM. A slot whose plane misses the tile produces zeros, which its level buffers already
+// hold, so it is skipped entirely.
 template <int NMAX, typename Store, int TD>
 __global__ void __launch_bounds__(256) pyr_down_kernel(const __grid_constant__ PyrArgs a) {
-  constexpr int T1 = TD / 2, T2 = TD / 4;
+  constexpr int T1 = TD / 2, T2 = TD / 4, A2 = T2 * T2;
   extern __shared__ float4 sm[];
   const int n = a.n;
-  float4* bufA = sm;                // levels 1, 3, 5: [n][T1*T1]
-  float4* bufB = sm + n * T1 * T1;  // levels 2, 4, 6: [n][T2*T2]
+  uint32_t* pix = reinterpret_cast<uint32_t*>(sm);  // level 0: [n][TD][TD] pixels
+  float4* bufA = sm;                                // levels 3, 5: [n][T1*T1], over level 0
+  float4* bufB = sm + n * T1 * T1;                  // levels 2, 4, 6: [n][T2*T2]
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int b = blockIdx.z;
   const int X0 = blockIdx.x * TD, Y0 = blockIdx.y * TD;
   const bool opaque = a.opaque != 0;
   const int L = a.levels;
+  const int lw0 = a.lw[0], lh0 = a.lh[0], lw1 = a.lw[1], lh1 = a.lh[1];
   bool active[NMAX];
+  uint32_t amask = 0;
 #pragma unroll
   for (int k = 0; k < NMAX; ++k) {
     const PlaneDev& P = a.slot[k];
     active[k] = k < n && !(X0 >= P.x0 + P.w || Y0 >= P.y0 + P.h || X0 + TD <= P.x0 || Y0 + TD <= P.y0);
+    if (active[k]) amask |= 1u << k;
   }
-  const int lw0 = a.lw[0], lh0 = a.lh[0], lw1 = a.lw[1], lh1 = a.lh[1];
-#pragma unroll 2
-  for (int i = threadIdx.x; i < T1 * T1; i += blockDim.x) {
-    const int tx = i % T1, ty = i / T1;
-    const int gx = (X0 >> 1) + tx, gy = (Y0 >> 1) + ty;
-    const bool inside = gx < lw1 && gy < lh1;
-    int own[NMAX][4];
-    uint32_t ent[NMAX][4];
+  // Level 0, step 1: table entries (the sentinel outside the level or the plane).
 #pragma unroll
-    for (int k = 0; k < NMAX; ++k)
+  for (int k = 0; k < NMAX; ++k) {
+    if (!active[k]) continue;
+    const PlaneDev& P = a.slot[k];
+    uint32_t* pk = pix + k * TD * TD;
+    for (int r = warp; r < TD; r += 8) {
+      const int y = Y0 + r, ry = y - P.y0;
 #pragma unroll
-      for (int q = 0; q < 4; ++q) {
-        const int ix = 2 * gx + (q & 1), iy = 2 * gy + (q >> 1);
-        own[k][q] = 0xFF;
-        ent[k][q] = 0xFFFFFFFFu;
-        if (active[k] && inside && ix < lw0 && iy < lh0) slot_lookup(a.slot[k], k, ix, iy, own[k][q], ent[k][q]);
+      for (int j = 0; j < TD / 32; ++j) {
+        const int x = X0 + 32 * j + lane, rx = x - P.x0;
+        uint32_t* d = pk + r * TD + 32 * j + lane;
+        if (x < lw0 && y < lh0 && (unsigned)rx < (unsigned)P.w && (unsigned)ry < (unsigned)P.h)
+          cp_async<4>(d, P.map + (long long)ry * P.map_pitch + rx);
+        else
+          *d = 0xFFFFFFFFu;
       }
-    uchar4 px[NMAX][4];
+    }
+  }
+  cp_async_commit_wait_all();
+  // Step 2: each thread replaces the entries it copied by their source pixels.
 #pragma unroll
-    for (int k = 0; k < NMAX; ++k)
+  for (int k = 0; k < NMAX; ++k) {
+    if (!active[k]) continue;
+    const PlaneDev& P = a.slot[k];
+    uint32_t* pk = pix + k * TD * TD;
+    for (int r = warp; r < TD; r += 8) {
+      const int y = Y0 + r, ry = y - P.y0;
 #pragma unroll
-      for (int q = 0; q < 4; ++q) px[k][q] = slot_fetch<NMAX>(a, k, own[k][q], ent[k][q], b, opaque);
+      for (int j = 0; j < TD / 32; ++j) {
+        const int x = X0 + 32 * j + lane, rx = x - P.x0;
+        uint32_t* d = pk + r * TD + 32 * j + lane;
+        const uint32_t e = *d;
+        int o = k;
+        if (P.owner != nullptr)
+          o = (x < lw0 && y < lh0 && (unsigned)rx < (unsigned)P.w && (unsigned)ry < (unsigned)P.h)
+                  ? int(__ldg(P.owner + (long long)ry * P.owner_pitch + rx))
+                  : 0xFF;
+        uint32_t fill;
+        const uchar4* sp = slot_src<NMAX>(a, k, o, e, b, opaque, fill);
+        if (sp)
+          cp_async<4>(d, sp);
+        else
+          *d = fill;
+      }
+    }
+  }
+  cp_async_commit_wait_all();
+  __syncthreads();
+  // Levels 1 and 2: one item = one level-2 pixel of one slot = its four level-1 pixels, each the
+  // alpha-aware mean of a 2x2 level-0 block (two 8-byte shared loads), summed in (0,0), (1,0),
+  // (0,1), (1,1) order at both levels.
+  const bool has2 = L > 2;
+  const int lw2 = a.lw[has2 ? 2 : 1], lh2 = a.lh[has2 ? 2 : 1];
+  for (int it = tid; it < n * A2; it += 256) {
+    const int k = it / A2, j = it - k * A2;
+    if (!((amask >> k) & 1u)) continue;
+    const int tx2 = j % T2, ty2 = j / T2;
+    const int gx2 = (X0 >> 2) + tx2, gy2 = (Y0 >> 2) + ty2;
+    const uint32_t* pk = pix + k * TD * TD;
+    Store* G1 = level_of<NMAX, Store>(a, k, 1, b);
+    DownAcc acc2;
 #pragma unroll
-    for (int k = 0; k < NMAX; ++k) {
-      if (!active[k]) continue;
-      float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-      if (inside) {
+    for (int q = 0; q < 4; ++q) {
+      const int tx = 2 * tx2 + (q & 1), ty = 2 * ty2 + (q >> 1);
+      const int gx = (X0 >> 1) + tx, gy = (Y0 >> 1) + ty;
+      if (gx < lw1 && gy < lh1) {
+        const uint2 r0 = *reinterpret_cast<const uint2*>(pk + (2 * ty) * TD + 2 * tx);
+        const uint2 r1 = *reinterpret_cast<const uint2*>(pk + (2 * ty + 1) * TD + 2 * tx);
+        const bool xin = 2 * gx + 1 < lw0, yin = 2 * gy + 1 < lh0;
         DownAcc acc;
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-          const int ix = 2 * gx + (q & 1), iy = 2 * gy + (q >> 1);
-          if (ix < lw0 && iy < lh0) acc.add(to_f4(px[k][q]));
-        }
-        v = acc.result();
-        Store* G1 = static_cast<Store*>(a.G[k][1]) + (long long)b * lw1 * lh1;
+        acc.add(u32_to_f4(r0.x));
+        if (xin) acc.add(u32_to_f4(r0.y));
+        if (yin) acc.add(u32_to_f4(r1.x));
+        if (xin && yin) acc.add(u32_to_f4(r1.y));
+        const float4 v = acc.result();
         store_level(G1 + (long long)gy * lw1 + gx, v);
+        acc2.add(v);
       }
-      bufA[k * T1 * T1 + i] = v;
+    }
+    if (has2) {
+      float4 v2 = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (gx2 < lw2 && gy2 < lh2) {
+        v2 = acc2.result();
+        store_level(level_of<NMAX, Store>(a, k, 2, b) + (long long)gy2 * lw2 + gx2, v2);
+      }
+      bufB[k * A2 + j] = v2;
     }
   }
   __syncthreads();
 #pragma unroll
-  for (int l = 2; l < kL; ++l) {
+  for (int l = 3; l < kL; ++l) {
     if (l >= L) break;
     const int Tp = TD >> (l - 1), Tn = TD >> l;
     const int area = Tn * Tn;
@@ -408,23 +517,31 @@ __device__ __forceinline__ float4 blend_nway(const float4* L, int n, float* w) {
 // Blend of one pixel at level l >= 1 with mask values m[0..K).
 template <int RULE, int NMAX>
 __device__ __forceinline__ float4 blend_level(int n, const float4* lap, const float* m) {
-  if (RULE == kRuleTwo) return blend_two(lap[0], lap[1], m[0]);
-  if (RULE == kRuleThree) return blend_three(lap, m[0], m[1], m[2]);
-  float w[NMAX];
+  if constexpr (RULE == kRuleTwo) {
+    return blend_two(lap[0], lap[1], m[0]);
+  } else if constexpr (RULE == kRuleThree) {
+    return blend_three(lap, m[0], m[1], m[2]);
+  } else {
+    float w[NMAX];
 #pragma unroll
-  for (int k = 0; k < NMAX; ++k) w[k] = k < n ? m[k] : 0.f;
-  return blend_nway<NMAX>(lap, n, w);
+    for (int k = 0; k < NMAX; ++k) w[k] = k < n ? m[k] : 0.f;
+    return blend_nway<NMAX>(lap, n, w);
+  }
 }
 
 // Blend of one level-0 pixel from its seam value (two-image weight) or label (one-hot).
 template <int RULE, int NMAX>
 __device__ __forceinline__ float4 blend_level0(int n, const float4* lap, int v) {
-  if (RULE == kRuleTwo) return blend_two(lap[0], lap[1], float(v));
-  if (RULE == kRuleThree) return blend_three(lap, v == 0 ? 1.f : 0.f, v == 1 ? 1.f : 0.f, v == 2 ? 1.f : 0.f);
-  float w[NMAX];
+  if constexpr (RULE == kRuleTwo) {
+    return blend_two(lap[0], lap[1], float(v));
+  } else if constexpr (RULE == kRuleThree) {
+    return blend_three(lap, v == 0 ? 1.f : 0.f, v == 1 ? 1.f : 0.f, v == 2 ? 1.f : 0.f);
+  } else {
+    float w[NMAX];
 #pragma unroll
-  for (int k = 0; k < NMAX; ++k) w[k] = v == k ? 1.f : 0.f;
-  return blend_nway<NMAX>(lap, n, w);
+    for (int k = 0; k < NMAX; ++k) w[k] = v == k ? 1.f : 0.f;
+    return blend_nway<NMAX>(lap, n, w);
+  }
 }
 
 // Shared-memory row stride and capacity (pixels) of level l >= 1 for an up-tile of edge TU: the
@@ -643,23 +760,6 @@ __global__ void __launch_bounds__(256) pyr_coarse_kernel(const __grid_constant__
 // (so the tile holds the clamped taps and the upsample needs no bounds checks).
 constexpr int kFineTW = 33, kFineTH = 9, kFineTA = kFineTW * kFineTH;
 
-__device__ __forceinline__ uint32_t smem_u32(const void* p) {
-  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
-}
-template <int BYTES>
-__device__ __forceinline__ void cp_async(void* dst, const void* src) {
-  asm volatile("cp.async.ca.shared.global [%0], [%1], %2;\n" ::"r"(smem_u32(dst)), "l"(src), "n"(BYTES));
-}
-
-// G^1 buffer of slot k, frame b (k selected at run time among the NMAX slots).
-template <int NMAX, typename Store>
-__device__ __forceinline__ const Store* g1_of(const PyrArgs& a, int k, int b) {
-  const void* p = a.G[0][1];
-#pragma unroll
-  for (int j = 1; j < NMAX; ++j)
-    if (j == k) p = a.G[j][1];
-  return static_cast<const Store*>(p) + (long long)b * a.lw[1] * a.lh[1];
-}
 
 // up_alpha from a pyr_fine tile: tap (0,0) at t[i]; (1,0) at t[i+1], (0,1) at t[i+TW]. Same
 // taps, order and exact shortcuts as up_alpha.
@@ -719,14 +819,13 @@ __global__ void __launch_bounds__(256) pyr_fine_kernel(const __grid_constant__ P
   if (has1) {
     const int tx0 = bx0 >> 1, ty0 = by0 >> 1;
     const long long fo = (long long)b * lw1 * lh1;
-    for (int i = tid; i < (n + 1) * kFineTA; i += 256) {
-      const int s = i / kFineTA, j = i - s * kFineTA;
+    for (int j = tid; j < kFineTA; j += 256) {
       const int y = min(ty0 + j / kFineTW, lh1 - 1), x = min(tx0 + j % kFineTW, lw1 - 1);
       const long long o = fo + (long long)y * lw1 + x;
-      if (s == 0)
-        cp_async<16>(rs + j, a.R1 + o);
-      else
-        cp_async<int(sizeof(Store))>(gs + (s - 1) * kFineTA + j, g1_of<NMAX, Store>(a, s - 1, 0) + o);
+      cp_async<16>(rs + j, a.R1 + o);
+#pragma unroll
+      for (int k = 0; k < NMAX; ++k)
+        if (k < n) cp_async<int(sizeof(Store))>(gs + k * kFineTA + j, static_cast<const Store*>(a.G[k][1]) + o);
     }
     asm volatile("cp.async.commit_group;\n" ::: "memory");
   }
@@ -860,8 +959,8 @@ void fine_dispatch(const PyrArgs& a, int rule, dim3 grid, cudaStream_t stream) {
 }  // namespace
 
 size_t pyr_down_smem(int n, int tile) {
-  const int t1 = tile / 2, t2 = tile / 4;
-  return size_t(n) * size_t(t1 * t1 + t2 * t2) * sizeof(float4);
+  const int t2 = tile / 4;
+  return size_t(n) * (size_t(tile) * tile * sizeof(uint32_t) + size_t(t2 * t2) * sizeof(float4));
 }
 
 size_t pyr_coarse_smem(int n, int k, int tile1, int levels) {

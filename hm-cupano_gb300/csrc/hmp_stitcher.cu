@@ -11,6 +11,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <climits>
 #include <cstdio>
 #include <cstring>
 #include <new>
@@ -300,7 +301,7 @@ struct hmp_stitcher {
     for (int i = 0; i < n_inputs; ++i) {
       const hmp_image& im = inputs[i];
       if (!im.data) return make_status(HMP_ERR_INVALID_DEVICE_POINTER, "input image is null");
-      if (im.width <= 0 || im.height <= 0 || im.pitch < size_t(im.width) * 4)
+      if (im.width <= 0 || im.height <= 0 || im.pitch < size_t(im.width) * 4 || im.pitch > size_t(INT_MAX))
         return make_status(HMP_ERR_INVALID_VALUE, "input image has an invalid size or pitch");
       if (im.width >= 65535 || im.height >= 65535)
         return make_status(HMP_ERR_INVALID_VALUE, "input images must be smaller than 65535 pixels per side");
