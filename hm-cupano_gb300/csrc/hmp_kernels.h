@@ -55,6 +55,7 @@ cudaError_t launch_pyr_coarse(const PyrArgs& a, int rule, int storage, dim3 grid
 cudaError_t launch_pyr_fine(const PyrArgs& a, int rule, int storage, dim3 grid, cudaStream_t stream);
 
 size_t pyr_down_smem(int n, int tile);
-size_t pyr_coarse_smem(int n, int k, int tile1, int levels);
+// Shared memory of a pyr_coarse CTA (levels 2..L-1 of its tile with halos).
+size_t pyr_coarse_smem(int n, int k, int tile1, int levels, int storage);
 
 }  // namespace hmp

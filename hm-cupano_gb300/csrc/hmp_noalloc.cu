@@ -219,7 +219,7 @@ extern "C" HMP_API hmp_status hmp_blend2_noalloc(const hmp_image* image1, const 
     // Same tiles as a two-image stitcher of this depth.
     const int align = 1 << (L - 1);
     const int tile_down = std::max(64, align), tile_coarse = std::max(32, align / 2);
-    const size_t coarse_smem = hmp::pyr_coarse_smem(2, 1, tile_coarse, L);
+    const size_t coarse_smem = hmp::pyr_coarse_smem(2, 1, tile_coarse, L, HMP_STORAGE_F32);
     if (hmp::pyr_down_smem(2, tile_down) > 227 * 1024 || coarse_smem > 227 * 1024)
       return status_of(HMP_ERR_NOT_SUPPORTED, "pyramid tile does not fit in shared memory");
     a.tile = tile_down;

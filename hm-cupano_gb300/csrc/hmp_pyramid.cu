@@ -388,10 +388,11 @@ __global__ void __launch_bounds__(256) pyr_down_kernel(const __grid_constant__ P
 // only turn a -0 sum into +0, and the uint8 pack maps both to 0). Every other product v*w is
 // exact. The weight sum is 1, 0.5, 0.25 or 0.75; dividing by the first three is an exact scaling
 // by 1, 2 or 4, so only a 0.75 sum (three of four taps valid) needs a division.
-__device__ __forceinline__ float3 up_alpha(const float4* buf, int cw, int ax, int ay, int lw, int lh, int x, int y) {
+template <typename T>
+__device__ __forceinline__ float3 up_alpha(const T* buf, int cw, int ax, int ay, int lw, int lh, int x, int y) {
   const int gxi = x >> 1, gyi = y >> 1;
-  const float4* r0 = buf + (gyi - ay) * cw - ax;
-  const float4 p00 = r0[gxi];
+  const T* r0 = buf + (gyi - ay) * cw - ax;
+  const float4 p00 = load_level(r0 + gxi);
   const bool ox = (x & 1) != 0, oy = (y & 1) != 0;
   if (!ox && !oy) {
     if (p00.w != 0.f) return make_float3(p00.x, p00.y, p00.z);
@@ -399,7 +400,7 @@ __device__ __forceinline__ float3 up_alpha(const float4* buf, int cw, int ax, in
   }
   if (ox != oy) {
     // Two taps of weight 0.5: (00, 10) for odd x, (00, 01) for odd y.
-    const float4 p1 = ox ? r0[min(gxi + 1, lw - 1)] : buf[(min(gyi + 1, lh - 1) - ay) * cw + (gxi - ax)];
+    const float4 p1 = ox ? load_level(r0 + min(gxi + 1, lw - 1)) : load_level(buf + (min(gyi + 1, lh - 1) - ay) * cw + (gxi - ax));
     const bool v0 = p00.w != 0.f, v1 = p1.w != 0.f;
     if (v0 && v1)  // (p00*0.5 + p1*0.5) / 1
       return make_float3(p00.x * 0.5f + p1.x * 0.5f, p00.y * 0.5f + p1.y * 0.5f, p00.z * 0.5f + p1.z * 0.5f);
@@ -410,8 +411,8 @@ __device__ __forceinline__ float3 up_alpha(const float4* buf, int cw, int ax, in
   }
   // Four taps of weight 0.25.
   const int gxi1 = min(gxi + 1, lw - 1), gyi1 = min(gyi + 1, lh - 1);
-  const float4* r1 = buf + (gyi1 - ay) * cw - ax;
-  const float4 q[4] = {p00, r0[gxi1], r1[gxi], r1[gxi1]};
+  const T* r1 = buf + (gyi1 - ay) * cw - ax;
+  const float4 q[4] = {p00, load_level(r0 + gxi1), load_level(r1 + gxi), load_level(r1 + gxi1)};
   float sw = 0.f, s0 = 0.f, s1 = 0.f, s2 = 0.f;
 #pragma unroll
   for (int i = 0; i < 4; ++i) {
@@ -560,23 +561,47 @@ __device__ __forceinline__ float4 ldg_level(const half4* p) {
 }
 
 // pyr_coarse: R^1 (the reconstruction at level 1) for one T1 x T1 tile of level-1 pixels.
-// Levels 2..L-1 of the tile plus the upsample halo are loaded into shared memory up front (one
-// wait on memory), blended and reconstructed from the coarsest level down; level 1 reads G^1 and
-// the level-1 mask straight from HBM and writes R^1 to HBM for pyr_fine. Pixels are processed
+// Shared memory holds, per level l >= 2, the tile's footprint plus the upsample halo (G of every
+// slot, the mask values, R once computed), all copied in with cp.async up front (one wait on
+// memory). The CTA then blends and reconstructs from the coarsest level down; level 1 reads G^1
+// and the level-1 mask from HBM and writes R^1 to HBM for pyr_fine. Pixels are processed
 // parity-class-major so that the upsample branches stay uniform across a warp.
+struct CoarseLayout {
+  int g[kL], r[kL], m[kL];  // byte offsets of G (n x cap, storage type), R (cap float4), mask (cap x K)
+  int total;
+};
+
+__host__ __device__ constexpr int align16(int v) { return (v + 15) & ~15; }
+
+__host__ __device__ inline CoarseLayout coarse_layout(int n, int K, int T1, int L, int store_bytes) {
+  CoarseLayout o{};
+  int t = 0;
+  for (int l = 1; l < kL; ++l) {
+    const int cap = (l > 1 && l < L) ? up_cap(T1, l - 1) : 0;
+    o.g[l] = t;
+    t += align16(n * cap * store_bytes);
+    o.r[l] = t;
+    t += l > 1 ? cap * 16 : 0;
+    o.m[l] = t;
+    t += align16(cap * K * 4);
+  }
+  o.total = t;
+  return o;
+}
+
 template <int RULE, int NMAX, typename Store, int T1>
 __global__ void __launch_bounds__(256) pyr_coarse_kernel(const __grid_constant__ PyrArgs a) {
   extern __shared__ float4 sm[];
+  char* smb = reinterpret_cast<char*>(sm);
   const int n = RULE == kRuleNway ? a.n : NMAX;
   const int K = RULE == kRuleTwo ? 1 : (RULE == kRuleThree ? 3 : a.K);
   const int b = blockIdx.z;
   const int X1 = (a.tx0 + blockIdx.x) * T1, Y1 = (a.ty0 + blockIdx.y) * T1;
   const int L = a.levels, c = L - 1;
   const int tid = threadIdx.x;
-  // Regions: level 1 is the tile itself; level l >= 2 adds the halo read by level l-1's
-  // upsample. Shared memory holds levels 2..c (G of every slot, R, mask values).
-  int rax[kL], ray[kL], rbx[kL], rby[kL], gofs[kL], rofs[kL], mofs[kL];
-  int f4_total = 0, mtotal = 0;
+  const CoarseLayout lo = coarse_layout(n, K, T1, L, int(sizeof(Store)));
+  // Regions: level 1 is the tile itself; level l >= 2 adds the halo read by level l-1's upsample.
+  int rax[kL], ray[kL], rbx[kL], rby[kL];
   {
     int ax = X1, ay = Y1, bx = min(X1 + T1, a.lw[1]), by = min(Y1 + T1, a.lh[1]);
 #pragma unroll
@@ -591,15 +616,8 @@ __global__ void __launch_bounds__(256) pyr_coarse_kernel(const __grid_constant__
       ray[l] = ay;
       rbx[l] = bx;
       rby[l] = by;
-      const int cap = (l > 1 && l < L) ? up_cap(T1, l - 1) : 0;
-      gofs[l] = f4_total;
-      rofs[l] = f4_total + n * cap;
-      f4_total = rofs[l] + cap;
-      mofs[l] = mtotal;
-      mtotal += cap * K;
     }
   }
-  float* mbuf = reinterpret_cast<float*>(sm + f4_total);
 #pragma unroll
   for (int l = 2; l < kL; ++l) {
     if (l >= L) break;
@@ -610,20 +628,23 @@ __global__ void __launch_bounds__(256) pyr_coarse_kernel(const __grid_constant__
     for (int k = 0; k < NMAX; ++k) {
       if (k >= n) break;
       const Store* Gl = static_cast<const Store*>(a.G[k][l]) + (long long)b * lw * lh;
-      float4* gl = sm + gofs[l] + k * CAP;
+      Store* gl = reinterpret_cast<Store*>(smb + lo.g[l]) + k * CAP;
       for (int i = tid; i < CAP; i += 256) {
         const int x = i % CW, y = i / CW;
-        if (x < rw && y < rh) gl[i] = ldg_level(Gl + (long long)(lay + y) * lw + (lax + x));
+        if (x < rw && y < rh) cp_async<int(sizeof(Store))>(gl + i, Gl + (long long)(lay + y) * lw + (lax + x));
       }
     }
     const float* ml = a.maskL[l];
-    float* mb = mbuf + mofs[l];
-    for (int i = tid; i < CAP * K; i += 256) {
-      const int p = i / K, q = i - p * K;
+    float* mb = reinterpret_cast<float*>(smb + lo.m[l]);
+    for (int p = tid; p < CAP; p += 256) {
       const int x = p % CW, y = p / CW;
-      if (x < rw && y < rh) mb[i] = __ldg(ml + ((long long)(lay + y) * lw + (lax + x)) * K + q);
+      if (x < rw && y < rh) {
+        const float* src = ml + ((long long)(lay + y) * lw + (lax + x)) * K;
+        for (int q = 0; q < K; ++q) cp_async<4>(mb + p * K + q, src + q);
+      }
     }
   }
+  cp_async_commit_wait_all();
   __syncthreads();
 #pragma unroll
   for (int l = kL - 1; l >= 2; --l) {
@@ -631,16 +652,16 @@ __global__ void __launch_bounds__(256) pyr_coarse_kernel(const __grid_constant__
     const int CW = up_cw(T1, l - 1), CAP = CW * CW;
     const int QW = (CW + 1) / 2, QC = QW * QW;
     const int lax = rax[l], lay = ray[l], rw = rbx[l] - lax, rh = rby[l] - lay;
-    const float4* gcur = sm + gofs[l];
-    float4* rcur = sm + rofs[l];
-    const float* mb = mbuf + mofs[l];
+    const Store* gcur = reinterpret_cast<const Store*>(smb + lo.g[l]);
+    float4* rcur = reinterpret_cast<float4*>(smb + lo.r[l]);
+    const float* mb = reinterpret_cast<const float*>(smb + lo.m[l]);
     const bool has_next = l < c;
     const int nl = l + 1 < kL ? l + 1 : l;
     const int CWN = up_cw(T1, nl - 1), CAPN = CWN * CWN;
     const int nax = rax[nl], nay = ray[nl];
     const int lwn = a.lw[nl], lhn = a.lh[nl];
-    const float4* gnext = sm + gofs[nl];
-    const float4* rnext = sm + rofs[nl];
+    const Store* gnext = reinterpret_cast<const Store*>(smb + lo.g[nl]);
+    const float4* rnext = reinterpret_cast<const float4*>(smb + lo.r[nl]);
     for (int t = tid; t < 4 * QC; t += 256) {
       const int cls = t / QC, j = t - cls * QC;
       const int x = 2 * (j % QW) + (cls & 1), y = 2 * (j / QW) + (cls >> 1);
@@ -649,11 +670,11 @@ __global__ void __launch_bounds__(256) pyr_coarse_kernel(const __grid_constant__
       const int px = lax + x, py = lay + y;
       float al[NMAX];
 #pragma unroll
-      for (int k = 0; k < NMAX; ++k) al[k] = k < n ? gcur[k * CAP + i].w : 0.f;
+      for (int k = 0; k < NMAX; ++k) al[k] = k < n ? load_level(gcur + k * CAP + i).w : 0.f;
       const int pk = blend_pick<RULE, NMAX>(n, al, mb + i * K);
       float4 r = make_float4(0.f, 0.f, 0.f, 0.f);
       if (pk >= 0) {
-        float4 g = gcur[pk * CAP + i];
+        float4 g = load_level(gcur + pk * CAP + i);
         if (has_next) {
           const float3 up = up_alpha(gnext + pk * CAPN, CWN, nax, nay, lwn, lhn, px, py);
           g.x = g.x - up.x;
@@ -666,7 +687,7 @@ __global__ void __launch_bounds__(256) pyr_coarse_kernel(const __grid_constant__
 #pragma unroll
         for (int k = 0; k < NMAX; ++k) {
           if (k < n) {
-            float4 g = gcur[k * CAP + i];
+            float4 g = load_level(gcur + k * CAP + i);
             if (has_next) {
               const float3 up = up_alpha(gnext + k * CAPN, CWN, nax, nay, lwn, lhn, px, py);
               g.x = g.x - up.x;
@@ -690,29 +711,30 @@ __global__ void __launch_bounds__(256) pyr_coarse_kernel(const __grid_constant__
     }
     __syncthreads();
   }
-  // Level 1: the tile's own pixels, G^1 and mask^1 from HBM, R^1 to HBM.
-  constexpr int HALF = T1 / 2, CLS = HALF * HALF, PER = T1 * T1 / 256;
-  static_assert(CLS % 32 == 0 && PER >= 1, "tile");
+  // Level 1: the tile's own pixels, R^1 to HBM.
+  constexpr int HALF = T1 / 2, CLS = HALF * HALF, PER = (T1 * T1 + 255) / 256;
+  static_assert(CLS % 32 == 0, "tile");
   const int lw1 = a.lw[1], lh1 = a.lh[1];
   const bool has2 = c >= 2;
   const int CW2 = up_cw(T1, 1), CAP2 = CW2 * CW2;
   const int nax = rax[2], nay = ray[2];
   const int lw2 = a.lw[2 < kL ? 2 : 1], lh2 = a.lh[2 < kL ? 2 : 1];
-  const float4* g2 = sm + gofs[2];
-  const float4* r2 = sm + rofs[2];
+  const Store* g2 = reinterpret_cast<const Store*>(smb + lo.g[2]);
+  const float4* r2 = reinterpret_cast<const float4*>(smb + lo.r[2]);
   float4* R1 = a.R1 + (long long)b * lw1 * lh1;
 #pragma unroll 2
   for (int p = 0; p < PER; ++p) {
     const int i = p * 256 + tid;
-    const int px = X1 + 2 * ((i % CLS) % HALF) + ((i / CLS) & 1);
-    const int py = Y1 + 2 * ((i % CLS) / HALF) + ((i / CLS) >> 1);
+    const int lx = 2 * ((i % CLS) % HALF) + ((i / CLS) & 1), ly = 2 * ((i % CLS) / HALF) + ((i / CLS) >> 1);
+    const int px = X1 + lx, py = Y1 + ly;
     if (px >= lw1 || py >= lh1) continue;
     const long long o1 = (long long)py * lw1 + px;
     float m[NMAX];
-#pragma unroll
-    for (int q = 0; q < NMAX; ++q) m[q] = q < K ? __ldg(a.maskL[1] + o1 * K + q) : 0.f;
     float4 g1[NMAX];
     float al[NMAX];
+#pragma unroll
+    for (int q = 0; q < NMAX; ++q)
+      m[q] = q < K ? __ldg(a.maskL[1] + o1 * K + q) : 0.f;
 #pragma unroll
     for (int k = 0; k < NMAX; ++k) {
       g1[k] = k < n ? ldg_level(static_cast<const Store*>(a.G[k][1]) + (long long)b * lw1 * lh1 + o1)
@@ -916,10 +938,14 @@ void set_up_attr() {
 }
 
 template <typename Store, int T>
-void set_attrs() {
+void set_down_attrs() {
   set_down_attr<2, Store, T>();
   set_down_attr<3, Store, T>();
   set_down_attr<8, Store, T>();
+}
+
+template <typename Store, int T>
+void set_coarse_attrs() {
   set_up_attr<kRuleTwo, 2, Store, T>();
   set_up_attr<kRuleThree, 3, Store, T>();
   set_up_attr<kRuleNway, 8, Store, T>();
@@ -963,18 +989,18 @@ size_t pyr_down_smem(int n, int tile) {
   return size_t(n) * (size_t(tile) * tile * sizeof(uint32_t) + size_t(t2 * t2) * sizeof(float4));
 }
 
-size_t pyr_coarse_smem(int n, int k, int tile1, int levels) {
-  size_t bytes = 0;
-  for (int l = 2; l < levels; ++l)
-    bytes += size_t(up_cap(tile1, l - 1)) * ((n + 1) * sizeof(float4) + k * sizeof(float));
-  return bytes;
+size_t pyr_coarse_smem(int n, int k, int tile1, int levels, int storage) {
+  const int sb = storage == 1 ? int(sizeof(half4)) : int(sizeof(float4));
+  return size_t(coarse_layout(n, k, tile1, levels, sb).total);
 }
 
 cudaError_t kernels_init() {
-  set_attrs<float4, 32>();
-  set_attrs<half4, 32>();
-  set_attrs<float4, 64>();
-  set_attrs<half4, 64>();
+  set_down_attrs<float4, 32>();
+  set_down_attrs<half4, 32>();
+  set_down_attrs<float4, 64>();
+  set_down_attrs<half4, 64>();
+  set_coarse_attrs<float4, 32>();
+  set_coarse_attrs<half4, 32>();
   return cudaGetLastError();
 }
 
@@ -1002,11 +1028,6 @@ cudaError_t launch_pyr_coarse(const PyrArgs& a, int rule, int storage, dim3 grid
       coarse_dispatch<half4, 32>(a, rule, grid, smem, stream);
     else
       coarse_dispatch<float4, 32>(a, rule, grid, smem, stream);
-  } else if (a.tile == 64) {
-    if (storage == 1)
-      coarse_dispatch<half4, 64>(a, rule, grid, smem, stream);
-    else
-      coarse_dispatch<float4, 64>(a, rule, grid, smem, stream);
   } else {
     return cudaErrorInvalidValue;
   }

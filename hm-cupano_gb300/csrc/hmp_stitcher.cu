@@ -171,10 +171,10 @@ struct hmp_stitcher {
       const int align = 1 << (L - 1);
       // Down tiles: 64 level-0 pixels amortise the per-CTA level walk; with more than three images
       // the per-tile shared memory calls for 32. Coarse tiles: 32 level-1 pixels (a multiple of
-      // 2^(L-2) for every supported L).
+      // 2^(L-2) for every supported L); smaller ones multiply the per-CTA halo and walk.
       tile_down = std::max(n <= 3 ? 64 : 32, align);
       tile_coarse = std::max(32, align / 2);
-      coarse_smem = hmp::pyr_coarse_smem(n, p.mask_k, tile_coarse, L);
+      coarse_smem = hmp::pyr_coarse_smem(n, p.mask_k, tile_coarse, L, p.storage);
       if (L > 1) {
         void* r = nullptr;
         e = alloc(&r, size_t(B) * p.lw[1] * p.lh[1] * sizeof(float4));
