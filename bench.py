@@ -8,13 +8,16 @@ on one frame. Inputs are larger than L2: three frame/canvas sets rotate between 
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
-Prints one JSON line. ``value`` is canvas Mpix/s over all ranks with inputs resident in HBM;
-``e2e`` is the same metric through the public API with pinned host frames copied in and the
-canvas copied out every step; ``roofline`` is the dominant kernel's algorithmic bytes per launch
-over its CUDA-event duration against the measured HBM copy bandwidth; ``cpu_baseline`` is the
-oracle (a C port of the reference's algorithm) on the host cores. ``--impl reference`` times
-that CPU implementation as the reference arm. Multi-GPU runs are independent replicas (weak
-scaling, no collective on the data path).
+Prints one JSON line. ``value`` is canvas Mpix/s over all ranks with inputs resident in HBM (the
+pyramid kernels run concurrently with the canvas gather, as in production); ``e2e`` is the same
+metric through the public API with pinned host frames copied in and the canvas copied out every
+step; ``roofline`` is the dominant kernel's algorithmic bytes per launch over its CUDA-event
+duration, taken in a pass where the stitcher runs its kernels one after another (so the time is
+the kernel's own), against the measured HBM copy bandwidth; ``hbm_frac_frame`` is the frame's
+compulsory bytes over the concurrent frame time. ``cpu_baseline`` is the oracle (a C port of the
+reference's algorithm) on the host cores. ``--impl reference`` times that CPU implementation as
+the reference arm. ``vs_baseline`` is fps over the reference's published 340 fps (RTX 4090, same
+metric). Multi-GPU runs are independent replicas (weak scaling, no collective on the data path).
 """
 from __future__ import annotations
 
@@ -36,6 +39,7 @@ sys.path.insert(0, str(REPO / "hm-cupano_gb300"))
 METRIC = "canvas Mpix/s & fps at 8500x3300 L=6; % HBM peak; p50/p99 serve latency"
 WORKLOAD = "pano2_5120x2880_to_8500x3300"
 N_SETS = 3
+PUBLISHED_FPS = 340.0  # reference README: 2 images -> ~8500x3300, 6 levels, RTX 4090
 
 
 def _peaks() -> tuple[float, str]:
@@ -59,31 +63,46 @@ class ClockSampler:
     def __init__(self, gpu_index: int):
         self.gpu = gpu_index
         self.samples: list[list[str]] = []
-        self._stop = threading.Event()
+        self.stamped: list[tuple[float, list[str]]] = []
+        self.window = (0.0, float("inf"))
+        self._proc = None
         self._thr = None
 
-    def _run(self):
-        while not self._stop.is_set():
-            try:
-                out = subprocess.run(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}",
-                                      "--format=csv,noheader,nounits"], capture_output=True, text=True, timeout=5)
-                for line in out.stdout.strip().splitlines():
-                    self.samples.append([v.strip() for v in line.split(",")])
-            except Exception:
-                pass
-            self._stop.wait(0.2)
+    def _read(self):
+        for line in self._proc.stdout:
+            parts = [v.strip() for v in line.split(",")]
+            if len(parts) >= 9:
+                self.stamped.append((time.perf_counter(), parts))
 
     def __enter__(self):
-        self._thr = threading.Thread(target=self._run, daemon=True)
-        self._thr.start()
+        try:
+            # Loop mode samples every 100 ms from one process (no per-sample start-up delay).
+            self._proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}",
+                                           "--format=csv,noheader,nounits", "-lms", "100"],
+                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self._thr = threading.Thread(target=self._read, daemon=True)
+            self._thr.start()
+            time.sleep(0.15)  # first sample lands inside the timed region
+        except Exception:
+            self._proc = None
         return self
 
     def __exit__(self, *exc):
-        self._stop.set()
+        if self._proc:
+            self._proc.terminate()
+            try:
+                self._proc.wait(timeout=5)
+            except Exception:
+                self._proc.kill()
         if self._thr:
-            self._thr.join(timeout=6)
+            self._thr.join(timeout=5)
+
+    def mark(self, start: float, end: float) -> None:
+        """Keep only the samples taken between start and end (host perf_counter)."""
+        self.window = (start, end)
 
     def summary(self) -> dict:
+        self.samples = [p for t, p in self.stamped if self.window[0] <= t <= self.window[1]]
         sm = [float(s[1]) for s in self.samples if len(s) >= 9 and s[1].replace(".", "").isdigit()]
         mx = [float(s[2]) for s in self.samples if len(s) >= 9 and s[2].replace(".", "").isdigit()]
         reasons = set()
@@ -105,15 +124,18 @@ def _masks(rig):
     return hmpano.ControlMasks(rig.map_x[0], rig.map_y[0], rig.map_x[1], rig.map_y[1], rig.seam, pos)
 
 
-def cpu_baseline(rig, frames, levels: int, frames_sample: int = 2) -> dict:
-    """The oracle (C port of the reference algorithm) on all host cores, bounded sample."""
+def cpu_baseline(rig, frames, levels: int, seconds: float = 10.0) -> dict:
+    """The oracle (C port of the reference algorithm) on all host cores, on a bounded sample:
+    as many full frames as fit in about `seconds` of CPU time."""
     from oracle import oracle
 
     oracle.build()
     threads = os.cpu_count() or 1
     oracle.set_threads(threads)
     st = oracle.Stitch.from_rig(rig, levels)
-    st.run(frames)  # warm-up
+    t0 = time.perf_counter()
+    st.run(frames)  # warm-up, also sizes the sample
+    frames_sample = max(2, int(seconds / max(time.perf_counter() - t0, 1e-3)))
     t0 = time.perf_counter()
     for _ in range(frames_sample):
         st.run(frames)
@@ -163,7 +185,7 @@ def reference_arm(args) -> None:
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--steps", type=int, default=5000)
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--levels", type=int, default=6)
@@ -235,13 +257,12 @@ def main() -> None:
     sampler = ClockSampler(local) if rank == 0 else None
     if sampler:
         sampler.__enter__()
+    t_region0 = time.perf_counter()
     e0.record(stream)
     for i in range(args.steps):
         step(i)
     e1.record(stream)
     torch.cuda.synchronize()
-    if sampler:
-        sampler.__exit__(None, None, None)
     if dist:
         dist.barrier()
     ms = e0.elapsed_time(e1) / args.steps
@@ -255,14 +276,30 @@ def main() -> None:
     mpix = W * H / 1e6
     value = frames_total * mpix / (ms * args.steps / 1e3)
 
-    # Untimed, timing-off pass of the same length: event records do not distort the number.
+    # The same pass without per-kernel event records (they cost a little): reported beside.
     torch.cuda.synchronize()
     e0.record(stream)
     for i in range(args.steps):
         step(i)
     e1.record(stream)
     torch.cuda.synchronize()
+    t_region1 = time.perf_counter()
+    if sampler:
+        sampler.__exit__(None, None, None)
+        sampler.mark(t_region0, t_region1)
     ms_plain = e0.elapsed_time(e1) / args.steps
+
+    # Kernel attribution: a pass with the kernels serialised on one stream, so that each
+    # kernel's event-timed duration is its own (feeds the roofline of the dominant kernel).
+    k_serial = max(20, min(args.steps, 1000))
+    pano.set_timing(True, serialize=True)
+    with torch.cuda.stream(stream):
+        for i in range(k_serial):
+            step(i)
+    torch.cuda.synchronize()
+    ktimes_serial = pano.kernel_times()
+    pano.set_timing(False)
+    torch.cuda.synchronize()
 
     # End to end through the public API: every step copies its frames in from pinned host memory
     # and its canvas out to pinned host memory. Three buffer sets and three streams (copy-in,
@@ -316,8 +353,8 @@ def main() -> None:
 
     peak, peak_kind = _peaks()
     names = ["canvas_gather", "pyr_down", "pyr_coarse", "pyr_fine"]
-    dom = max(names, key=lambda k: ktimes[k][0])
-    tot, cnt = ktimes[dom]
+    dom = max(names, key=lambda k: ktimes_serial[k][0])
+    tot, cnt = ktimes_serial[dom]
     per_launch_ms = tot / max(cnt, 1)
     wr = info["write_rect"]
     canvas_px = W * H
@@ -341,7 +378,7 @@ def main() -> None:
         "ms_per_step": round(ms, 5),
         "higher_is_better": True,
         "scaling": "weak",
-        "vs_baseline": None,
+        "vs_baseline": round(world * 1e3 / ms / PUBLISHED_FPS, 3) if args.storage == "f32" else None,
         "dtype": "f32" if args.storage == "f32" else "f16-storage/f32-arith",
         "data": "synthetic",
         "fps": round(world * 1e3 / ms, 1),
@@ -356,8 +393,10 @@ def main() -> None:
                      "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4) if achieved else None,
                      "traffic": traffic, "peak_kind": peak_kind,
                      "bytes_per_launch": int(dom_bytes) if dom_bytes else None,
-                     "ms_per_launch": round(per_launch_ms, 5)},
+                     "ms_per_launch": round(per_launch_ms, 5),
+                     "timing": f"CUDA events, {k_serial} steps with the kernels serialised on one stream"},
         "kernel_ms": {k: round(v[0] / max(v[1], 1), 5) for k, v in ktimes.items()},
+        "kernel_ms_serialized": {k: round(v[0] / max(v[1], 1), 5) for k, v in ktimes_serial.items()},
         "gpu_launches": int(sum(v[1] for v in ktimes.values())),
         "e2e": e2e,
         "clocks": sampler.summary() if sampler else None,

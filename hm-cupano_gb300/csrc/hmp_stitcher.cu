@@ -64,6 +64,7 @@ struct hmp_stitcher {
   static constexpr int kTimingSlots = 4096;
   static constexpr int kTimed = 4;
   bool timing = false;
+  bool serialize = false;  // timing mode 2: every kernel on the caller stream, one after another
   std::vector<cudaEvent_t> tev;  // [slot][kernel][begin/end], kernels: gather, down, coarse, fine
   std::vector<unsigned char> tused;
   int tnext = 0;
@@ -230,7 +231,9 @@ struct hmp_stitcher {
     m0_bytes = bytes;
   }
 
-  cudaError_t timing_enable(bool on) {
+  cudaError_t timing_enable(int mode) {
+    const bool on = mode != 0;
+    serialize = mode == 2;
     if (on && tev.empty()) {
       tev.resize(size_t(kTimingSlots) * kTimed * 2);
       for (auto& e : tev) {
@@ -344,7 +347,7 @@ struct hmp_stitcher {
     }
     // Fork: the pyramid goes to the high-priority stream `aux` when the canvas gather also
     // runs; the gather is launched on the caller stream after the pyramid kernels.
-    const bool fork = p.canvas_plane_used;
+    const bool fork = p.canvas_plane_used && !serialize;
     cudaStream_t ps = s;
     if (fork) {
       e = cudaEventRecord(ev_fork, s);
@@ -405,11 +408,13 @@ struct hmp_stitcher {
       tend(3, ps);
       if (e != cudaSuccess) return cuda_status(e, "pyr_fine launch");
     }
-    if (fork) {
+    if (p.canvas_plane_used) {
       tbegin(0, s);
       e = hmp::launch_canvas_gather(ga, s);
       tend(0, s);
       if (e != cudaSuccess) return cuda_status(e, "canvas_gather launch");
+    }
+    if (fork) {
       e = cudaEventRecord(ev_join, aux);
       if (e == cudaSuccess) e = cudaStreamWaitEvent(s, ev_join, 0);
       if (e != cudaSuccess) return cuda_status(e, "stream join");
@@ -498,7 +503,7 @@ HMP_API hmp_status hmp_stitcher_process(hmp_stitcher* st, const hmp_image* input
 
 HMP_API hmp_status hmp_stitcher_set_timing(hmp_stitcher* st, int enable) {
   if (!st) return make_status(HMP_ERR_INVALID_VALUE, "stitcher is null");
-  const cudaError_t e = st->timing_enable(enable != 0);
+  const cudaError_t e = st->timing_enable(enable);
   if (e != cudaSuccess) return cuda_status(e, "timing events");
   return ok_status();
 }

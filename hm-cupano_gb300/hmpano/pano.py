@@ -240,9 +240,11 @@ class _Stitcher:
             "device_bytes": inf.device_bytes,
         }
 
-    def set_timing(self, enable: bool) -> None:
-        """Record per-kernel CUDA-event times of subsequent process() calls."""
-        s = _status(_lib.lib().hmp_stitcher_set_timing(self._handle, int(bool(enable))))
+    def set_timing(self, enable: bool, serialize: bool = False) -> None:
+        """Record per-kernel CUDA-event times of subsequent process() calls; ``serialize`` also runs
+        the kernels one after another on the caller stream, so each time is the kernel alone."""
+        mode = (2 if serialize else 1) if enable else 0
+        s = _status(_lib.lib().hmp_stitcher_set_timing(self._handle, mode))
         if not s.ok():
             raise CudaStatusError(s)
 

@@ -160,7 +160,9 @@ typedef struct hmp_kernel_timing {
 } hmp_kernel_timing;
 
 /* Enable (1) or disable (0) per-kernel event timing; enabling clears the accumulated times.
- * At most 4096 process() calls are recorded between two hmp_stitcher_get_timing() calls. */
+ * Mode 2 also serialises the kernels on the caller stream (no concurrent pyramid stream), so that
+ * each kernel's time is its time alone. At most 4096 process() calls are recorded between two
+ * hmp_stitcher_get_timing() calls. */
 HMP_API hmp_status hmp_stitcher_set_timing(hmp_stitcher* st, int enable);
 
 /* Accumulated kernel times since timing was enabled or last read; waits for the recorded
