@@ -31,8 +31,9 @@ UNITS = {
     "hmp_pyramid.cu": ["-fmad=false"],
     "hmp_stitcher.cu": [],
     "hmp_noalloc.cu": ["-fmad=false"],
+    "hmp_binomial.cu": ["-fmad=false"],
 }
-HEADERS = ["hmp_plan.h", "hmp_device.cuh", "hmp_kernels.h"]
+HEADERS = ["hmp_plan.h", "hmp_device.cuh", "hmp_kernels.h", "hmp_blend.cuh"]
 
 
 def nvcc() -> str:

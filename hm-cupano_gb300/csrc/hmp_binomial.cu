@@ -1,0 +1,321 @@
+// hmp_binomial.cu -- the Binomial5 pyramid: 5-tap [1,4,6,4,1]/16 separable filter with reflect-101
+// borders in place of the reference's 2x2 box / bilinear pair (no reference implementation; the
+// oracle's FP64 build is the judge, its FP32 build the bit-level twin).
+//
+//   down:  G^{l+1}(x, y) = sum over taps (2x+i, 2y+j), i, j in -2..2 with alpha != 0, of
+//          w_i w_j / 256 * G^l, divided by the sum of those weights (0 if none); alpha is the
+//          max over the in-bounds 2x2 block (2x..2x+1, 2y..2y+1), as in the box pyramid.
+//   up:    Burt-Adelson expand: per axis, even x reads x/2-1, x/2, x/2+1 with weights 1, 6, 1,
+//          odd x reads (x-1)/2, (x+1)/2 with weights 4, 4; weight w_x w_y / 64; alpha-aware
+//          (alpha-0 taps dropped, renormalised).
+//   blend, reconstruct, pack: as in the box pyramid (the reference's rules).
+//
+// The 5-tap filter has a halo, so the box pyramid's tile-local level walk does not apply; the
+// pyramid is built level by level through HBM (L2-resident at these sizes):
+//   b5_down0   level 0 (gathered through the slot planes) -> G^1, 16x16 output tiles, halo in smem
+//   b5_down    G^l -> G^{l+1}
+//   b5_top     R^{L-1} = blend(G^{L-1})
+//   b5_up      R^l = up(R^{l+1}) + blend(G^l - up(G^{l+1}))         (l = L-2 .. 1)
+//   b5_fine    level 0 of the write rect: blend(G^0 - up(G^1)) + up(R^1), packed into the canvas
+// Arithmetic order follows the oracle term by term (this file is compiled with -fmad=false).
+#include "hmp_blend.cuh"
+
+namespace hmp {
+namespace {
+
+constexpr int kB5Tile = 16;                    // output tile edge of the down kernels
+constexpr int kB5Src = 2 * kB5Tile + 3;        // source tile edge: 2x-2 .. 2x+2 of 16 outputs
+constexpr int kB5SrcArea = kB5Src * kB5Src;
+
+__device__ __forceinline__ int reflect101(int m, int n) {
+  if (n == 1) return 0;
+  // Coordinates here are at most 2 outside [0, n), so this settles in at most two steps.
+  for (int it = 0; it < 4 && (m < 0 || m >= n); ++it) {
+    if (m < 0) m = -m;
+    if (m >= n) m = 2 * n - 2 - m;
+  }
+  return m;
+}
+
+// Down-filter output (ox, oy) of a source tile `t` whose element (p, q) is source pixel
+// (reflect(2*X0 - 2 + p), reflect(2*Y0 - 2 + q)); (tx, ty) = output position in the tile.
+__device__ __forceinline__ float4 down5(const float4* t, int tx, int ty, int ox, int oy, int iw, int ih) {
+  const float k5[5] = {1.f, 4.f, 6.f, 4.f, 1.f};
+  float sw = 0.f, s0 = 0.f, s1 = 0.f, s2 = 0.f;
+#pragma unroll
+  for (int j = 0; j < 5; ++j)
+#pragma unroll
+    for (int i = 0; i < 5; ++i) {
+      const float4 p = t[(2 * ty + j) * kB5Src + 2 * tx + i];
+      if (p.w == 0.f) continue;
+      const float wgt = (k5[i] * k5[j]) / 256.f;
+      sw += wgt;
+      s0 += wgt * p.x;
+      s1 += wgt * p.y;
+      s2 += wgt * p.z;
+    }
+  float amax = 0.f;
+#pragma unroll
+  for (int dy = 0; dy < 2; ++dy)
+#pragma unroll
+    for (int dx = 0; dx < 2; ++dx) {
+      if (2 * ox + dx < iw && 2 * oy + dy < ih) {
+        const float a = t[(2 * ty + 2 + dy) * kB5Src + 2 * tx + 2 + dx].w;
+        if (a > amax) amax = a;
+      }
+    }
+  if (sw > 0.f) return make_float4(s0 / sw, s1 / sw, s2 / sw, amax);
+  return make_float4(0.f, 0.f, 0.f, amax);
+}
+
+// Burt-Adelson expand of a level buffer (lw x lh, frame base `low`) at high-res pixel (x, y).
+template <typename T>
+__device__ __forceinline__ float3 up5(const T* low, int lw, int lh, int x, int y) {
+  int tx[3], ty[3];
+  float wx[3], wy[3];
+  int nx, ny;
+  if ((x & 1) == 0) {
+    nx = 3;
+    tx[0] = reflect101(x / 2 - 1, lw), tx[1] = reflect101(x / 2, lw), tx[2] = reflect101(x / 2 + 1, lw);
+    wx[0] = 1.f, wx[1] = 6.f, wx[2] = 1.f;
+  } else {
+    nx = 2;
+    tx[0] = reflect101((x - 1) / 2, lw), tx[1] = reflect101((x + 1) / 2, lw), tx[2] = 0;
+    wx[0] = 4.f, wx[1] = 4.f, wx[2] = 0.f;
+  }
+  if ((y & 1) == 0) {
+    ny = 3;
+    ty[0] = reflect101(y / 2 - 1, lh), ty[1] = reflect101(y / 2, lh), ty[2] = reflect101(y / 2 + 1, lh);
+    wy[0] = 1.f, wy[1] = 6.f, wy[2] = 1.f;
+  } else {
+    ny = 2;
+    ty[0] = reflect101((y - 1) / 2, lh), ty[1] = reflect101((y + 1) / 2, lh), ty[2] = 0;
+    wy[0] = 4.f, wy[1] = 4.f, wy[2] = 0.f;
+  }
+  float sw = 0.f, s0 = 0.f, s1 = 0.f, s2 = 0.f;
+#pragma unroll
+  for (int j = 0; j < 3; ++j) {
+    if (j >= ny) break;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      if (i >= nx) break;
+      const float4 p = ldg_level(low + (long long)ty[j] * lw + tx[i]);
+      if (p.w == 0.f) continue;
+      const float wgt = (wx[i] * wy[j]) / 64.f;
+      sw += wgt;
+      s0 += wgt * p.x;
+      s1 += wgt * p.y;
+      s2 += wgt * p.z;
+    }
+  }
+  if (sw > 0.f) return make_float3(s0 / sw, s1 / sw, s2 / sw);
+  return make_float3(0.f, 0.f, 0.f);
+}
+
+template <int NMAX, typename Store>
+__device__ __forceinline__ const Store* g_of(const PyrArgs& a, int k, int l, int b) {
+  const void* p = a.G[0][l];
+#pragma unroll
+  for (int j = 1; j < NMAX; ++j)
+    if (j == k) p = a.G[j][l];
+  return static_cast<const Store*>(p) + (long long)b * a.lw[l] * a.lh[l];
+}
+
+// Level 0 -> G^1 for every slot: the source tile is gathered through the slot plane at
+// reflected level-0 coordinates.
+template <int NMAX, typename Store>
+__global__ void __launch_bounds__(256) b5_down0_kernel(const __grid_constant__ PyrArgs a) {
+  __shared__ float4 t[kB5SrcArea];
+  const int n = a.n, b = blockIdx.z, tid = threadIdx.x;
+  const int X0 = blockIdx.x * kB5Tile, Y0 = blockIdx.y * kB5Tile;
+  const int iw = a.lw[0], ih = a.lh[0], ow = a.lw[1], oh = a.lh[1];
+  const int tx = tid % kB5Tile, ty = tid / kB5Tile, ox = X0 + tx, oy = Y0 + ty;
+#pragma unroll
+  for (int k = 0; k < NMAX; ++k) {
+    if (k >= n) break;
+    for (int i = tid; i < kB5SrcArea; i += 256) {
+      const int sx = reflect101(2 * X0 - 2 + i % kB5Src, iw), sy = reflect101(2 * Y0 - 2 + i / kB5Src, ih);
+      int own;
+      uint32_t ent;
+      slot_lookup(a.slot[k], k, sx, sy, own, ent);
+      t[i] = to_f4(slot_fetch<NMAX>(a, k, own, ent, b, a.opaque != 0));
+    }
+    __syncthreads();
+    if (ox < ow && oy < oh) {
+      Store* G1 = static_cast<Store*>(a.G[k][1]) + (long long)b * ow * oh;
+      store_level(G1 + (long long)oy * ow + ox, down5(t, tx, ty, ox, oy, iw, ih));
+    }
+    __syncthreads();
+  }
+}
+
+// G^l -> G^{l+1} (l >= 1) for every slot.
+template <int NMAX, typename Store>
+__global__ void __launch_bounds__(256) b5_down_kernel(const __grid_constant__ PyrArgs a, int l) {
+  __shared__ float4 t[kB5SrcArea];
+  const int n = a.n, b = blockIdx.z, tid = threadIdx.x;
+  const int X0 = blockIdx.x * kB5Tile, Y0 = blockIdx.y * kB5Tile;
+  const int iw = a.lw[l], ih = a.lh[l], ow = a.lw[l + 1], oh = a.lh[l + 1];
+  const int tx = tid % kB5Tile, ty = tid / kB5Tile, ox = X0 + tx, oy = Y0 + ty;
+#pragma unroll
+  for (int k = 0; k < NMAX; ++k) {
+    if (k >= n) break;
+    const Store* src = static_cast<const Store*>(a.G[k][l]) + (long long)b * iw * ih;
+    for (int i = tid; i < kB5SrcArea; i += 256) {
+      const int sx = reflect101(2 * X0 - 2 + i % kB5Src, iw), sy = reflect101(2 * Y0 - 2 + i / kB5Src, ih);
+      t[i] = ldg_level(src + (long long)sy * iw + sx);
+    }
+    __syncthreads();
+    if (ox < ow && oy < oh) {
+      Store* dst = static_cast<Store*>(a.G[k][l + 1]) + (long long)b * ow * oh;
+      store_level(dst + (long long)oy * ow + ox, down5(t, tx, ty, ox, oy, iw, ih));
+    }
+    __syncthreads();
+  }
+}
+
+// R^l at (x, y), l >= 1: blend of the Laplacians G^l - up(G^{l+1}) (of the picked image where the
+// weights are one-hot; G^l itself at the coarsest level) plus up(R^{l+1}).
+template <int RULE, int NMAX, typename Store>
+__global__ void __launch_bounds__(256) b5_up_kernel(const __grid_constant__ PyrArgs a, int l) {
+  const int n = RULE == kRuleNway ? a.n : NMAX;
+  const int K = RULE == kRuleTwo ? 1 : (RULE == kRuleThree ? 3 : a.K);
+  const int b = blockIdx.z;
+  const int x = blockIdx.x * 32 + threadIdx.x, y = blockIdx.y * 8 + threadIdx.y;
+  const int lw = a.lw[l], lh = a.lh[l];
+  if (x >= lw || y >= lh) return;
+  const bool has_next = l + 1 < a.levels;
+  const int lwn = a.lw[has_next ? l + 1 : l], lhn = a.lh[has_next ? l + 1 : l];
+  const long long o = (long long)y * lw + x;
+  float4 g[NMAX];
+  float al[NMAX], m[NMAX];
+#pragma unroll
+  for (int k = 0; k < NMAX; ++k) {
+    g[k] = k < n ? ldg_level(g_of<NMAX, Store>(a, k, l, b) + o) : make_float4(0.f, 0.f, 0.f, 0.f);
+    al[k] = g[k].w;
+    m[k] = k < K ? __ldg(a.maskL[l] + o * K + k) : 0.f;
+  }
+  const int pk = blend_pick<RULE, NMAX>(n, al, m);
+  float4 r = make_float4(0.f, 0.f, 0.f, 0.f);
+  if (pk >= 0) {
+    float4 v = g[0];
+#pragma unroll
+    for (int k = 1; k < NMAX; ++k)
+      if (k == pk) v = g[k];
+    if (has_next) {
+      const float3 up = up5(g_of<NMAX, Store>(a, pk, l + 1, b), lwn, lhn, x, y);
+      v.x = v.x - up.x;
+      v.y = v.y - up.y;
+      v.z = v.z - up.z;
+    }
+    r = make_float4(v.x, v.y, v.z, blend_alpha<RULE, NMAX>(al, pk));
+  } else if (pk == kPickAll) {
+#pragma unroll
+    for (int k = 0; k < NMAX; ++k) {
+      if (k < n && has_next) {
+        const float3 up = up5(g_of<NMAX, Store>(a, k, l + 1, b), lwn, lhn, x, y);
+        g[k].x = g[k].x - up.x;
+        g[k].y = g[k].y - up.y;
+        g[k].z = g[k].z - up.z;
+      }
+    }
+    r = blend_level<RULE, NMAX>(n, g, m);
+  }
+  if (has_next) {
+    const float3 up = up5(a.Rl[l + 1] + (long long)b * lwn * lhn, lwn, lhn, x, y);
+    r.x = up.x + r.x;
+    r.y = up.y + r.y;
+    r.z = up.z + r.z;
+  }
+  a.Rl[l][(long long)b * lw * lh + o] = r;
+}
+
+// Level 0 of the write rect: Laplacians against up(G^1), blend with the level-0 seam value, add
+// up(R^1), truncating pack into the canvas.
+template <int RULE, int NMAX, typename Store>
+__global__ void __launch_bounds__(256) b5_fine_kernel(const __grid_constant__ PyrArgs a) {
+  const int n = RULE == kRuleNway ? a.n : NMAX;
+  const int b = blockIdx.z;
+  const int x = a.wx0 + blockIdx.x * 32 + threadIdx.x, y = a.wy0 + blockIdx.y * 8 + threadIdx.y;
+  if (x >= a.wx1 || y >= a.wy1) return;
+  const int lw1 = a.lw[1], lh1 = a.lh[1];
+  const int mv = int(__ldg(a.mask0 + (long long)y * a.mask0_pitch + x));
+  uchar4 src[NMAX];
+  float al[NMAX];
+#pragma unroll
+  for (int k = 0; k < NMAX; ++k) {
+    int own = 0xFF;
+    uint32_t ent = 0xFFFFFFFFu;
+    if (k < n) slot_lookup(a.slot[k], k, x, y, own, ent);
+    src[k] = slot_fetch<NMAX>(a, k, own, ent, b, a.opaque != 0);
+    al[k] = float(src[k].w);
+  }
+  const int pk = blend_pick0<RULE, NMAX>(n, al, mv);
+  float4 r = make_float4(0.f, 0.f, 0.f, 0.f);
+  if (pk >= 0) {
+    uchar4 s = src[0];
+#pragma unroll
+    for (int k = 1; k < NMAX; ++k)
+      if (k == pk) s = src[k];
+    float4 v = to_f4(s);
+    const float3 up = up5(g_of<NMAX, Store>(a, pk, 1, b), lw1, lh1, x, y);
+    r = make_float4(v.x - up.x, v.y - up.y, v.z - up.z, blend_alpha<RULE, NMAX>(al, pk));
+  } else if (pk == kPickAll) {
+    float4 lap[NMAX];
+#pragma unroll
+    for (int k = 0; k < NMAX; ++k) {
+      float4 v = to_f4(src[k]);
+      if (k < n) {
+        const float3 up = up5(g_of<NMAX, Store>(a, k, 1, b), lw1, lh1, x, y);
+        v.x = v.x - up.x;
+        v.y = v.y - up.y;
+        v.z = v.z - up.z;
+      }
+      lap[k] = v;
+    }
+    r = blend_level0<RULE, NMAX>(n, lap, mv);
+  }
+  const float3 up = up5(a.Rl[1] + (long long)b * lw1 * lh1, lw1, lh1, x, y);
+  r.x = up.x + r.x;
+  r.y = up.y + r.y;
+  r.z = up.z + r.z;
+  uchar4* crow =
+      reinterpret_cast<uchar4*>(reinterpret_cast<char*>(a.C.ptr) + b * a.C.bstride + (long long)(y + a.cy_off) * a.C.pitch);
+  crow[x + a.cx_off] = pack_rgba(r);
+}
+
+template <int RULE, int NMAX, typename Store>
+cudaError_t b5_chain(const PyrArgs& a, int batch, cudaStream_t s) {
+  const int L = a.levels;
+  for (int l = 0; l + 1 < L; ++l) {
+    const dim3 grid((a.lw[l + 1] + kB5Tile - 1) / kB5Tile, (a.lh[l + 1] + kB5Tile - 1) / kB5Tile, batch);
+    if (l == 0)
+      b5_down0_kernel<NMAX, Store><<<grid, 256, 0, s>>>(a);
+    else
+      b5_down_kernel<NMAX, Store><<<grid, 256, 0, s>>>(a, l);
+  }
+  const dim3 blk(32, 8);
+  for (int l = L - 1; l >= 1; --l)
+    b5_up_kernel<RULE, NMAX, Store><<<dim3((a.lw[l] + 31) / 32, (a.lh[l] + 7) / 8, batch), blk, 0, s>>>(a, l);
+  b5_fine_kernel<RULE, NMAX, Store>
+      <<<dim3((a.wx1 - a.wx0 + 31) / 32, (a.wy1 - a.wy0 + 7) / 8, batch), blk, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+template <typename Store>
+cudaError_t b5_dispatch(const PyrArgs& a, int rule, int batch, cudaStream_t s) {
+  if (rule == kRuleTwo) return b5_chain<kRuleTwo, 2, Store>(a, batch, s);
+  if (rule == kRuleThree) return b5_chain<kRuleThree, 3, Store>(a, batch, s);
+  return b5_chain<kRuleNway, 8, Store>(a, batch, s);
+}
+
+}  // namespace
+
+cudaError_t launch_b5_pyramid(const PyrArgs& a, int rule, int storage, int batch, cudaStream_t stream) {
+  if (a.levels < 2) return cudaErrorInvalidValue;
+  return storage == 1 ? b5_dispatch<half4>(a, rule, batch, stream) : b5_dispatch<float4>(a, rule, batch, stream);
+}
+
+int b5_launches(int levels) { return levels < 2 ? 0 : 2 * levels - 1; }
+
+}  // namespace hmp

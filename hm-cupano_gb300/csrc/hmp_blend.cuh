@@ -1,0 +1,250 @@
+// hmp_blend.cuh -- device helpers shared by the pyramid kernels (box and Binomial5 filters):
+// slot-plane lookups, the reference's blend rules, and the one-hot "pick" that lets the up-pass
+// compute a single Laplacian where the blend weights are one-hot.
+#pragma once
+
+#include "hmp_kernels.h"
+
+namespace hmp {
+
+constexpr int kRuleNway = 1, kRuleTwo = 2, kRuleThree = 3;
+
+// Table lookup of slot k at (x, y); the owner is k unless the slot has an owner plane.
+__device__ __forceinline__ void slot_lookup(const PlaneDev& P, int k, int x, int y, int& owner, uint32_t& entry) {
+  const int rx = x - P.x0, ry = y - P.y0;
+  owner = 0xFF;
+  entry = 0xFFFFFFFFu;
+  if ((unsigned)rx >= (unsigned)P.w || (unsigned)ry >= (unsigned)P.h) return;
+  owner = P.owner ? int(__ldg(P.owner + (long long)ry * P.owner_pitch + rx)) : k;
+  entry = __ldg(P.map + (long long)ry * P.map_pitch + rx);
+}
+
+// Source pixel of slot k for a looked-up (owner, entry). A slot without an owner plane only ever
+// reads image k (outside its plane the entry is the sentinel, which reads as zero), so it skips
+// the owner select.
+template <int NMAX>
+__device__ __forceinline__ uchar4 slot_fetch(const PyrArgs& a, int k, int own, uint32_t e, int b, bool opaque) {
+  if (a.slot[k].owner != nullptr) return fetch_sel<NMAX>(a.S, own, e, b, opaque);
+  const int sx = int(e & 0xFFFFu), sy = int(e >> 16);
+  uchar4 out = make_uchar4(0, 0, 0, 0);
+  if (sx < a.S.w[k] && sy < a.S.h[k]) {
+    const char* base = reinterpret_cast<const char*>(a.S.ptr[k]) + b * a.S.bstride[k];
+    out = __ldg(reinterpret_cast<const uchar4*>(base + (long long)sy * int(a.S.pitch[k])) + sx);
+  } else if (opaque && sx != 0xFFFF) {
+    out.w = 255;
+  }
+  return out;
+}
+
+// Blends whose weights are one-hot need a single Laplacian. With weight 1 on image s and 0 on
+// the others, every rule below returns Lap_s's colour up to the sign of a zero (1*x + 0*y = x
+// unless x is a zero) and an alpha known from the alphas alone; a zero's sign never changes a
+// later non-zero sum, product or alpha test, and the uint8 pack maps both zeros to 0. So the
+// up-pass computes the Laplacian of the picked image only:
+//   pick >= 0 : the result is Lap_pick's colour with the alpha of blend_alpha();
+//   kPickNone : the result is (0, 0, 0, 0);
+//   kPickAll  : fractional weights, the full blend of every Laplacian.
+constexpr int kPickNone = -1, kPickAll = -2;
+
+// First image of strictly largest non-zero alpha (the rules' fallback when no weighted image has
+// alpha), or kPickNone.
+template <int NMAX>
+__device__ __forceinline__ int pick_max_alpha(int n, const float* al) {
+  float amax = 0.f;
+  int idx = kPickNone;
+#pragma unroll
+  for (int k = 0; k < NMAX; ++k)
+    if (k < n && al[k] > amax) {
+      amax = al[k];
+      idx = k;
+    }
+  return idx;
+}
+
+// Level 0: the seam value v is the two-image weight of image 1, or the label (one-hot weights).
+template <int RULE, int NMAX>
+__device__ __forceinline__ int blend_pick0(int n, const float* al, int v) {
+  if (RULE == kRuleTwo) {
+    if (al[0] == 0.f) return 1;  // blend_two returns b
+    if (al[1] == 0.f) return 0;  // blend_two returns a
+    if (v == 1) return 0;
+    if (v == 0) return 1;
+    return kPickAll;
+  }
+  float alv = 0.f;
+#pragma unroll
+  for (int k = 0; k < NMAX; ++k)
+    if (k == v) alv = al[k];
+  if (v < n && alv != 0.f) return v;
+  return pick_max_alpha<NMAX>(n, al);
+}
+
+// Levels >= 1: mask values m[0..K).
+template <int RULE, int NMAX>
+__device__ __forceinline__ int blend_pick(int n, const float* al, const float* m) {
+  if (RULE == kRuleTwo) {
+    if (al[0] == 0.f) return 1;
+    if (al[1] == 0.f) return 0;
+    if (m[0] == 1.f) return 0;
+    if (m[0] == 0.f) return 1;
+    return kPickAll;
+  }
+  int hot = kPickNone;
+  bool onehot = true;
+#pragma unroll
+  for (int k = 0; k < NMAX; ++k) {
+    if (k >= n) break;
+    if (m[k] == 1.f) {
+      if (hot != kPickNone) onehot = false;
+      hot = k;
+    } else if (m[k] != 0.f) {
+      onehot = false;
+    }
+  }
+  if (!onehot) return kPickAll;
+  float alh = 0.f;
+#pragma unroll
+  for (int k = 0; k < NMAX; ++k)
+    if (k == hot) alh = al[k];
+  if (hot != kPickNone && alh != 0.f) return hot;
+  return pick_max_alpha<NMAX>(n, al);
+}
+
+// Alpha of a picked blend: the two-image rule keeps b's alpha unless b has none; the others
+// keep the picked image's.
+template <int RULE, int NMAX>
+__device__ __forceinline__ float blend_alpha(const float* al, int pick) {
+  if (RULE == kRuleTwo) return al[1] == 0.f ? al[0] : al[1];
+  float r = 0.f;
+#pragma unroll
+  for (int k = 0; k < NMAX; ++k)
+    if (k == pick) r = al[k];
+  return r;
+}
+
+// Two-image rule (src/cuda/cudaBlend.cu:520-576).
+__device__ __forceinline__ float4 blend_two(const float4 a, const float4 b, const float m) {
+  if (a.w == 0.f) return b;
+  if (b.w == 0.f) return a;
+  const float mm1 = 1.f - m;
+  return make_float4(m * a.x + mm1 * b.x, m * a.y + mm1 * b.y, m * a.z + mm1 * b.z, b.w);
+}
+
+// Three-image rule (src/cuda/cudaBlend3.cu:376-531).
+__device__ __forceinline__ float4 blend_three(const float4* L, float m0, float m1, float m2) {
+  if (L[0].w == 0.f) m0 = 0.f;
+  if (L[1].w == 0.f) m1 = 0.f;
+  if (L[2].w == 0.f) m2 = 0.f;
+  const float sum = (m0 + m1) + m2;
+  if (!(sum > 0.f)) {
+    float4 r = make_float4(0.f, 0.f, 0.f, 0.f);
+    float amax = 0.f;
+#pragma unroll
+    for (int k = 0; k < 3; ++k)
+      if (L[k].w > amax) {
+        amax = L[k].w;
+        r = L[k];
+      }
+    return r;
+  }
+  m0 /= sum;
+  m1 /= sum;
+  m2 /= sum;
+  float aout = 0.f;
+  if (m0 > 0.f && L[0].w > aout) aout = L[0].w;
+  if (m1 > 0.f && L[1].w > aout) aout = L[1].w;
+  if (m2 > 0.f && L[2].w > aout) aout = L[2].w;
+  return make_float4((m0 * L[0].x + m1 * L[1].x) + m2 * L[2].x, (m0 * L[0].y + m1 * L[1].y) + m2 * L[2].y,
+                     (m0 * L[0].z + m1 * L[1].z) + m2 * L[2].z, aout);
+}
+
+// N-way rule (src/cuda/cudaBlendN.cu:199-288).
+template <int NMAX>
+__device__ __forceinline__ float4 blend_nway(const float4* L, int n, float* w) {
+  float sumw = 0.f;
+#pragma unroll
+  for (int k = 0; k < NMAX; ++k)
+    if (k < n) sumw += w[k];
+  if (sumw > 0.f) {
+#pragma unroll
+    for (int k = 0; k < NMAX; ++k)
+      if (k < n) w[k] /= sumw;
+  }
+  float sumw2 = 0.f, amax = 0.f;
+  int aidx = -1;
+#pragma unroll
+  for (int k = 0; k < NMAX; ++k) {
+    if (k < n) {
+      const float al = L[k].w;
+      if (al > amax) {
+        amax = al;
+        aidx = k;
+      }
+      if (al == 0.f) w[k] = 0.f;
+      sumw2 += w[k];
+    }
+  }
+  if (!(sumw2 > 0.f)) {
+    float4 r = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+    for (int k = 0; k < NMAX; ++k)
+      if (k == aidx && amax != 0.f) r = L[k];
+    return r;
+  }
+#pragma unroll
+  for (int k = 0; k < NMAX; ++k)
+    if (k < n) w[k] /= sumw2;
+  float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+  for (int k = 0; k < NMAX; ++k) {
+    if (k < n) {
+      acc.x += w[k] * L[k].x;
+      acc.y += w[k] * L[k].y;
+      acc.z += w[k] * L[k].z;
+      if (w[k] != 0.f && L[k].w > acc.w) acc.w = L[k].w;
+    }
+  }
+  return acc;
+}
+
+// Blend of one pixel at level l >= 1 with mask values m[0..K).
+template <int RULE, int NMAX>
+__device__ __forceinline__ float4 blend_level(int n, const float4* lap, const float* m) {
+  if constexpr (RULE == kRuleTwo) {
+    return blend_two(lap[0], lap[1], m[0]);
+  } else if constexpr (RULE == kRuleThree) {
+    return blend_three(lap, m[0], m[1], m[2]);
+  } else {
+    float w[NMAX];
+#pragma unroll
+    for (int k = 0; k < NMAX; ++k) w[k] = k < n ? m[k] : 0.f;
+    return blend_nway<NMAX>(lap, n, w);
+  }
+}
+
+// Blend of one level-0 pixel from its seam value (two-image weight) or label (one-hot).
+template <int RULE, int NMAX>
+__device__ __forceinline__ float4 blend_level0(int n, const float4* lap, int v) {
+  if constexpr (RULE == kRuleTwo) {
+    return blend_two(lap[0], lap[1], float(v));
+  } else if constexpr (RULE == kRuleThree) {
+    return blend_three(lap, v == 0 ? 1.f : 0.f, v == 1 ? 1.f : 0.f, v == 2 ? 1.f : 0.f);
+  } else {
+    float w[NMAX];
+#pragma unroll
+    for (int k = 0; k < NMAX; ++k) w[k] = v == k ? 1.f : 0.f;
+    return blend_nway<NMAX>(lap, n, w);
+  }
+}
+
+// Read-only loads of a level buffer in HBM (through the non-coherent cache).
+__device__ __forceinline__ float4 ldg_level(const float4* p) { return __ldg(p); }
+__device__ __forceinline__ float4 ldg_level(const half4* p) {
+  const uint2 raw = __ldg(reinterpret_cast<const uint2*>(p));
+  const __half2 a = *reinterpret_cast<const __half2*>(&raw.x);
+  const __half2 b = *reinterpret_cast<const __half2*>(&raw.y);
+  const float2 fa = __half22float2(a), fb = __half22float2(b);
+  return make_float4(fa.x, fa.y, fb.x, fb.y);
+}
+
+}  // namespace hmp

@@ -34,6 +34,7 @@ struct PyrArgs {
   int opaque;
   int tile;  // tile edge (level 0 for pyr_down, level 1 for pyr_coarse)
   float4* R1;  // level-1 reconstruction [batch][lh1][lw1] (levels >= 2)
+  float4* Rl[kDevMaxLevels];  // Binomial5 filter: reconstruction R^l, l = 1..L-1, [batch][lh][lw]
   CanvasDev C;
   int wx0, wy0, wx1, wy1;  // write rect, blend coordinates, end exclusive
   int cx_off, cy_off;      // canvas = blend + offset
@@ -53,6 +54,10 @@ cudaError_t launch_pyr_coarse(const PyrArgs& a, int rule, int storage, dim3 grid
 
 // Level 0 of the write rect: blend + reconstruct + pack; grid = 64 x 16 pixel blocks x batch.
 cudaError_t launch_pyr_fine(const PyrArgs& a, int rule, int storage, dim3 grid, cudaStream_t stream);
+
+// Binomial5 filter: the whole pyramid (levels >= 2) as a level-by-level chain of launches.
+cudaError_t launch_b5_pyramid(const PyrArgs& a, int rule, int storage, int batch, cudaStream_t stream);
+int b5_launches(int levels);
 
 size_t pyr_down_smem(int n, int tile);
 // Shared memory of a pyr_coarse CTA (levels 2..L-1 of its tile with halos).

@@ -56,6 +56,8 @@ struct hmp_stitcher {
   int tile_down = 0, tile_coarse = 0;
   size_t coarse_smem = 0;
   float4* R1 = nullptr;
+  bool b5 = false;  // Binomial5 filter with at least two levels
+  float4* Rl[hmp::kDevMaxLevels]{};
   cudaStream_t aux = nullptr;
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   double m0_bytes = 0;
@@ -133,8 +135,6 @@ struct hmp_stitcher {
       if (e != cudaSuccess) return cuda_status(e, "canvas plane upload");
     }
     launches = p.canvas_plane_used ? 1 : 0;
-    if (p.levels > 0 && p.filter != HMP_FILTER_REFBOX)
-      return make_status(HMP_ERR_NOT_SUPPORTED, "the Binomial5 pyramid filter has no GPU kernels in this build");
     if (p.levels > 0) {
       const int n = p.n, B = p.batch, L = p.levels;
       for (int k = 0; k < n; ++k) {
@@ -176,17 +176,24 @@ struct hmp_stitcher {
       tile_down = std::max(n <= 3 ? 64 : 32, align);
       tile_coarse = std::max(32, align / 2);
       coarse_smem = hmp::pyr_coarse_smem(n, p.mask_k, tile_coarse, L, p.storage);
-      if (L > 1) {
+      b5 = p.filter == HMP_FILTER_BINOMIAL5 && L > 1;
+      if (L > 1 && !b5) {
         void* r = nullptr;
         e = alloc(&r, size_t(B) * p.lw[1] * p.lh[1] * sizeof(float4));
         if (e != cudaSuccess) return cuda_status(e, "reconstruction buffer");
         R1 = static_cast<float4*>(r);
       }
+      for (int l = 1; b5 && l < L; ++l) {
+        void* r = nullptr;
+        e = alloc(&r, size_t(B) * p.lw[l] * p.lh[l] * sizeof(float4));
+        if (e != cudaSuccess) return cuda_status(e, "reconstruction buffer");
+        Rl[l] = static_cast<float4*>(r);
+      }
       if (hmp::pyr_down_smem(n, tile_down) > 227 * 1024)
         return make_status(HMP_ERR_NOT_SUPPORTED, "pyramid tile does not fit in shared memory");
       if (coarse_smem > 227 * 1024)
         return make_status(HMP_ERR_NOT_SUPPORTED, "pyramid tile does not fit in shared memory");
-      launches += (L > 1 ? 2 : 0) + 1;
+      launches += b5 ? hmp::b5_launches(L) : (L > 1 ? 2 : 0) + 1;
     }
     if (p.canvas_plane_used && p.levels > 0) {
       // The pyramid chain (latency-bound, few CTAs) runs on a high-priority stream so that its
@@ -377,7 +384,15 @@ struct hmp_stitcher {
     a.wy1 = a.wy0 + p.write.h;
     a.cx_off = p.blend.x;
     a.cy_off = p.blend.y;
-    if (p.levels > 1) {
+    if (b5) {
+      // Binomial5: the level-by-level chain (its time is reported under pyr_down).
+      for (int l = 1; l < p.levels; ++l) a.Rl[l] = Rl[l];
+      tbegin(1, ps);
+      e = hmp::launch_b5_pyramid(a, p.rule, p.storage, p.batch, ps);
+      tend(1, ps);
+      if (e != cudaSuccess) return cuda_status(e, "Binomial5 pyramid launch");
+    }
+    if (p.levels > 1 && !b5) {
       a.tile = tile_down;
       const dim3 grid((p.lw[0] + tile_down - 1) / tile_down, (p.lh[0] + tile_down - 1) / tile_down, p.batch);
       tbegin(1, ps);
@@ -386,7 +401,7 @@ struct hmp_stitcher {
       if (e != cudaSuccess) return cuda_status(e, "pyr_down launch");
     }
     a.R1 = R1;
-    if (p.levels > 1) {
+    if (p.levels > 1 && !b5) {
       // Level-1 pixels the fine pass reads: floor(x/2) and floor(x/2)+1 of the write rect.
       const int x1lo = a.wx0 >> 1, x1hi = std::min(((a.wx1 - 1) >> 1) + 2, p.lw[1]);
       const int y1lo = a.wy0 >> 1, y1hi = std::min(((a.wy1 - 1) >> 1) + 2, p.lh[1]);
@@ -400,7 +415,7 @@ struct hmp_stitcher {
       tend(2, ps);
       if (e != cudaSuccess) return cuda_status(e, "pyr_coarse launch");
     }
-    {
+    if (!b5) {
       const int fx0 = a.wx0 & ~1, fy0 = a.wy0 & ~1;
       const dim3 fgrid((a.wx1 - fx0 + 63) / 64, (a.wy1 - fy0 + 15) / 16, p.batch);
       tbegin(3, ps);

@@ -153,7 +153,7 @@ HMP_API hmp_status hmp_stitcher_process(hmp_stitcher* st, const hmp_image* input
 /* Per-kernel device time of process() calls made while timing is enabled, measured with CUDA
  * events recorded on the stream each kernel is launched on (the pyramid kernels run on the
  * stitcher's auxiliary stream). Index 0 = canvas_gather, 1 = pyr_down, 2 = pyr_coarse,
- * 3 = pyr_fine. */
+ * 3 = pyr_fine; with the Binomial5 filter index 1 holds its whole pyramid chain. */
 typedef struct hmp_kernel_timing {
   double total_ms[4];
   long long launches[4];
