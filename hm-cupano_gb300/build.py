@@ -32,8 +32,9 @@ UNITS = {
     "hmp_stitcher.cu": [],
     "hmp_noalloc.cu": ["-fmad=false"],
     "hmp_binomial.cu": ["-fmad=false"],
+    "hmp_server.cpp": [],
 }
-HEADERS = ["hmp_plan.h", "hmp_device.cuh", "hmp_kernels.h", "hmp_blend.cuh"]
+HEADERS = ["hmp_plan.h", "hmp_device.cuh", "hmp_kernels.h", "hmp_blend.cuh", "hmp_admission.h"]
 
 
 def nvcc() -> str:

@@ -205,7 +205,9 @@ struct hmp_stitcher {
       if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev_join, cudaEventDisableTiming);
       if (e != cudaSuccess) return cuda_status(e, "stream setup");
     }
-    e = cudaDeviceSynchronize();
+    // The uploads and clears ran on the legacy default stream; wait for them only, so that a
+    // stitcher created while others run (a server admitting a configuration) does not stall them.
+    e = cudaStreamSynchronize(nullptr);
     if (e != cudaSuccess) return cuda_status(e, "upload");
     compute_m0();
     // Release the large host-side arrays; geometry stays.

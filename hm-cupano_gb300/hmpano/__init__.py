@@ -14,6 +14,7 @@ from .pano import (
     CudaStitchPano3,
     CudaStitchPanoN,
     SpatialTiff,
+    StitchServer,
     plan_geometry,
 )
 
@@ -27,6 +28,7 @@ __all__ = [
     "CudaStitchPano3",
     "CudaStitchPanoN",
     "SpatialTiff",
+    "StitchServer",
     "UNMAPPED_POSITION_VALUE",
     "plan_geometry",
 ]

@@ -79,6 +79,29 @@ class KernelTiming(C.Structure):
     _fields_ = [("total_ms", C.c_double * 4), ("launches", C.c_longlong * 4)]
 
 
+class ServerOptions(C.Structure):
+    _fields_ = [("hbm_budget_bytes", C.c_size_t), ("slots", C.c_int), ("max_instances_per_config", C.c_int)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [
+        ("submitted", C.c_longlong),
+        ("completed", C.c_longlong),
+        ("failed", C.c_longlong),
+        ("instances_created", C.c_longlong),
+        ("instances_evicted", C.c_longlong),
+        ("max_in_flight", C.c_int),
+        ("p50_ms", C.c_double),
+        ("p99_ms", C.c_double),
+        ("mean_ms", C.c_double),
+        ("max_ms", C.c_double),
+        ("span_ms", C.c_double),
+        ("canvas_mpix", C.c_double),
+        ("resident_bytes", C.c_double),
+        ("resident_bytes_peak", C.c_double),
+    ]
+
+
 # Every symbol include/hmpano.h declares, with its signature.
 SIGNATURES = {
     "hmp_version": ([], C.c_char_p),
@@ -93,6 +116,15 @@ SIGNATURES = {
     "hmp_stitcher_set_timing": ([C.c_void_p, C.c_int], Status),
     "hmp_stitcher_get_timing": ([C.c_void_p, C.POINTER(KernelTiming)], Status),
     "hmp_plan_geometry": ([C.POINTER(Config), C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)], Status),
+    "hmp_server_create": ([C.POINTER(ServerOptions), C.POINTER(C.c_void_p)], Status),
+    "hmp_server_destroy": ([C.c_void_p], None),
+    "hmp_server_add_config": ([C.c_void_p, C.POINTER(Config), C.POINTER(C.c_int)], Status),
+    "hmp_server_submit": ([C.c_void_p, C.c_int, C.POINTER(Image), C.c_int, C.POINTER(Image), C.POINTER(C.c_longlong)],
+                          Status),
+    "hmp_server_wait": ([C.c_void_p, C.c_longlong, C.c_int], Status),
+    "hmp_server_drain": ([C.c_void_p, C.c_int], Status),
+    "hmp_server_get_stats": ([C.c_void_p, C.POINTER(ServerStats)], Status),
+    "hmp_server_reset_stats": ([C.c_void_p], None),
     "hmp_blend2_noalloc": ([C.POINTER(Image), C.POINTER(Image), C.c_void_p, C.c_size_t, C.c_int, C.c_int,
                             C.POINTER(Image), C.c_void_p], Status),
 }

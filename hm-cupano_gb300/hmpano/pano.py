@@ -352,3 +352,76 @@ def plan_geometry(kind: int, control_masks, num_levels: int, minimize_blend: boo
         raise CudaStatusError(st)
     v = list(out)
     return {"canvas": (cw.value, ch.value), "blend": tuple(v[0:4]), "write": tuple(v[4:8]), "levels": v[8]}
+
+
+class StitchServer:
+    """Continuous-batching stitch server over hmp_server_* (include/hmpano.h).
+
+    Register configurations first (``add_config``), then ``submit`` requests from any thread;
+    ``wait`` / ``drain`` return their statuses. Input and canvas tensors are kept referenced here
+    until their request finished.
+    """
+
+    def __init__(self, hbm_budget_bytes: int, slots: int = 4, max_instances_per_config: int = 2):
+        self._h = C.c_void_p()
+        opt = _lib.ServerOptions(int(hbm_budget_bytes), int(slots), int(max_instances_per_config))
+        st = _status(_lib.lib().hmp_server_create(C.byref(opt), C.byref(self._h)))
+        if not st.ok():
+            raise CudaStatusError(st)
+        self._live = {}
+        self._canvas = {}
+
+    def close(self) -> None:
+        if self._h:
+            _lib.lib().hmp_server_destroy(self._h)
+            self._h = C.c_void_p()
+            self._live.clear()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def add_config(self, kind: int, control_masks, num_levels: int, batch_size: int = 1, minimize_blend: bool = True,
+                   fused: bool = True, storage: str = "f32", filter: str = "refbox") -> int:
+        cfg, keep = build_config(kind, control_masks, num_levels, batch_size, minimize_blend, fused, storage, filter)
+        cid = C.c_int()
+        st = _status(_lib.lib().hmp_server_add_config(self._h, C.byref(cfg), C.byref(cid)))
+        del keep
+        if not st.ok():
+            raise CudaStatusError(st)
+        return int(cid.value)
+
+    def submit(self, config_id: int, inputs: Sequence, canvas) -> int:
+        batched = [_ensure_batched(t) for t in inputs]
+        canvas = _ensure_batched(canvas)
+        imgs = (Image * len(batched))(*[_image(t) for t in batched])
+        cv = _image(canvas)
+        rid = C.c_longlong()
+        st = _status(_lib.lib().hmp_server_submit(self._h, int(config_id), imgs, len(batched), C.byref(cv),
+                                                  C.byref(rid)))
+        if not st.ok():
+            raise CudaStatusError(st)
+        self._live[int(rid.value)] = (batched, canvas)
+        return int(rid.value)
+
+    def wait(self, request_id: int, timeout_ms: int = 60000) -> CudaStatus:
+        st = _status(_lib.lib().hmp_server_wait(self._h, int(request_id), int(timeout_ms)))
+        if st.code != 909:
+            self._live.pop(int(request_id), None)
+        return st
+
+    def drain(self, timeout_ms: int = 600000) -> CudaStatus:
+        st = _status(_lib.lib().hmp_server_drain(self._h, int(timeout_ms)))
+        if st.ok():
+            self._live.clear()
+        return st
+
+    def stats(self) -> dict:
+        s = _lib.ServerStats()
+        _lib.lib().hmp_server_get_stats(self._h, C.byref(s))
+        return {name: getattr(s, name) for name, _ in _lib.ServerStats._fields_}
+
+    def reset_stats(self) -> None:
+        _lib.lib().hmp_server_reset_stats(self._h)

@@ -200,6 +200,46 @@ HMP_API hmp_status hmp_blend2_noalloc(const hmp_image* image1, const hmp_image* 
                                       size_t seam_pitch, int num_levels, int batch_size, const hmp_image* out,
                                       void* stream);
 
+/* ---- Stitch server: continuous batching of requests for many pano configurations. ----
+ * No counterpart in the reference (it stitches one configuration per process). Configurations are
+ * registered once (host tables copied); requests (configuration, device inputs, device canvas)
+ * are submitted from any thread and run as soon as one of `slots` streams and a resident stitcher
+ * of their configuration are free, so requests that arrive while others run overlap on the GPU.
+ * Stitchers stay resident (tables, seam, pyramid scratch) within `hbm_budget_bytes`; idle ones are
+ * evicted least-recently-used when a new one does not fit. Inputs and canvas must stay valid until
+ * the request finishes (hmp_server_wait / hmp_server_drain). */
+typedef struct hmp_server hmp_server;
+
+typedef struct hmp_server_options {
+  size_t hbm_budget_bytes;      /* device bytes resident stitchers may hold together */
+  int slots;                    /* requests on the GPU at once, one stream each (1..64) */
+  int max_instances_per_config; /* resident stitchers per configuration (one request each at a time) */
+} hmp_server_options;
+
+typedef struct hmp_server_stats {
+  long long submitted, completed, failed;
+  long long instances_created, instances_evicted;
+  int max_in_flight;
+  double p50_ms, p99_ms, mean_ms, max_ms; /* latency: observed completion - submission (host clock) */
+  double span_ms;                         /* first submission to last completion */
+  double canvas_mpix;                     /* canvas megapixels completed (frames x canvas) */
+  double resident_bytes, resident_bytes_peak;
+} hmp_server_stats;
+
+HMP_API hmp_status hmp_server_create(const hmp_server_options* options, hmp_server** out);
+/* Finishes every submitted request, then releases the server's streams and stitchers. */
+HMP_API void hmp_server_destroy(hmp_server* server);
+/* Register a configuration (as for hmp_stitcher_create) while no request is outstanding. */
+HMP_API hmp_status hmp_server_add_config(hmp_server* server, const hmp_config* cfg, int* config_id);
+HMP_API hmp_status hmp_server_submit(hmp_server* server, int config_id, const hmp_image* inputs, int n_inputs,
+                                     const hmp_image* canvas, long long* request_id);
+/* The request's own status once it finished, or HMP_ERR_TIMEOUT after timeout_ms. */
+HMP_API hmp_status hmp_server_wait(hmp_server* server, long long request_id, int timeout_ms);
+/* Wait until no request is outstanding (HMP_ERR_TIMEOUT after timeout_ms). */
+HMP_API hmp_status hmp_server_drain(hmp_server* server, int timeout_ms);
+HMP_API hmp_status hmp_server_get_stats(hmp_server* server, hmp_server_stats* stats);
+HMP_API void hmp_server_reset_stats(hmp_server* server);
+
 /* Geometry of a configuration computed on the host only (no device work): blend rect, write
  * rect and effective levels, out9 = {bx, by, bw, bh, wx, wy, ww, wh, levels}; also the canvas
  * size. Mirrors CanvasManager::updateMinimizeBlend / convertMaskMat (src/pano/canvasManager.cpp:
