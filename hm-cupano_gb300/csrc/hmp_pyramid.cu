@@ -379,6 +379,25 @@ __global__ void __launch_bounds__(256) pyr_coarse_kernel(const __grid_constant__
       rby[l] = by;
     }
   }
+  // Slots whose plane misses the level-0 footprint of every region read here have all-zero levels
+  // (alpha 0) in it: the blend never picks them, so their loads are skipped and they read as 0.
+  uint32_t amask = 0;
+  {
+    int fx0 = rax[1] << 1, fy0 = ray[1] << 1, fx1 = rbx[1] << 1, fy1 = rby[1] << 1;
+#pragma unroll
+    for (int l = 2; l < kL; ++l) {
+      if (l >= L) break;
+      fx0 = min(fx0, rax[l] << l);
+      fy0 = min(fy0, ray[l] << l);
+      fx1 = max(fx1, rbx[l] << l);
+      fy1 = max(fy1, rby[l] << l);
+    }
+#pragma unroll
+    for (int k = 0; k < NMAX; ++k) {
+      const PlaneDev& P = a.slot[k];
+      if (k < n && fx0 < P.x0 + P.w && P.x0 < fx1 && fy0 < P.y0 + P.h && P.y0 < fy1) amask |= 1u << k;
+    }
+  }
 #pragma unroll
   for (int l = 2; l < kL; ++l) {
     if (l >= L) break;
@@ -388,6 +407,7 @@ __global__ void __launch_bounds__(256) pyr_coarse_kernel(const __grid_constant__
 #pragma unroll
     for (int k = 0; k < NMAX; ++k) {
       if (k >= n) break;
+      if (!((amask >> k) & 1u)) continue;
       const Store* Gl = static_cast<const Store*>(a.G[k][l]) + (long long)b * lw * lh;
       Store* gl = reinterpret_cast<Store*>(smb + lo.g[l]) + k * CAP;
       for (int i = tid; i < CAP; i += 256) {
@@ -431,12 +451,15 @@ __global__ void __launch_bounds__(256) pyr_coarse_kernel(const __grid_constant__
       const int px = lax + x, py = lay + y;
       float al[NMAX];
 #pragma unroll
-      for (int k = 0; k < NMAX; ++k) al[k] = k < n ? load_level(gcur + k * CAP + i).w : 0.f;
+      for (int k = 0; k < NMAX; ++k) al[k] = ((amask >> k) & 1u) ? load_level(gcur + k * CAP + i).w : 0.f;
       const int pk = blend_pick<RULE, NMAX>(n, al, mb + i * K);
       float4 r = make_float4(0.f, 0.f, 0.f, 0.f);
       if (pk >= 0) {
-        float4 g = load_level(gcur + pk * CAP + i);
-        if (has_next) {
+        // The two-image rule can pick an inactive slot (image 2 where neither has alpha); its
+        // levels are all zero here, so its Laplacian is zero.
+        const bool act = (amask >> pk) & 1u;
+        float4 g = act ? load_level(gcur + pk * CAP + i) : make_float4(0.f, 0.f, 0.f, 0.f);
+        if (has_next && act) {
           const float3 up = up_alpha(gnext + pk * CAPN, CWN, nax, nay, lwn, lhn, px, py);
           g.x = g.x - up.x;
           g.y = g.y - up.y;
@@ -447,7 +470,7 @@ __global__ void __launch_bounds__(256) pyr_coarse_kernel(const __grid_constant__
         float4 lap[NMAX];
 #pragma unroll
         for (int k = 0; k < NMAX; ++k) {
-          if (k < n) {
+          if ((amask >> k) & 1u) {
             float4 g = load_level(gcur + k * CAP + i);
             if (has_next) {
               const float3 up = up_alpha(gnext + k * CAPN, CWN, nax, nay, lwn, lhn, px, py);
@@ -498,8 +521,8 @@ __global__ void __launch_bounds__(256) pyr_coarse_kernel(const __grid_constant__
       m[q] = q < K ? __ldg(a.maskL[1] + o1 * K + q) : 0.f;
 #pragma unroll
     for (int k = 0; k < NMAX; ++k) {
-      g1[k] = k < n ? ldg_level(static_cast<const Store*>(a.G[k][1]) + (long long)b * lw1 * lh1 + o1)
-                    : make_float4(0.f, 0.f, 0.f, 0.f);
+      g1[k] = ((amask >> k) & 1u) ? ldg_level(static_cast<const Store*>(a.G[k][1]) + (long long)b * lw1 * lh1 + o1)
+                                  : make_float4(0.f, 0.f, 0.f, 0.f);
       al[k] = g1[k].w;
     }
     const int pk = blend_pick<RULE, NMAX>(n, al, m);
@@ -509,7 +532,7 @@ __global__ void __launch_bounds__(256) pyr_coarse_kernel(const __grid_constant__
 #pragma unroll
       for (int k = 1; k < NMAX; ++k)
         if (k == pk) g = g1[k];
-      if (has2) {
+      if (has2 && ((amask >> pk) & 1u)) {
         const float3 up = up_alpha(g2 + pk * CAP2, CW2, nax, nay, lw2, lh2, px, py);
         g.x = g.x - up.x;
         g.y = g.y - up.y;
@@ -519,7 +542,7 @@ __global__ void __launch_bounds__(256) pyr_coarse_kernel(const __grid_constant__
     } else if (pk == kPickAll) {
 #pragma unroll
       for (int k = 0; k < NMAX; ++k) {
-        if (k < n && has2) {
+        if (((amask >> k) & 1u) && has2) {
           const float3 up = up_alpha(g2 + k * CAP2, CW2, nax, nay, lw2, lh2, px, py);
           g1[k].x = g1[k].x - up.x;
           g1[k].y = g1[k].y - up.y;
@@ -599,6 +622,16 @@ __global__ void __launch_bounds__(256) pyr_fine_kernel(const __grid_constant__ P
   const int lw0 = a.lw[0], lh0 = a.lh[0], lw1 = a.lw[1], lh1 = a.lh[1];
   float4* rs = fsm;
   Store* gs = reinterpret_cast<Store*>(fsm + kFineTA);
+  // A slot whose plane misses the level-0 footprint of this block's G^1 taps (the block plus the
+  // 2-pixel upsample halo) has zero pixels (alpha 0) and zero G^1 taps here, so the blend reads
+  // nothing non-zero from it: its lookups and G^1 tiles are skipped. (The halo matters: the
+  // two-image rule returns image 2's Laplacian, 0 - up(G^1), where neither image has alpha.)
+  uint32_t amask = 0;
+#pragma unroll
+  for (int k = 0; k < NMAX; ++k) {
+    const PlaneDev& P = a.slot[k];
+    if (k < n && bx0 < P.x0 + P.w && P.x0 < bx0 + 66 && by0 < P.y0 + P.h && P.y0 < by0 + 18) amask |= 1u << k;
+  }
   if (has1) {
     const int tx0 = bx0 >> 1, ty0 = by0 >> 1;
     const long long fo = (long long)b * lw1 * lh1;
@@ -608,82 +641,94 @@ __global__ void __launch_bounds__(256) pyr_fine_kernel(const __grid_constant__ P
       cp_async<16>(rs + j, a.R1 + o);
 #pragma unroll
       for (int k = 0; k < NMAX; ++k)
-        if (k < n) cp_async<int(sizeof(Store))>(gs + k * kFineTA + j, static_cast<const Store*>(a.G[k][1]) + o);
+        if ((amask >> k) & 1u)
+          cp_async<int(sizeof(Store))>(gs + k * kFineTA + j, static_cast<const Store*>(a.G[k][1]) + o);
     }
     asm volatile("cp.async.commit_group;\n" ::: "memory");
   }
-  int own[4][NMAX], mv[4];
-  uint32_t ent[4][NMAX];
-  bool live[4];
-#pragma unroll
-  for (int q = 0; q < 4; ++q) {
-    const int x = X + (q & 1), y = Y + (q >> 1);
-    live[q] = x < lw0 && y < lh0 && x >= a.wx0 && x < a.wx1 && y >= a.wy0 && y < a.wy1;
-    mv[q] = live[q] ? int(__ldg(a.mask0 + (long long)y * a.mask0_pitch + x)) : 0;
-#pragma unroll
-    for (int k = 0; k < NMAX; ++k) {
-      own[q][k] = 0xFF;
-      ent[q][k] = 0xFFFFFFFFu;
-      if (live[q] && k < n) slot_lookup(a.slot[k], k, x, y, own[q][k], ent[q][k]);
-    }
-  }
-  uchar4 src[4][NMAX];
-#pragma unroll
-  for (int q = 0; q < 4; ++q)
-#pragma unroll
-    for (int k = 0; k < NMAX; ++k) src[q][k] = slot_fetch<NMAX>(a, k, own[q][k], ent[q][k], b, opaque);
-  if (has1) {
-    asm volatile("cp.async.wait_group 0;\n" ::: "memory");
-    __syncthreads();
-  }
+  // Pixels of the quad are processed QB at a time: all four (every lookup and gather in flight
+  // together) for up to three images; one at a time for the N-way kernel, whose eight images'
+  // arrays would not fit in registers four times over.
+  constexpr int QB = NMAX > 3 ? 1 : 4;
   const int ti = warp * kFineTW + lane;  // tap (0,0) of the quad in the tiles
 #pragma unroll
-  for (int q = 0; q < 4; ++q) {
-    if (!live[q]) continue;
-    const bool ox = (q & 1) != 0, oy = (q >> 1) != 0;
-    float al[NMAX];
+  for (int q0 = 0; q0 < 4; q0 += QB) {
+    int own[QB][NMAX], mv[QB];
+    uint32_t ent[QB][NMAX];
+    bool live[QB];
 #pragma unroll
-    for (int k = 0; k < NMAX; ++k) al[k] = float(src[q][k].w);
-    const int pk = blend_pick0<RULE, NMAX>(n, al, mv[q]);
-    float4 r = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (pk >= 0) {
-      uchar4 sp = src[q][0];
-#pragma unroll
-      for (int k = 1; k < NMAX; ++k)
-        if (k == pk) sp = src[q][k];
-      float4 g = to_f4(sp);
-      if (has1) {
-        const float3 up = up_tile(gs + pk * kFineTA, ti, ox, oy);
-        g.x = g.x - up.x;
-        g.y = g.y - up.y;
-        g.z = g.z - up.z;
-      }
-      r = make_float4(g.x, g.y, g.z, blend_alpha<RULE, NMAX>(al, pk));
-    } else if (pk == kPickAll) {
-      float4 lap[NMAX];
+    for (int u = 0; u < QB; ++u) {
+      const int q = q0 + u;
+      const int x = X + (q & 1), y = Y + (q >> 1);
+      live[u] = x < lw0 && y < lh0 && x >= a.wx0 && x < a.wx1 && y >= a.wy0 && y < a.wy1;
+      mv[u] = live[u] ? int(__ldg(a.mask0 + (long long)y * a.mask0_pitch + x)) : 0;
 #pragma unroll
       for (int k = 0; k < NMAX; ++k) {
-        float4 g = to_f4(src[q][k]);
-        if (has1 && k < n) {
-          const float3 up = up_tile(gs + k * kFineTA, ti, ox, oy);
+        own[u][k] = 0xFF;
+        ent[u][k] = 0xFFFFFFFFu;
+        if (live[u] && ((amask >> k) & 1u)) slot_lookup(a.slot[k], k, x, y, own[u][k], ent[u][k]);
+      }
+    }
+    uchar4 src[QB][NMAX];
+#pragma unroll
+    for (int u = 0; u < QB; ++u)
+#pragma unroll
+      for (int k = 0; k < NMAX; ++k)
+        src[u][k] = ((amask >> k) & 1u) ? slot_fetch<NMAX>(a, k, own[u][k], ent[u][k], b, opaque)
+                                        : make_uchar4(0, 0, 0, 0);
+    if (q0 == 0 && has1) {
+      asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+      __syncthreads();
+    }
+#pragma unroll
+    for (int u = 0; u < QB; ++u) {
+      const int q = q0 + u;
+      if (!live[u]) continue;
+      const bool ox = (q & 1) != 0, oy = (q >> 1) != 0;
+      float al[NMAX];
+#pragma unroll
+      for (int k = 0; k < NMAX; ++k) al[k] = float(src[u][k].w);
+      const int pk = blend_pick0<RULE, NMAX>(n, al, mv[u]);
+      float4 r = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (pk >= 0) {
+        uchar4 sp = src[u][0];
+#pragma unroll
+        for (int k = 1; k < NMAX; ++k)
+          if (k == pk) sp = src[u][k];
+        float4 g = to_f4(sp);
+        if (has1 && ((amask >> pk) & 1u)) {  // an inactive slot's G^1 taps are all zero here
+          const float3 up = up_tile(gs + pk * kFineTA, ti, ox, oy);
           g.x = g.x - up.x;
           g.y = g.y - up.y;
           g.z = g.z - up.z;
         }
-        lap[k] = g;
+        r = make_float4(g.x, g.y, g.z, blend_alpha<RULE, NMAX>(al, pk));
+      } else if (pk == kPickAll) {
+        float4 lap[NMAX];
+#pragma unroll
+        for (int k = 0; k < NMAX; ++k) {
+          float4 g = to_f4(src[u][k]);
+          if (has1 && ((amask >> k) & 1u)) {
+            const float3 up = up_tile(gs + k * kFineTA, ti, ox, oy);
+            g.x = g.x - up.x;
+            g.y = g.y - up.y;
+            g.z = g.z - up.z;
+          }
+          lap[k] = g;
+        }
+        r = blend_level0<RULE, NMAX>(n, lap, mv[u]);
       }
-      r = blend_level0<RULE, NMAX>(n, lap, mv[q]);
+      if (has1) {
+        const float3 up = up_tile(rs, ti, ox, oy);
+        r.x = up.x + r.x;
+        r.y = up.y + r.y;
+        r.z = up.z + r.z;
+      }
+      const int px = X + (q & 1), py = Y + (q >> 1);
+      uchar4* crow = reinterpret_cast<uchar4*>(reinterpret_cast<char*>(a.C.ptr) + b * a.C.bstride +
+                                               (long long)(py + a.cy_off) * a.C.pitch);
+      crow[px + a.cx_off] = pack_rgba(r);
     }
-    if (has1) {
-      const float3 up = up_tile(rs, ti, ox, oy);
-      r.x = up.x + r.x;
-      r.y = up.y + r.y;
-      r.z = up.z + r.z;
-    }
-    const int px = X + (q & 1), py = Y + (q >> 1);
-    uchar4* crow = reinterpret_cast<uchar4*>(reinterpret_cast<char*>(a.C.ptr) + b * a.C.bstride +
-                                             (long long)(py + a.cy_off) * a.C.pitch);
-    crow[px + a.cx_off] = pack_rgba(r);
   }
 }
 
