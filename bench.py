@@ -17,7 +17,12 @@ the kernel's own), against the measured HBM copy bandwidth; ``hbm_frac_frame`` i
 compulsory bytes over the concurrent frame time. ``cpu_baseline`` is the oracle (a C port of the
 reference's algorithm) on the host cores. ``--impl reference`` times that CPU implementation as
 the reference arm. ``vs_baseline`` is fps over the reference's published 340 fps (RTX 4090, same
-metric). Multi-GPU runs are independent replicas (weak scaling, no collective on the data path).
+metric). ``batched`` is the multi-stream batched job (hmpano/batch.py): one CUDA graph per job,
+frames per call and tiles autotuned, FP16 storage, against the plain per-frame path on the same
+frames. ``serve`` is the serving sweep (hmpano/serve_bench.py): 12 seeded configurations,
+Poisson arrivals at fractions of the saturation rate, p50/p99 latency, against the plain
+per-frame path on the same request mix. Multi-GPU runs are independent replicas (weak scaling,
+no collective on the data path).
 """
 from __future__ import annotations
 
@@ -197,6 +202,9 @@ def main() -> None:
                     help="capture one process() per buffer set into a CUDA graph and replay it")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-serve", action="store_true", help="skip the serving sweep (p50/p99 latency)")
+    ap.add_argument("--no-batched", action="store_true", help="skip the batched multi-stream graph job")
+    ap.add_argument("--serve-seconds", type=float, default=1.0, help="arrival window per offered rate")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     if args.impl == "reference":
@@ -435,6 +443,17 @@ def main() -> None:
     }
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(rig, host_frames, args.levels)
+    if not args.no_batched and world == 1:
+        # Batched streaming job: 4 two-image + 4 three-image streams x 32 frames, FP16 storage, one
+        # CUDA graph, frames per call and tiles autotuned.
+        from hmpano import batch
+
+        line["batched"] = batch.run(dev)
+    if not args.no_serve:
+        # Serving mix on this GPU: 12 configurations, Poisson arrivals, 150 GB admission budget.
+        from hmpano import serve_bench
+
+        line["serve"] = serve_bench.sweep(dev, seconds=args.serve_seconds)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if dist:

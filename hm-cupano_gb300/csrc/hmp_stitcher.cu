@@ -518,6 +518,24 @@ HMP_API hmp_status hmp_stitcher_process(hmp_stitcher* st, const hmp_image* input
   return s;
 }
 
+HMP_API hmp_status hmp_stitcher_set_tiles(hmp_stitcher* st, int tile_down, int tile_coarse) {
+  if (!st) return make_status(HMP_ERR_INVALID_VALUE, "stitcher is null");
+  if (st->status.code != HMP_OK) return st->status;
+  const hmp::Plan& p = st->plan;
+  if (p.levels < 2) return make_status(HMP_OK, "");  // no pyramid tiles to choose
+  const int align = 1 << (p.levels - 1);
+  if ((tile_down != 32 && tile_down != 64) || tile_down % align != 0)
+    return make_status(HMP_ERR_INVALID_VALUE, "tile_down must be 32 or 64 and a multiple of 2^(levels-1)");
+  if (tile_coarse != 32 || (tile_coarse * 2) % align != 0)
+    return make_status(HMP_ERR_INVALID_VALUE, "tile_coarse must be 32");
+  if (hmp::pyr_down_smem(p.n, tile_down) > 227 * 1024)
+    return make_status(HMP_ERR_NOT_SUPPORTED, "pyramid tile does not fit in shared memory");
+  st->tile_down = tile_down;
+  st->tile_coarse = tile_coarse;
+  st->coarse_smem = hmp::pyr_coarse_smem(p.n, p.mask_k, tile_coarse, p.levels, p.storage);
+  return make_status(HMP_OK, "");
+}
+
 HMP_API hmp_status hmp_stitcher_set_timing(hmp_stitcher* st, int enable) {
   if (!st) return make_status(HMP_ERR_INVALID_VALUE, "stitcher is null");
   const cudaError_t e = st->timing_enable(enable);

@@ -114,6 +114,7 @@ SIGNATURES = {
     "hmp_stitcher_get_info": ([C.c_void_p, C.POINTER(StitcherInfo)], Status),
     "hmp_stitcher_process": ([C.c_void_p, C.POINTER(Image), C.c_int, C.POINTER(Image), C.c_void_p], Status),
     "hmp_stitcher_set_timing": ([C.c_void_p, C.c_int], Status),
+    "hmp_stitcher_set_tiles": ([C.c_void_p, C.c_int, C.c_int], Status),
     "hmp_stitcher_get_timing": ([C.c_void_p, C.POINTER(KernelTiming)], Status),
     "hmp_plan_geometry": ([C.POINTER(Config), C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)], Status),
     "hmp_server_create": ([C.POINTER(ServerOptions), C.POINTER(C.c_void_p)], Status),

@@ -240,6 +240,12 @@ class _Stitcher:
             "device_bytes": inf.device_bytes,
         }
 
+    def set_tiles(self, tile_down: int, tile_coarse: int = 32) -> None:
+        """Pyramid tile edges (tuning only: every choice gives the same bits)."""
+        s = _status(_lib.lib().hmp_stitcher_set_tiles(self._handle, int(tile_down), int(tile_coarse)))
+        if not s.ok():
+            raise CudaStatusError(s)
+
     def set_timing(self, enable: bool, serialize: bool = False) -> None:
         """Record per-kernel CUDA-event times of subsequent process() calls; ``serialize`` also runs
         the kernels one after another on the caller stream, so each time is the kernel alone."""

@@ -150,6 +150,11 @@ HMP_API hmp_status hmp_stitcher_get_info(const hmp_stitcher* st, hmp_stitcher_in
 HMP_API hmp_status hmp_stitcher_process(hmp_stitcher* st, const hmp_image* inputs, int n_inputs,
                                         const hmp_image* canvas, void* stream);
 
+/* Tile edges of the pyramid kernels (a tuning knob, results are identical for every choice):
+ * tile_down 32 or 64 level-0 pixels (a multiple of 2^(levels-1)), tile_coarse 32 level-1
+ * pixels. Takes effect from the next process(); no counterpart in the reference. */
+HMP_API hmp_status hmp_stitcher_set_tiles(hmp_stitcher* st, int tile_down, int tile_coarse);
+
 /* Per-kernel device time of process() calls made while timing is enabled, measured with CUDA
  * events recorded on the stream each kernel is launched on (the pyramid kernels run on the
  * stitcher's auxiliary stream). Index 0 = canvas_gather, 1 = pyr_down, 2 = pyr_coarse,
