@@ -35,6 +35,10 @@ struct PyrArgs {
   int tile;  // tile edge (level 0 for pyr_down, level 1 for pyr_coarse)
   float4* R1;  // level-1 reconstruction [batch][lh1][lw1] (levels >= 2)
   float4* Rl[kDevMaxLevels];  // Binomial5 filter: reconstruction R^l, l = 1..L-1, [batch][lh][lw]
+  // Level-0 pixels of each slot over its plane rect, [batch][P.h][P.w] RGBA8, written by pyr_down
+  // and read by pyr_fine (when use_p0; levels >= 2 with the box filter).
+  uint32_t* P0[kDevMaxImages];
+  int use_p0;
   CanvasDev C;
   int wx0, wy0, wx1, wy1;  // write rect, blend coordinates, end exclusive
   int cx_off, cy_off;      // canvas = blend + offset

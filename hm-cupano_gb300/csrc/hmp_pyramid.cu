@@ -117,6 +117,9 @@ __device__ __forceinline__ Store* level_of(const PyrArgs& a, int k, int l, int b
 // hold, so it is skipped entirely.
 template <int NMAX, typename Store, int TD>
 __global__ void __launch_bounds__(256) pyr_down_kernel(const __grid_constant__ PyrArgs a) {
+  // Only the three- and N-image kernels keep level 0 for pyr_fine; the two-image kernel is
+  // compiled without that code (it measured faster that way, running beside the canvas gather).
+  constexpr bool kKeepLevel0 = NMAX >= 3;
   constexpr int T1 = TD / 2, T2 = TD / 4, A2 = T2 * T2;
   extern __shared__ float4 sm[];
   const int n = a.n;
@@ -186,6 +189,26 @@ __global__ void __launch_bounds__(256) pyr_down_kernel(const __grid_constant__ P
   }
   cp_async_commit_wait_all();
   __syncthreads();
+  // Level 0 for pyr_fine: each slot's gathered pixels inside its plane rect, so that the level-0
+  // pass reads them back directly instead of repeating the table lookups and gathers.
+  if constexpr (kKeepLevel0) {
+#pragma unroll
+    for (int k = 0; k < NMAX; ++k) {
+      if (!active[k] || !a.use_p0) continue;
+      const PlaneDev& P = a.slot[k];
+      uint32_t* dst = a.P0[k] + (long long)b * P.w * P.h;
+      const uint32_t* pk = pix + k * TD * TD;
+      for (int r = warp; r < TD; r += 8) {
+        const int ry = Y0 + r - P.y0;
+        if ((unsigned)ry >= (unsigned)P.h) continue;
+#pragma unroll
+        for (int j = 0; j < TD / 32; ++j) {
+          const int x = X0 + 32 * j + lane, rx = x - P.x0;
+          if ((unsigned)rx < (unsigned)P.w) dst[(long long)ry * P.w + rx] = pk[r * TD + 32 * j + lane];
+        }
+      }
+    }
+  }
   // Levels 1 and 2: one item = one level-2 pixel of one slot = its four level-1 pixels, each the
   // alpha-aware mean of a 2x2 level-0 block (two 8-byte shared loads), summed in (0,0), (1,0),
   // (0,1), (1,1) order at both levels.
@@ -609,7 +632,7 @@ __device__ __forceinline__ float3 up_tile(const T* t, int i, bool ox, bool oy) {
 // source gathers, and waits for the tiles only after that. Per pixel: Lap = G^0 - up(G^1) of the
 // picked image (of every image where the weights are fractional), blend, add up(R^1), truncating
 // pack into the canvas.
-template <int RULE, int NMAX, typename Store>
+template <int RULE, int NMAX, typename Store, bool P0M>
 __global__ void __launch_bounds__(256) pyr_fine_kernel(const __grid_constant__ PyrArgs a) {
   extern __shared__ float4 fsm[];  // R^1 tile, then G^1 tiles of slots 0..n-1 (Store)
   const int n = RULE == kRuleNway ? a.n : NMAX;
@@ -666,16 +689,31 @@ __global__ void __launch_bounds__(256) pyr_fine_kernel(const __grid_constant__ P
       for (int k = 0; k < NMAX; ++k) {
         own[u][k] = 0xFF;
         ent[u][k] = 0xFFFFFFFFu;
-        if (live[u] && ((amask >> k) & 1u)) slot_lookup(a.slot[k], k, x, y, own[u][k], ent[u][k]);
+        if (P0M) {
+          // Level-0 pixel kept by pyr_down (zero outside the slot's plane): in ent.
+          const PlaneDev& P = a.slot[k];
+          const int rx = x - P.x0, ry = y - P.y0;
+          ent[u][k] = 0u;
+          if (live[u] && ((amask >> k) & 1u) && (unsigned)rx < (unsigned)P.w && (unsigned)ry < (unsigned)P.h)
+            ent[u][k] = __ldg(a.P0[k] + (long long)b * P.w * P.h + (long long)ry * P.w + rx);
+        } else if (live[u] && ((amask >> k) & 1u)) {
+          slot_lookup(a.slot[k], k, x, y, own[u][k], ent[u][k]);
+        }
       }
     }
     uchar4 src[QB][NMAX];
 #pragma unroll
     for (int u = 0; u < QB; ++u)
 #pragma unroll
-      for (int k = 0; k < NMAX; ++k)
-        src[u][k] = ((amask >> k) & 1u) ? slot_fetch<NMAX>(a, k, own[u][k], ent[u][k], b, opaque)
-                                        : make_uchar4(0, 0, 0, 0);
+      for (int k = 0; k < NMAX; ++k) {
+        if (P0M) {
+          const uint32_t v = ent[u][k];
+          src[u][k] = make_uchar4(v & 0xFF, (v >> 8) & 0xFF, (v >> 16) & 0xFF, v >> 24);
+        } else {
+          src[u][k] = ((amask >> k) & 1u) ? slot_fetch<NMAX>(a, k, own[u][k], ent[u][k], b, opaque)
+                                          : make_uchar4(0, 0, 0, 0);
+        }
+      }
     if (q0 == 0 && has1) {
       asm volatile("cp.async.wait_group 0;\n" ::: "memory");
       __syncthreads();
@@ -777,15 +815,23 @@ void coarse_dispatch(const PyrArgs& a, int rule, dim3 grid, size_t smem, cudaStr
     pyr_coarse_kernel<kRuleNway, 8, Store, T><<<grid, 256, smem, stream>>>(a);
 }
 
+template <typename Store, bool P0M>
+void fine_dispatch2(const PyrArgs& a, int rule, dim3 grid, size_t smem, cudaStream_t stream) {
+  if (rule == kRuleTwo)
+    pyr_fine_kernel<kRuleTwo, 2, Store, P0M><<<grid, 256, smem, stream>>>(a);
+  else if (rule == kRuleThree)
+    pyr_fine_kernel<kRuleThree, 3, Store, P0M><<<grid, 256, smem, stream>>>(a);
+  else
+    pyr_fine_kernel<kRuleNway, 8, Store, P0M><<<grid, 256, smem, stream>>>(a);
+}
+
 template <typename Store>
 void fine_dispatch(const PyrArgs& a, int rule, dim3 grid, cudaStream_t stream) {
   const size_t smem = a.levels > 1 ? size_t(kFineTA) * (sizeof(float4) + size_t(a.n) * sizeof(Store)) : 0;
-  if (rule == kRuleTwo)
-    pyr_fine_kernel<kRuleTwo, 2, Store><<<grid, 256, smem, stream>>>(a);
-  else if (rule == kRuleThree)
-    pyr_fine_kernel<kRuleThree, 3, Store><<<grid, 256, smem, stream>>>(a);
+  if (a.use_p0)
+    fine_dispatch2<Store, true>(a, rule, grid, smem, stream);
   else
-    pyr_fine_kernel<kRuleNway, 8, Store><<<grid, 256, smem, stream>>>(a);
+    fine_dispatch2<Store, false>(a, rule, grid, smem, stream);
 }
 
 }  // namespace

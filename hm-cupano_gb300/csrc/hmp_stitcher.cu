@@ -58,6 +58,8 @@ struct hmp_stitcher {
   float4* R1 = nullptr;
   bool b5 = false;  // Binomial5 filter with at least two levels
   float4* Rl[hmp::kDevMaxLevels]{};
+  uint32_t* P0[hmp::kDevMaxImages]{};  // level-0 pixels per slot over its plane rect (box filter)
+  bool use_p0 = false;
   cudaStream_t aux = nullptr;
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   double m0_bytes = 0;
@@ -182,6 +184,18 @@ struct hmp_stitcher {
         e = alloc(&r, size_t(B) * p.lw[1] * p.lh[1] * sizeof(float4));
         if (e != cudaSuccess) return cuda_status(e, "reconstruction buffer");
         R1 = static_cast<float4*>(r);
+      }
+      // With three or more images pyr_down keeps the level-0 pixels for pyr_fine (one load per slot
+      // instead of a table lookup and a gather); with two it measured slower (the extra writes
+      // lengthen pyr_down more than they shorten pyr_fine), so pyr_fine gathers again.
+      use_p0 = L > 1 && !b5 && n >= 3;
+      for (int k = 0; use_p0 && k < n; ++k) {
+        const hmp::PlaneDev& P = slot_planes[k];
+        if (P.w <= 0 || P.h <= 0) continue;
+        void* q = nullptr;
+        e = alloc(&q, size_t(B) * P.w * P.h * sizeof(uint32_t));
+        if (e != cudaSuccess) return cuda_status(e, "level-0 buffer");
+        P0[k] = static_cast<uint32_t*>(q);
       }
       for (int l = 1; b5 && l < L; ++l) {
         void* r = nullptr;
@@ -386,6 +400,8 @@ struct hmp_stitcher {
     a.wy1 = a.wy0 + p.write.h;
     a.cx_off = p.blend.x;
     a.cy_off = p.blend.y;
+    a.use_p0 = use_p0 ? 1 : 0;
+    for (int k = 0; k < p.n; ++k) a.P0[k] = P0[k];
     if (b5) {
       // Binomial5: the level-by-level chain (its time is reported under pyr_down).
       for (int l = 1; l < p.levels; ++l) a.Rl[l] = Rl[l];
