@@ -286,6 +286,184 @@ __global__ void __launch_bounds__(256) pyr_down_kernel(const __grid_constant__ P
   }
 }
 
+// Source pixel address of slot k (k and the owner known only at run time), as slot_src.
+__device__ __forceinline__ const uchar4* slot_src_dyn(const PyrArgs& a, int k, int o, uint32_t e, int b, bool opaque,
+                                                      uint32_t& fill) {
+  const int sx = int(e & 0xFFFFu), sy = int(e >> 16);
+  fill = 0u;
+  if (a.slot[k].owner == nullptr) o = k;
+  if (o >= kDevMaxImages) return nullptr;
+  if (sx < a.S.w[o] && sy < a.S.h[o])
+    return reinterpret_cast<const uchar4*>(reinterpret_cast<const char*>(a.S.ptr[o]) + b * a.S.bstride[o] +
+                                           (long long)sy * int(a.S.pitch[o])) + sx;
+  if (opaque && sx != 0xFFFF) fill = 0xFF000000u;
+  return nullptr;
+}
+
+// pyr_down for the N-way rule (up to eight slots). A tile of the N-image blend region overlaps
+// only one to three slots' planes, so instead of loops unrolled over all eight slots (whose code
+// and per-slot checks dominated: instruction-cache stalls) the tile's active slots form a run-time
+// list, and shared memory holds `a.slots_cap` slots (the most any tile has, from the planner).
+// Same steps and arithmetic as pyr_down_kernel; level 0 is kept for pyr_fine.
+template <typename Store, int TD>
+__global__ void __launch_bounds__(256) pyr_down_n_kernel(const __grid_constant__ PyrArgs a) {
+  constexpr int T1 = TD / 2, T2 = TD / 4, A2 = T2 * T2;
+  extern __shared__ float4 sm[];
+  const int n = a.n, cap = a.slots_cap;
+  uint32_t* pix = reinterpret_cast<uint32_t*>(sm);  // level 0: [cap][TD][TD]
+  float4* bufA = sm;                                // levels 3, 5: [cap][T1*T1], over level 0
+  float4* bufB = sm + cap * T1 * T1;                // levels 2, 4, 6: [cap][T2*T2]
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int b = blockIdx.z;
+  const int X0 = blockIdx.x * TD, Y0 = blockIdx.y * TD;
+  const bool opaque = a.opaque != 0;
+  const int L = a.levels;
+  const int lw0 = a.lw[0], lh0 = a.lh[0], lw1 = a.lw[1], lh1 = a.lh[1];
+  uint32_t list = 0;  // active slots, four bits each
+  int na = 0;
+  for (int k = 0; k < n; ++k) {
+    const PlaneDev& P = a.slot[k];
+    if (!(X0 >= P.x0 + P.w || Y0 >= P.y0 + P.h || X0 + TD <= P.x0 || Y0 + TD <= P.y0) && na < cap)
+      list |= uint32_t(k) << (4 * na++);
+  }
+#pragma unroll 1
+  for (int c = 0; c < na; ++c) {
+    const PlaneDev& P = a.slot[(list >> (4 * c)) & 15u];
+    uint32_t* pk = pix + c * TD * TD;
+    for (int r = warp; r < TD; r += 8) {
+      const int y = Y0 + r, ry = y - P.y0;
+#pragma unroll
+      for (int j = 0; j < TD / 32; ++j) {
+        const int x = X0 + 32 * j + lane, rx = x - P.x0;
+        uint32_t* d = pk + r * TD + 32 * j + lane;
+        if (x < lw0 && y < lh0 && (unsigned)rx < (unsigned)P.w && (unsigned)ry < (unsigned)P.h)
+          cp_async<4>(d, P.map + (long long)ry * P.map_pitch + rx);
+        else
+          *d = 0xFFFFFFFFu;
+      }
+    }
+  }
+  cp_async_commit_wait_all();
+#pragma unroll 1
+  for (int c = 0; c < na; ++c) {
+    const int k = (list >> (4 * c)) & 15u;
+    const PlaneDev& P = a.slot[k];
+    uint32_t* pk = pix + c * TD * TD;
+    for (int r = warp; r < TD; r += 8) {
+      const int y = Y0 + r, ry = y - P.y0;
+#pragma unroll
+      for (int j = 0; j < TD / 32; ++j) {
+        const int x = X0 + 32 * j + lane, rx = x - P.x0;
+        uint32_t* d = pk + r * TD + 32 * j + lane;
+        const uint32_t e = *d;
+        int o = k;
+        if (P.owner != nullptr)
+          o = (x < lw0 && y < lh0 && (unsigned)rx < (unsigned)P.w && (unsigned)ry < (unsigned)P.h)
+                  ? int(__ldg(P.owner + (long long)ry * P.owner_pitch + rx))
+                  : 0xFF;
+        uint32_t fill;
+        const uchar4* sp = slot_src_dyn(a, k, o, e, b, opaque, fill);
+        if (sp)
+          cp_async<4>(d, sp);
+        else
+          *d = fill;
+      }
+    }
+  }
+  cp_async_commit_wait_all();
+  __syncthreads();
+  if (a.use_p0) {
+#pragma unroll 1
+    for (int c = 0; c < na; ++c) {
+      const int k = (list >> (4 * c)) & 15u;
+      const PlaneDev& P = a.slot[k];
+      uint32_t* dst = a.P0[k] + (long long)b * P.w * P.h;
+      const uint32_t* pk = pix + c * TD * TD;
+      for (int r = warp; r < TD; r += 8) {
+        const int ry = Y0 + r - P.y0;
+        if ((unsigned)ry >= (unsigned)P.h) continue;
+#pragma unroll
+        for (int j = 0; j < TD / 32; ++j) {
+          const int x = X0 + 32 * j + lane, rx = x - P.x0;
+          if ((unsigned)rx < (unsigned)P.w) dst[(long long)ry * P.w + rx] = pk[r * TD + 32 * j + lane];
+        }
+      }
+    }
+  }
+  const bool has2 = L > 2;
+  const int lw2 = a.lw[has2 ? 2 : 1], lh2 = a.lh[has2 ? 2 : 1];
+#pragma unroll 1
+  for (int it = tid; it < na * A2; it += 256) {
+    const int c = it / A2, j = it - c * A2;
+    const int k = (list >> (4 * c)) & 15u;
+    const int tx2 = j % T2, ty2 = j / T2;
+    const int gx2 = (X0 >> 2) + tx2, gy2 = (Y0 >> 2) + ty2;
+    const uint32_t* pk = pix + c * TD * TD;
+    Store* G1 = static_cast<Store*>(a.G[k][1]) + (long long)b * lw1 * lh1;
+    DownAcc acc2;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int tx = 2 * tx2 + (q & 1), ty = 2 * ty2 + (q >> 1);
+      const int gx = (X0 >> 1) + tx, gy = (Y0 >> 1) + ty;
+      if (gx < lw1 && gy < lh1) {
+        const uint2 r0 = *reinterpret_cast<const uint2*>(pk + (2 * ty) * TD + 2 * tx);
+        const uint2 r1 = *reinterpret_cast<const uint2*>(pk + (2 * ty + 1) * TD + 2 * tx);
+        const bool xin = 2 * gx + 1 < lw0, yin = 2 * gy + 1 < lh0;
+        DownAcc acc;
+        acc.add(u32_to_f4(r0.x));
+        if (xin) acc.add(u32_to_f4(r0.y));
+        if (yin) acc.add(u32_to_f4(r1.x));
+        if (xin && yin) acc.add(u32_to_f4(r1.y));
+        const float4 v = acc.result();
+        store_level(G1 + (long long)gy * lw1 + gx, v);
+        acc2.add(v);
+      }
+    }
+    if (has2) {
+      float4 v2 = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (gx2 < lw2 && gy2 < lh2) {
+        v2 = acc2.result();
+        store_level(static_cast<Store*>(a.G[k][2]) + (long long)b * lw2 * lh2 + (long long)gy2 * lw2 + gx2, v2);
+      }
+      bufB[c * A2 + j] = v2;
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int l = 3; l < kL; ++l) {
+    if (l >= L) break;
+    const int Tp = TD >> (l - 1), Tn = TD >> l;
+    const int area = Tn * Tn;
+    const float4* src = (l & 1) ? bufB : bufA;
+    float4* dst = (l & 1) ? bufA : bufB;
+    const int sstride = (l & 1) ? T2 * T2 : T1 * T1;
+    const int dstride = (l & 1) ? T1 * T1 : T2 * T2;
+    const int lwl = a.lw[l], lhl = a.lh[l], lwp = a.lw[l - 1], lhp = a.lh[l - 1];
+#pragma unroll 1
+    for (int it = tid; it < na * area; it += 256) {
+      const int c = it / area, j = it - c * area;
+      const int k = (list >> (4 * c)) & 15u;
+      const int tx = j % Tn, ty = j / Tn;
+      const int gx = (X0 >> l) + tx, gy = (Y0 >> l) + ty;
+      float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (gx < lwl && gy < lhl) {
+        DownAcc acc;
+        const float4* sk = src + c * sstride;
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          const int dx = q & 1, dy = q >> 1;
+          if (2 * gx + dx < lwp && 2 * gy + dy < lhp) acc.add(sk[(2 * ty + dy) * Tp + 2 * tx + dx]);
+        }
+        v = acc.result();
+        Store* Gl = static_cast<Store*>(a.G[k][l]) + (long long)b * lwl * lhl;
+        store_level(Gl + (long long)gy * lwl + gx, v);
+      }
+      dst[c * dstride + j] = v;
+    }
+    __syncthreads();
+  }
+}
+
 // Alpha-aware bilinear upsample of a shared-memory region (origin ax, ay; row stride cw) of a
 // level of size lw x lh, sampled for high-res pixel (x, y): top-left aligned, gx = x/2, taps
 // floor and floor+1 clamped to the level, only taps with alpha != 0, renormalised
@@ -786,6 +964,7 @@ void set_down_attrs() {
   set_down_attr<2, Store, T>();
   set_down_attr<3, Store, T>();
   set_down_attr<8, Store, T>();
+  cudaFuncSetAttribute(pyr_down_n_kernel<Store, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
 }
 
 template <typename Store, int T>
@@ -801,6 +980,8 @@ void down_dispatch(const PyrArgs& a, dim3 grid, size_t smem, cudaStream_t stream
     pyr_down_kernel<2, Store, T><<<grid, 256, smem, stream>>>(a);
   else if (a.n == 3)
     pyr_down_kernel<3, Store, T><<<grid, 256, smem, stream>>>(a);
+  else if (a.slots_cap > 0)
+    pyr_down_n_kernel<Store, T><<<grid, 256, pyr_down_smem(a.slots_cap, T), stream>>>(a);
   else
     pyr_down_kernel<8, Store, T><<<grid, 256, smem, stream>>>(a);
 }

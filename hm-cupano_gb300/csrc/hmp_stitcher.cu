@@ -54,6 +54,7 @@ struct hmp_stitcher {
   const uint8_t* mask0 = nullptr;
   int mask0_pitch = 0;
   int tile_down = 0, tile_coarse = 0;
+  int down_cap = 0;  // N-way pyr_down: slots held in shared memory (the most any tile overlaps)
   size_t coarse_smem = 0;
   float4* R1 = nullptr;
   bool b5 = false;  // Binomial5 filter with at least two levels
@@ -126,6 +127,22 @@ struct hmp_stitcher {
     return cudaSuccess;
   }
 
+  // The most slot planes any td x td level-0 tile of the blend region overlaps.
+  int down_cap_for(int td) const {
+    const hmp::Plan& p = plan;
+    int best = 1;
+    for (int y0 = 0; y0 < p.lh[0]; y0 += td)
+      for (int x0 = 0; x0 < p.lw[0]; x0 += td) {
+        int c = 0;
+        for (int k = 0; k < p.n; ++k) {
+          const hmp::PlaneDev& P = slot_planes[k];
+          if (!(x0 >= P.x0 + P.w || y0 >= P.y0 + P.h || x0 + td <= P.x0 || y0 + td <= P.y0)) ++c;
+        }
+        best = std::max(best, c);
+      }
+    return best;
+  }
+
   hmp_status setup() {
     hmp::Plan& p = plan;
     cudaError_t e = cudaGetDevice(&device);
@@ -176,6 +193,18 @@ struct hmp_stitcher {
       // the per-tile shared memory calls for 32. Coarse tiles: 32 level-1 pixels (a multiple of
       // 2^(L-2) for every supported L); smaller ones multiply the per-CTA halo and walk.
       tile_down = std::max(n <= 3 ? 64 : 32, align);
+      if (n > 3) {
+        // The N-way pyr_down keeps only a tile's overlapping slots in shared memory; size it for
+        // the most any tile overlaps and prefer 64-pixel tiles while two CTAs still fit an SM.
+        const auto cap_for = [&](int td) { return down_cap_for(td); };
+        const int c64 = cap_for(64);
+        if (align <= 64 && hmp::pyr_down_smem(c64, 64) <= 113 * 1024) {
+          tile_down = 64;
+          down_cap = c64;
+        } else {
+          down_cap = cap_for(tile_down);
+        }
+      }
       tile_coarse = std::max(32, align / 2);
       coarse_smem = hmp::pyr_coarse_smem(n, p.mask_k, tile_coarse, L, p.storage);
       b5 = p.filter == HMP_FILTER_BINOMIAL5 && L > 1;
@@ -203,7 +232,7 @@ struct hmp_stitcher {
         if (e != cudaSuccess) return cuda_status(e, "reconstruction buffer");
         Rl[l] = static_cast<float4*>(r);
       }
-      if (hmp::pyr_down_smem(n, tile_down) > 227 * 1024)
+      if (hmp::pyr_down_smem(down_cap > 0 ? down_cap : n, tile_down) > 227 * 1024)
         return make_status(HMP_ERR_NOT_SUPPORTED, "pyramid tile does not fit in shared memory");
       if (coarse_smem > 227 * 1024)
         return make_status(HMP_ERR_NOT_SUPPORTED, "pyramid tile does not fit in shared memory");
@@ -412,6 +441,7 @@ struct hmp_stitcher {
     }
     if (p.levels > 1 && !b5) {
       a.tile = tile_down;
+      a.slots_cap = down_cap;
       const dim3 grid((p.lw[0] + tile_down - 1) / tile_down, (p.lh[0] + tile_down - 1) / tile_down, p.batch);
       tbegin(1, ps);
       e = hmp::launch_pyr_down(a, p.storage, grid, ps);
@@ -544,9 +574,11 @@ HMP_API hmp_status hmp_stitcher_set_tiles(hmp_stitcher* st, int tile_down, int t
     return make_status(HMP_ERR_INVALID_VALUE, "tile_down must be 32 or 64 and a multiple of 2^(levels-1)");
   if (tile_coarse != 32 || (tile_coarse * 2) % align != 0)
     return make_status(HMP_ERR_INVALID_VALUE, "tile_coarse must be 32");
-  if (hmp::pyr_down_smem(p.n, tile_down) > 227 * 1024)
+  const int cap = p.n > 3 ? st->down_cap_for(tile_down) : 0;
+  if (hmp::pyr_down_smem(cap > 0 ? cap : p.n, tile_down) > 227 * 1024)
     return make_status(HMP_ERR_NOT_SUPPORTED, "pyramid tile does not fit in shared memory");
   st->tile_down = tile_down;
+  st->down_cap = cap;
   st->tile_coarse = tile_coarse;
   st->coarse_smem = hmp::pyr_coarse_smem(p.n, p.mask_k, tile_coarse, p.levels, p.storage);
   return make_status(HMP_OK, "");
