@@ -762,6 +762,220 @@ __global__ void __launch_bounds__(256) pyr_coarse_kernel(const __grid_constant__
   }
 }
 
+// pyr_coarse for the N-way rule: the tile's active slots (those whose plane meets the footprint
+// of the regions read) form a run-time list, shared memory holds `a.coarse_cap` slots (the most
+// any tile has, from the planner), and level 1 reads only the alphas before the pick, then the
+// picked slot's pixel. Same arithmetic as pyr_coarse_kernel (inactive slots read as zero).
+template <typename Store, int T1>
+__global__ void __launch_bounds__(256) pyr_coarse_n_kernel(const __grid_constant__ PyrArgs a) {
+  constexpr int NMAX = kDevMaxImages;
+  extern __shared__ float4 sm[];
+  char* smb = reinterpret_cast<char*>(sm);
+  const int n = a.n, K = a.K, cap = a.coarse_cap;
+  const int b = blockIdx.z;
+  const int X1 = (a.tx0 + blockIdx.x) * T1, Y1 = (a.ty0 + blockIdx.y) * T1;
+  const int L = a.levels, c = L - 1;
+  const int tid = threadIdx.x;
+  const CoarseLayout lo = coarse_layout(cap, K, T1, L, int(sizeof(Store)));
+  int rax[kL], ray[kL], rbx[kL], rby[kL];
+  {
+    int ax = X1, ay = Y1, bx = min(X1 + T1, a.lw[1]), by = min(Y1 + T1, a.lh[1]);
+#pragma unroll
+    for (int l = 1; l < kL; ++l) {
+      if (l > 1 && l < L) {
+        ax >>= 1;
+        ay >>= 1;
+        bx = min(((bx - 1) >> 1) + 2, a.lw[l]);
+        by = min(((by - 1) >> 1) + 2, a.lh[l]);
+      }
+      rax[l] = ax;
+      ray[l] = ay;
+      rbx[l] = bx;
+      rby[l] = by;
+    }
+  }
+  uint32_t list = 0, cmap = 0xFFFFFFFFu;  // compact list (slot per nibble), slot -> compact index
+  int na = 0;
+  {
+    int fx0 = rax[1] << 1, fy0 = ray[1] << 1, fx1 = rbx[1] << 1, fy1 = rby[1] << 1;
+#pragma unroll
+    for (int l = 2; l < kL; ++l) {
+      if (l >= L) break;
+      fx0 = min(fx0, rax[l] << l);
+      fy0 = min(fy0, ray[l] << l);
+      fx1 = max(fx1, rbx[l] << l);
+      fy1 = max(fy1, rby[l] << l);
+    }
+    for (int k = 0; k < n; ++k) {
+      const PlaneDev& P = a.slot[k];
+      if (fx0 < P.x0 + P.w && P.x0 < fx1 && fy0 < P.y0 + P.h && P.y0 < fy1 && na < cap) {
+        list |= uint32_t(k) << (4 * na);
+        cmap = (cmap & ~(0xFu << (4 * k))) | (uint32_t(na) << (4 * k));
+        ++na;
+      }
+    }
+  }
+#pragma unroll
+  for (int l = 2; l < kL; ++l) {
+    if (l >= L) break;
+    const int CW = up_cw(T1, l - 1), CAP = CW * CW;
+    const int lax = rax[l], lay = ray[l], rw = rbx[l] - lax, rh = rby[l] - lay;
+    const int lw = a.lw[l], lh = a.lh[l];
+#pragma unroll 1
+    for (int ci = 0; ci < na; ++ci) {
+      const int k = (list >> (4 * ci)) & 15u;
+      const Store* Gl = static_cast<const Store*>(a.G[k][l]) + (long long)b * lw * lh;
+      Store* gl = reinterpret_cast<Store*>(smb + lo.g[l]) + ci * CAP;
+      for (int i = tid; i < CAP; i += 256) {
+        const int x = i % CW, y = i / CW;
+        if (x < rw && y < rh) cp_async<int(sizeof(Store))>(gl + i, Gl + (long long)(lay + y) * lw + (lax + x));
+      }
+    }
+    const float* ml = a.maskL[l];
+    float* mb = reinterpret_cast<float*>(smb + lo.m[l]);
+    for (int p = tid; p < CAP; p += 256) {
+      const int x = p % CW, y = p / CW;
+      if (x < rw && y < rh) {
+        const float* src = ml + ((long long)(lay + y) * lw + (lax + x)) * K;
+        for (int q = 0; q < K; ++q) cp_async<4>(mb + p * K + q, src + q);
+      }
+    }
+  }
+  cp_async_commit_wait_all();
+  __syncthreads();
+#pragma unroll
+  for (int l = kL - 1; l >= 2; --l) {
+    if (l > c) continue;
+    const int CW = up_cw(T1, l - 1), CAP = CW * CW;
+    const int QW = (CW + 1) / 2, QC = QW * QW;
+    const int lax = rax[l], lay = ray[l], rw = rbx[l] - lax, rh = rby[l] - lay;
+    const Store* gcur = reinterpret_cast<const Store*>(smb + lo.g[l]);
+    float4* rcur = reinterpret_cast<float4*>(smb + lo.r[l]);
+    const float* mb = reinterpret_cast<const float*>(smb + lo.m[l]);
+    const bool has_next = l < c;
+    const int nl = l + 1 < kL ? l + 1 : l;
+    const int CWN = up_cw(T1, nl - 1), CAPN = CWN * CWN;
+    const int nax = rax[nl], nay = ray[nl];
+    const int lwn = a.lw[nl], lhn = a.lh[nl];
+    const Store* gnext = reinterpret_cast<const Store*>(smb + lo.g[nl]);
+    const float4* rnext = reinterpret_cast<const float4*>(smb + lo.r[nl]);
+    for (int t = tid; t < 4 * QC; t += 256) {
+      const int cls = t / QC, j = t - cls * QC;
+      const int x = 2 * (j % QW) + (cls & 1), y = 2 * (j / QW) + (cls >> 1);
+      if (x >= rw || y >= rh) continue;
+      const int i = y * CW + x;
+      const int px = lax + x, py = lay + y;
+      float al[NMAX];
+#pragma unroll
+      for (int k = 0; k < NMAX; ++k) {
+        const uint32_t ci = (cmap >> (4 * k)) & 15u;
+        al[k] = (k < n && ci < 15u) ? load_level(gcur + ci * CAP + i).w : 0.f;
+      }
+      const int pk = blend_pick<kRuleNway, NMAX>(n, al, mb + i * K);
+      float4 r = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (pk >= 0) {
+        const int ci = (cmap >> (4 * pk)) & 15u;  // picked: alpha > 0, so active
+        float4 g = load_level(gcur + ci * CAP + i);
+        if (has_next) {
+          const float3 up = up_alpha(gnext + ci * CAPN, CWN, nax, nay, lwn, lhn, px, py);
+          g.x = g.x - up.x;
+          g.y = g.y - up.y;
+          g.z = g.z - up.z;
+        }
+        r = make_float4(g.x, g.y, g.z, blend_alpha<kRuleNway, NMAX>(al, pk));
+      } else if (pk == kPickAll) {
+        float4 lap[NMAX];
+#pragma unroll
+        for (int k = 0; k < NMAX; ++k) {
+          const uint32_t ci = (cmap >> (4 * k)) & 15u;
+          lap[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+          if (k < n && ci < 15u) {
+            float4 g = load_level(gcur + ci * CAP + i);
+            if (has_next) {
+              const float3 up = up_alpha(gnext + ci * CAPN, CWN, nax, nay, lwn, lhn, px, py);
+              g.x = g.x - up.x;
+              g.y = g.y - up.y;
+              g.z = g.z - up.z;
+            }
+            lap[k] = g;
+          }
+        }
+        r = blend_level<kRuleNway, NMAX>(n, lap, mb + i * K);
+      }
+      if (has_next) {
+        const float3 up = up_alpha(rnext, CWN, nax, nay, lwn, lhn, px, py);
+        r.x = up.x + r.x;
+        r.y = up.y + r.y;
+        r.z = up.z + r.z;
+      }
+      rcur[i] = r;
+    }
+    __syncthreads();
+  }
+  constexpr int HALF = T1 / 2, CLS = HALF * HALF, PER = (T1 * T1 + 255) / 256;
+  const int lw1 = a.lw[1], lh1 = a.lh[1];
+  const bool has2 = c >= 2;
+  const int CW2 = up_cw(T1, 1), CAP2 = CW2 * CW2;
+  const int nax = rax[2], nay = ray[2];
+  const int lw2 = a.lw[2 < kL ? 2 : 1], lh2 = a.lh[2 < kL ? 2 : 1];
+  const Store* g2 = reinterpret_cast<const Store*>(smb + lo.g[2]);
+  const float4* r2 = reinterpret_cast<const float4*>(smb + lo.r[2]);
+  float4* R1 = a.R1 + (long long)b * lw1 * lh1;
+#pragma unroll 1
+  for (int p = 0; p < PER; ++p) {
+    const int i = p * 256 + tid;
+    const int lx = 2 * ((i % CLS) % HALF) + ((i / CLS) & 1), ly = 2 * ((i % CLS) / HALF) + ((i / CLS) >> 1);
+    const int px = X1 + lx, py = Y1 + ly;
+    if (px >= lw1 || py >= lh1) continue;
+    const long long o1 = (long long)py * lw1 + px;
+    float m[NMAX], al[NMAX];
+#pragma unroll
+    for (int q = 0; q < NMAX; ++q) m[q] = q < K ? __ldg(a.maskL[1] + o1 * K + q) : 0.f;
+#pragma unroll
+    for (int k = 0; k < NMAX; ++k) {
+      const uint32_t ci = (cmap >> (4 * k)) & 15u;
+      al[k] = (k < n && ci < 15u) ? ldg_level(static_cast<const Store*>(a.G[k][1]) + (long long)b * lw1 * lh1 + o1).w : 0.f;
+    }
+    const int pk = blend_pick<kRuleNway, NMAX>(n, al, m);
+    float4 r = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (pk >= 0) {
+      const int ci = (cmap >> (4 * pk)) & 15u;
+      float4 g = ldg_level(static_cast<const Store*>(a.G[pk][1]) + (long long)b * lw1 * lh1 + o1);
+      if (has2) {
+        const float3 up = up_alpha(g2 + ci * CAP2, CW2, nax, nay, lw2, lh2, px, py);
+        g.x = g.x - up.x;
+        g.y = g.y - up.y;
+        g.z = g.z - up.z;
+      }
+      r = make_float4(g.x, g.y, g.z, blend_alpha<kRuleNway, NMAX>(al, pk));
+    } else if (pk == kPickAll) {
+      float4 g1[NMAX];
+#pragma unroll
+      for (int k = 0; k < NMAX; ++k) {
+        const uint32_t ci = (cmap >> (4 * k)) & 15u;
+        g1[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (k < n && ci < 15u) {
+          g1[k] = ldg_level(static_cast<const Store*>(a.G[k][1]) + (long long)b * lw1 * lh1 + o1);
+          if (has2) {
+            const float3 up = up_alpha(g2 + ci * CAP2, CW2, nax, nay, lw2, lh2, px, py);
+            g1[k].x = g1[k].x - up.x;
+            g1[k].y = g1[k].y - up.y;
+            g1[k].z = g1[k].z - up.z;
+          }
+        }
+      }
+      r = blend_level<kRuleNway, NMAX>(n, g1, m);
+    }
+    if (has2) {
+      const float3 up = up_alpha(r2, CW2, nax, nay, lw2, lh2, px, py);
+      r.x = up.x + r.x;
+      r.y = up.y + r.y;
+      r.z = up.z + r.z;
+    }
+    R1[o1] = r;
+  }
+}
+
 // Level-1 tile of a pyr_fine CTA: the 32 x 8 level-1 pixels under its 64 x 16 level-0 block
 // plus the +1 column and row the bilinear upsample reads, with coordinates clamped to the level
 // (so the tile holds the clamped taps and the upsample needs no bounds checks).
@@ -972,6 +1186,7 @@ void set_coarse_attrs() {
   set_up_attr<kRuleTwo, 2, Store, T>();
   set_up_attr<kRuleThree, 3, Store, T>();
   set_up_attr<kRuleNway, 8, Store, T>();
+  cudaFuncSetAttribute(pyr_coarse_n_kernel<Store, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
 }
 
 template <typename Store, int T>
@@ -992,6 +1207,8 @@ void coarse_dispatch(const PyrArgs& a, int rule, dim3 grid, size_t smem, cudaStr
     pyr_coarse_kernel<kRuleTwo, 2, Store, T><<<grid, 256, smem, stream>>>(a);
   else if (rule == kRuleThree)
     pyr_coarse_kernel<kRuleThree, 3, Store, T><<<grid, 256, smem, stream>>>(a);
+  else if (a.coarse_cap > 0)
+    pyr_coarse_n_kernel<Store, T><<<grid, 256, smem, stream>>>(a);
   else
     pyr_coarse_kernel<kRuleNway, 8, Store, T><<<grid, 256, smem, stream>>>(a);
 }

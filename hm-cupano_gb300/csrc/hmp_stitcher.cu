@@ -55,6 +55,7 @@ struct hmp_stitcher {
   int mask0_pitch = 0;
   int tile_down = 0, tile_coarse = 0;
   int down_cap = 0;  // N-way pyr_down: slots held in shared memory (the most any tile overlaps)
+  int coarse_cap = 0;  // N-way pyr_coarse: likewise per coarse tile
   size_t coarse_smem = 0;
   float4* R1 = nullptr;
   bool b5 = false;  // Binomial5 filter with at least two levels
@@ -125,6 +126,36 @@ struct hmp_stitcher {
       d.owner_pitch = op;
     }
     return cudaSuccess;
+  }
+
+  // The most slot planes the footprint of any coarse tile (level-1 edge t1, its regions of levels
+  // 2..L-1 with their halos, in level-0 pixels) overlaps; the same footprint rule as the kernel.
+  int coarse_cap_for(int t1) const {
+    const hmp::Plan& p = plan;
+    const int L = p.levels;
+    int best = 1;
+    for (int Y1 = 0; Y1 < p.lh[1]; Y1 += t1)
+      for (int X1 = 0; X1 < p.lw[1]; X1 += t1) {
+        int ax = X1, ay = Y1, bx = std::min(X1 + t1, p.lw[1]), by = std::min(Y1 + t1, p.lh[1]);
+        int fx0 = ax << 1, fy0 = ay << 1, fx1 = bx << 1, fy1 = by << 1;
+        for (int l = 2; l < L; ++l) {
+          ax >>= 1;
+          ay >>= 1;
+          bx = std::min(((bx - 1) >> 1) + 2, p.lw[l]);
+          by = std::min(((by - 1) >> 1) + 2, p.lh[l]);
+          fx0 = std::min(fx0, ax << l);
+          fy0 = std::min(fy0, ay << l);
+          fx1 = std::max(fx1, bx << l);
+          fy1 = std::max(fy1, by << l);
+        }
+        int c = 0;
+        for (int k = 0; k < p.n; ++k) {
+          const hmp::PlaneDev& P = slot_planes[k];
+          if (fx0 < P.x0 + P.w && P.x0 < fx1 && fy0 < P.y0 + P.h && P.y0 < fy1) ++c;
+        }
+        best = std::max(best, c);
+      }
+    return best;
   }
 
   // The most slot planes any td x td level-0 tile of the blend region overlaps.
@@ -206,7 +237,8 @@ struct hmp_stitcher {
         }
       }
       tile_coarse = std::max(32, align / 2);
-      coarse_smem = hmp::pyr_coarse_smem(n, p.mask_k, tile_coarse, L, p.storage);
+      coarse_cap = (n > 3 && L > 2) ? coarse_cap_for(tile_coarse) : 0;
+      coarse_smem = hmp::pyr_coarse_smem(coarse_cap > 0 ? coarse_cap : n, p.mask_k, tile_coarse, L, p.storage);
       b5 = p.filter == HMP_FILTER_BINOMIAL5 && L > 1;
       if (L > 1 && !b5) {
         void* r = nullptr;
@@ -454,6 +486,7 @@ struct hmp_stitcher {
       const int x1lo = a.wx0 >> 1, x1hi = std::min(((a.wx1 - 1) >> 1) + 2, p.lw[1]);
       const int y1lo = a.wy0 >> 1, y1hi = std::min(((a.wy1 - 1) >> 1) + 2, p.lh[1]);
       a.tile = tile_coarse;
+      a.coarse_cap = coarse_cap;
       a.tx0 = x1lo / tile_coarse;
       a.ty0 = y1lo / tile_coarse;
       const dim3 cgrid((x1hi + tile_coarse - 1) / tile_coarse - a.tx0, (y1hi + tile_coarse - 1) / tile_coarse - a.ty0,
