@@ -130,6 +130,15 @@ __device__ __forceinline__ uchar4 plane_pixel(const SrcSet& S, const PlaneDev& P
   return out;
 }
 
+// Canvas-plane entries resolved for the frames being stitched (resolve_plane_kernel): a pixel
+// offset within the owner's frame (sy * pitch / 4 + sx), or one of two fills -- the reference's
+// remap rule (src/cuda/cudaRemap.cu:60-123): an entry outside the source reads zero, with alpha
+// 255 under the soft-seam ("opaque") rule unless its x is the 65535 sentinel.
+constexpr uint32_t kOffZero = 0xFFFFFFFFu;    // (0, 0, 0, 0)
+constexpr uint32_t kOffOpaque = 0xFFFFFFFEu;  // (0, 0, 0, 255)
+
+__device__ __forceinline__ uint32_t fill_of(uint32_t off) { return off == kOffOpaque ? 0xFF000000u : 0u; }
+
 // Truncating float -> uint8 pack (src/cuda/cudaUtils.cuh:18-28): v <= 0 -> 0, v >= 255 -> 255,
 // otherwise truncation toward zero.
 __device__ __forceinline__ unsigned char pack_u8(float v) {

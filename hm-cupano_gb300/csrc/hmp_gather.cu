@@ -5,7 +5,9 @@
 // seam src/cuda/cudaFusedKernels3.cu:124-217; the N-image fused hard seam cudaRemap.cu:251-294).
 // One pass over the canvas: each warp owns a 256-pixel row segment, copies its owner bytes and
 // packed table entries into shared memory, copies the source pixels they select (cp.async, for
-// every frame of the batch) and stores them in full lines. Pixels with no owner get zero, so no memset is needed.
+// every frame of the batch) and stores them in full lines. Pixels with no owner get zero, so no
+// memset is needed. Table entries are resolved offsets (resolve_plane_kernel below), so a pixel
+// costs one compare and one multiply-add besides its copies.
 // HBM-bound: 1 + 4 + 4 + 4 = 13 bytes per canvas pixel.
 #include <algorithm>
 
@@ -31,16 +33,13 @@ __device__ __forceinline__ void cp_async8(void* dst, const void* src) {
   asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(smem_addr(dst)), "l"(src));
 }
 
-// Source pixel of canvas pixel with owner o and entry e: a 4-byte copy into *dst, or the fill
-// value (zero; alpha 255 under the soft-seam rule for an out-of-range entry that is not the
-// 65535 sentinel).
-__device__ __forceinline__ void gather_one(uint32_t* dst, const char* base, int pitch, int sw, int sh, uint32_t e,
-                                           bool opaque) {
-  const int sx = int(e & 0xFFFFu), sy = int(e >> 16);
-  if (sx < sw && sy < sh)
-    cp_async4(dst, reinterpret_cast<const uchar4*>(base + (long long)sy * pitch) + sx);
+// Source pixel of a canvas pixel with resolved entry off in a frame at base: a 4-byte copy into
+// *dst, or its fill.
+__device__ __forceinline__ void gather_one(uint32_t* dst, const uchar4* base, uint32_t off) {
+  if (off < kOffOpaque)
+    cp_async4(dst, base + off);
   else
-    *dst = (opaque && sx != 0xFFFF) ? 0xFF000000u : 0u;
+    *dst = fill_of(off);
 }
 
 // Each warp owns a 256-pixel segment of one canvas row; lane l handles the pixel pairs
@@ -87,7 +86,6 @@ __global__ void __launch_bounds__(256, 6) canvas_gather_kernel(const __grid_cons
   cp_async_commit();
   cp_async_wait<0>();
   __syncwarp();
-  const bool opaque = a.opaque != 0;
   // Segments with one owner (all but those a seam crosses) resolve the source image once per
   // warp instead of once per pixel.
   int uo = a.P.default_owner;
@@ -108,13 +106,13 @@ __global__ void __launch_bounds__(256, 6) canvas_gather_kernel(const __grid_cons
   for (int b = 0; b < a.batch; ++b) {
     uint32_t* pxw = reinterpret_cast<uint32_t*>(px);
     if (uniform) {
-      const char* base = reinterpret_cast<const char*>(a.S.ptr[uo]) + b * a.S.bstride[uo];
-      const int pitch = int(a.S.pitch[uo]), sw = a.S.w[uo], sh = a.S.h[uo];
+      const uchar4* base =
+          reinterpret_cast<const uchar4*>(reinterpret_cast<const char*>(a.S.ptr[uo]) + b * a.S.bstride[uo]);
 #pragma unroll
       for (int j = 0; j < PJ; ++j) {
         const uint2 e = ent[32 * j + lane];
-        gather_one(pxw + 2 * (32 * j + lane), base, pitch, sw, sh, e.x, opaque);
-        gather_one(pxw + 2 * (32 * j + lane) + 1, base, pitch, sw, sh, e.y, opaque);
+        gather_one(pxw + 2 * (32 * j + lane), base, e.x);
+        gather_one(pxw + 2 * (32 * j + lane) + 1, base, e.y);
       }
     } else {
 #pragma unroll
@@ -125,12 +123,11 @@ __global__ void __launch_bounds__(256, 6) canvas_gather_kernel(const __grid_cons
           const int x = x0 + 64 * j + 2 * lane + h;
           const int o = orow ? (x < W ? int(own[64 * j + 2 * lane + h]) : 0xFF) : a.P.default_owner;
           uint32_t* d = pxw + 2 * (32 * j + lane) + h;
-          if (o < kDevMaxImages) {
-            const char* base = reinterpret_cast<const char*>(a.S.ptr[o]) + b * a.S.bstride[o];
-            gather_one(d, base, int(a.S.pitch[o]), a.S.w[o], a.S.h[o], h ? e2.y : e2.x, opaque);
-          } else {
-            *d = 0u;
-          }
+          const uint32_t e = h ? e2.y : e2.x;
+          if (o < kDevMaxImages && e < kOffOpaque)
+            cp_async4(d, reinterpret_cast<const uchar4*>(reinterpret_cast<const char*>(a.S.ptr[o]) + b * a.S.bstride[o]) + e);
+          else
+            *d = fill_of(e);
         }
       }
     }
@@ -155,7 +152,35 @@ __global__ void __launch_bounds__(256, 6) canvas_gather_kernel(const __grid_cons
   }
 }
 
+// Resolves one plane's packed entries (raw.map) into offsets (res, same layout) for the frames'
+// geometry: owner o < n and (sx, sy) inside image o give sy * pitch / 4 + sx; anything else
+// kOffZero, or kOffOpaque under the soft-seam rule when the owner is valid and sx is not the 65535
+// sentinel.
+__global__ void resolve_plane_kernel(const __grid_constant__ PlaneDev raw, uint32_t* res, const __grid_constant__ SrcSet S,
+                                     int n, int opaque) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y;
+  if (x >= raw.w || y >= raw.h) return;
+  const int o = raw.owner ? int(raw.owner[(long long)y * raw.owner_pitch + x]) : raw.default_owner;
+  const uint32_t e = raw.map[(long long)y * raw.map_pitch + x];
+  const int sx = int(e & 0xFFFFu), sy = int(e >> 16);
+  uint32_t r = kOffZero;
+  if (o < n) {
+    if (sx < S.w[o] && sy < S.h[o])
+      r = uint32_t(sy) * uint32_t(S.pitch[o] / 4) + uint32_t(sx);
+    else if (opaque && sx != 0xFFFF)
+      r = kOffOpaque;
+  }
+  res[(long long)y * raw.map_pitch + x] = r;
+}
+
 }  // namespace
+
+cudaError_t launch_resolve_plane(const PlaneDev& raw, uint32_t* res, const SrcSet& S, int n, bool opaque,
+                                 cudaStream_t stream) {
+  if (raw.w <= 0 || raw.h <= 0) return cudaSuccess;
+  resolve_plane_kernel<<<dim3((raw.w + 255) / 256, raw.h), 256, 0, stream>>>(raw, res, S, n, opaque ? 1 : 0);
+  return cudaGetLastError();
+}
 
 cudaError_t launch_canvas_gather(const GatherArgs& a, cudaStream_t stream) {
   const dim3 grid((a.C.w + 255) / 256, (a.C.h + 7) / 8);

@@ -10,11 +10,10 @@ namespace hmp {
 // Canvas gather: every canvas pixel outside `skip` takes its gather-plane pixel.
 struct GatherArgs {
   SrcSet S;
-  PlaneDev P;  // canvas plane, rect = whole canvas
+  PlaneDev P;  // canvas plane (entries resolved to offsets), rect = whole canvas
   CanvasDev C;
   int batch;
   int skip_x0, skip_y0, skip_x1, skip_y1;  // pixels written by the pyramid (end exclusive)
-  int opaque;
   int n_owners;  // images the plane can select (owners are < n_owners)
 };
 
@@ -49,6 +48,11 @@ struct PyrArgs {
 
 // One-time attribute setup (dynamic shared memory limits). Call before capture.
 cudaError_t kernels_init();
+
+// Resolves a plane's packed entries (raw.map) into offsets for the frames S (res: raw's layout).
+// opaque: the soft-seam rule for entries outside their source.
+cudaError_t launch_resolve_plane(const PlaneDev& raw, uint32_t* res, const SrcSet& S, int n, bool opaque,
+                                 cudaStream_t stream);
 
 cudaError_t launch_canvas_gather(const GatherArgs& a, cudaStream_t stream);
 

@@ -1,8 +1,10 @@
 // hmp_stitcher.cu -- stitcher object and the C ABI (include/hmpano.h).
 //
 // Construction plans the configuration on the host (hmp_plan.cpp), uploads the gather planes and
-// the mask pyramid, and allocates the pyramid levels. process() then launches at most three
-// kernels and allocates nothing:
+// the mask pyramid, and allocates the pyramid levels. The first process() -- and any call whose
+// frames differ in size or pitch from the previous call's -- resolves the canvas plane's packed
+// entries into pixel offsets for those frames (resolve_plane_kernel). process() then launches at
+// most four kernels and allocates nothing:
 //   aux stream (high priority) : pyr_down (Gaussian levels), pyr_coarse (reconstruction down to
 //                                level 1), pyr_fine (level 0: blend + reconstruct + pack of the
 //                                write rect), forked from and joined back to the caller stream
@@ -47,7 +49,12 @@ struct hmp_stitcher {
   int device = -1;
   std::vector<void*> allocations;
   size_t device_bytes = 0;
-  hmp::PlaneDev canvas_plane{};
+  // Canvas plane as the gather reads it (entries resolved to offsets for the current frames'
+  // geometry) and with the planned packed entries it is resolved from.
+  hmp::PlaneDev canvas_plane{}, canvas_raw{};
+  bool resolved = false;  // canvas_plane holds offsets for the geometry below
+  int geo_w[hmp::kDevMaxImages]{}, geo_h[hmp::kDevMaxImages]{};
+  long long geo_pitch[hmp::kDevMaxImages]{};
   hmp::PlaneDev slot_planes[hmp::kDevMaxImages]{};
   void* G[hmp::kDevMaxImages][hmp::kDevMaxLevels]{};
   const float* maskL[hmp::kDevMaxLevels]{};
@@ -183,6 +190,13 @@ struct hmp_stitcher {
     if (p.canvas_plane_used) {
       e = upload_plane(p.canvas, canvas_plane);
       if (e != cudaSuccess) return cuda_status(e, "canvas plane upload");
+      canvas_raw = canvas_plane;
+      if (canvas_plane.w > 0) {
+        void* r = nullptr;
+        e = alloc(&r, size_t(canvas_plane.map_pitch) * 4 * canvas_plane.h);
+        if (e != cudaSuccess) return cuda_status(e, "canvas plane allocation");
+        canvas_plane.map = static_cast<const uint32_t*>(r);
+      }
     }
     launches = p.canvas_plane_used ? 1 : 0;
     if (p.levels > 0) {
@@ -388,8 +402,11 @@ struct hmp_stitcher {
     for (int i = 0; i < n_inputs; ++i) {
       const hmp_image& im = inputs[i];
       if (!im.data) return make_status(HMP_ERR_INVALID_DEVICE_POINTER, "input image is null");
-      if (im.width <= 0 || im.height <= 0 || im.pitch < size_t(im.width) * 4 || im.pitch > size_t(INT_MAX))
+      if (im.width <= 0 || im.height <= 0 || im.pitch < size_t(im.width) * 4 || im.pitch > size_t(INT_MAX) ||
+          im.pitch % 4 != 0)
         return make_status(HMP_ERR_INVALID_VALUE, "input image has an invalid size or pitch");
+      if (size_t(im.height) * (im.pitch / 4) >= size_t(hmp::kOffOpaque))
+        return make_status(HMP_ERR_INVALID_VALUE, "input frame is larger than 4G pixels");
       if (im.width >= 65535 || im.height >= 65535)
         return make_status(HMP_ERR_INVALID_VALUE, "input images must be smaller than 65535 pixels per side");
     }
@@ -398,6 +415,24 @@ struct hmp_stitcher {
     if (dev != device) return make_status(HMP_ERR_INVALID_VALUE, "process() called on another device");
 
     const hmp::SrcSet S = sources(inputs);
+    if (p.canvas_plane_used) {
+      // The gather reads the canvas plane as offsets into these frames: resolve it for their
+      // geometry on the first call and whenever a size or pitch changes.
+      bool same = resolved;
+      for (int i = 0; i < p.n; ++i)
+        same = same && S.w[i] == geo_w[i] && S.h[i] == geo_h[i] && S.pitch[i] == geo_pitch[i];
+      if (!same) {
+        const cudaError_t re = hmp::launch_resolve_plane(canvas_raw, const_cast<uint32_t*>(canvas_plane.map), S, p.n,
+                                                         p.canvas_opaque, s);
+        if (re != cudaSuccess) return cuda_status(re, "canvas plane resolve launch");
+        for (int i = 0; i < p.n; ++i) {
+          geo_w[i] = S.w[i];
+          geo_h[i] = S.h[i];
+          geo_pitch[i] = S.pitch[i];
+        }
+        resolved = true;
+      }
+    }
     hmp::CanvasDev C;
     C.ptr = static_cast<uchar4*>(canvas->data);
     C.pitch = (long long)canvas->pitch;
@@ -411,7 +446,6 @@ struct hmp_stitcher {
       ga.P = canvas_plane;
       ga.C = C;
       ga.batch = p.batch;
-      ga.opaque = p.canvas_opaque ? 1 : 0;
       ga.n_owners = p.n;
       if (p.levels > 0) {
         ga.skip_x0 = p.write.x;
