@@ -395,9 +395,10 @@ def main() -> None:
     per_launch_ms = tot / max(cnt, 1)
     wr = info["write_rect"]
     canvas_px = W * H
-    # 4 table + 1 owner bytes once per call, 4 source + 4 canvas bytes per frame of the batch.
+    # 4 table bytes once per call (the entry carries the owner), 4 source + 4 canvas bytes per
+    # frame of the batch.
     gather_px = (canvas_px - wr[2] * wr[3]) if info["levels"] else canvas_px
-    gather_bytes = gather_px * (5.0 + 8.0 * B)
+    gather_bytes = gather_px * (4.0 + 8.0 * B)
     dom_bytes = {"canvas_gather": gather_bytes}.get(dom)
     achieved = dom_bytes / (per_launch_ms / 1e3) / 1e9 if dom_bytes else None
     traffic = None

@@ -130,12 +130,15 @@ __device__ __forceinline__ uchar4 plane_pixel(const SrcSet& S, const PlaneDev& P
   return out;
 }
 
-// Canvas-plane entries resolved for the frames being stitched (resolve_plane_kernel): a pixel
-// offset within the owner's frame (sy * pitch / 4 + sx), or one of two fills -- the reference's
-// remap rule (src/cuda/cudaRemap.cu:60-123): an entry outside the source reads zero, with alpha
-// 255 under the soft-seam ("opaque") rule unless its x is the 65535 sentinel.
+// Canvas-plane entries resolved for the frames being stitched (resolve_plane_kernel): the owner
+// and a pixel offset within the owner's frame, owner << 29 | (sy * pitch / 4 + sx), or one of two
+// fills -- the reference's remap rule (src/cuda/cudaRemap.cu:60-123): an entry outside the source
+// reads zero, with alpha 255 under the soft-seam ("opaque") rule unless its x is the 65535
+// sentinel.
 constexpr uint32_t kOffZero = 0xFFFFFFFFu;    // (0, 0, 0, 0)
 constexpr uint32_t kOffOpaque = 0xFFFFFFFEu;  // (0, 0, 0, 255)
+constexpr int kOwnerShift = 29;
+constexpr uint32_t kOffMask = (1u << kOwnerShift) - 1u;  // frames hold fewer than kOffMask - 1 pixels
 
 __device__ __forceinline__ uint32_t fill_of(uint32_t off) { return off == kOffOpaque ? 0xFF000000u : 0u; }
 

@@ -33,13 +33,13 @@ __device__ __forceinline__ void cp_async8(void* dst, const void* src) {
   asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(smem_addr(dst)), "l"(src));
 }
 
-// Source pixel of a canvas pixel with resolved entry off in a frame at base: a 4-byte copy into
-// *dst, or its fill.
-__device__ __forceinline__ void gather_one(uint32_t* dst, const uchar4* base, uint32_t off) {
-  if (off < kOffOpaque)
-    cp_async4(dst, base + off);
+// Source pixel of a canvas pixel with resolved entry e in the frame at base (the entry's owner):
+// a 4-byte copy into *dst, or its fill.
+__device__ __forceinline__ void gather_one(uint32_t* dst, const uchar4* base, uint32_t e) {
+  if (e < kOffOpaque)
+    cp_async4(dst, base + (e & kOffMask));
   else
-    *dst = fill_of(off);
+    *dst = fill_of(e);
 }
 
 // Each warp owns a 256-pixel segment of one canvas row; lane l handles the pixel pairs
@@ -48,13 +48,13 @@ __device__ __forceinline__ void gather_one(uint32_t* dst, const uchar4* base, ui
 // neighbouring canvas pixels land in the same few source lines, and the canvas stores are
 // 8-byte streaming stores of full lines. All loads are cp.async copies into shared memory laid
 // out [pixel step][lane] (conflict-free), so they need no destination registers and stay in
-// flight together: table entries and owners first, then one 4-byte copy per source pixel and
-// frame. Each lane reads back only what it copied itself (the owner bytes of a lane's pixels
-// come from other lanes' 4-byte copies, hence a warp sync).
+// flight together: table entries first, then one 4-byte copy per source pixel and frame. Each
+// lane reads back only what it copied itself. Entries carry their owner (owner << 29 | offset),
+// so no owner plane is read; a segment whose entries share one owner (all but those a seam
+// crosses) resolves the owner's frame once per warp.
 __global__ void __launch_bounds__(256, 6) canvas_gather_kernel(const __grid_constant__ GatherArgs a) {
   constexpr int PJ = 4;  // 64-pixel steps per segment
   __shared__ __align__(16) uint2 s_ent[8][PJ][32];
-  __shared__ __align__(16) uint8_t s_own[8][64 * PJ];
   __shared__ __align__(16) uint2 s_px[8][PJ][32];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int x0 = blockIdx.x * (64 * PJ);
@@ -63,10 +63,8 @@ __global__ void __launch_bounds__(256, 6) canvas_gather_kernel(const __grid_cons
   if (y >= H) return;
   const bool row_skip = y >= a.skip_y0 && y < a.skip_y1;
   if (row_skip && x0 >= a.skip_x0 && x0 + 64 * PJ <= a.skip_x1) return;
-  const uint8_t* orow = a.P.owner ? a.P.owner + (long long)y * a.P.owner_pitch : nullptr;
   const uint32_t* mrow = a.P.map + (long long)y * a.P.map_pitch;
   uint2* ent = &s_ent[w][0][0];
-  uint8_t* own = s_own[w];
   uint2* px = &s_px[w][0][0];
 #pragma unroll
   for (int j = 0; j < PJ; ++j) {
@@ -74,33 +72,22 @@ __global__ void __launch_bounds__(256, 6) canvas_gather_kernel(const __grid_cons
     if (x + 1 < W)
       cp_async8(ent + 32 * j + lane, mrow + x);  // map rows: 8-entry aligned pitch, x even
     else
-      ent[32 * j + lane] = make_uint2(x < W ? __ldg(mrow + x) : 0xFFFFFFFFu, 0xFFFFFFFFu);
-  }
-  if (orow) {
-#pragma unroll
-    for (int h = 0; h < 2; ++h) {
-      const int xb = x0 + 128 * h + 4 * lane;
-      if (xb < W) cp_async4(own + 128 * h + 4 * lane, orow + xb);
-    }
+      ent[32 * j + lane] = make_uint2(x < W ? __ldg(mrow + x) : kOffZero, kOffZero);
   }
   cp_async_commit();
   cp_async_wait<0>();
-  __syncwarp();
-  // Segments with one owner (all but those a seam crosses) resolve the source image once per
-  // warp instead of once per pixel.
-  int uo = a.P.default_owner;
-  bool uniform = true;
-  if (orow) {
-    uo = own[0];  // x0 < W for every launched segment
+  // Owners of this lane's entries (fills carry none), then the warp's range of owners.
+  unsigned lo = 8u, hi = 0u;
 #pragma unroll
-    for (int j = 0; j < PJ; ++j) {
-      const int x = x0 + 64 * j + 2 * lane;
-      const int o0 = own[64 * j + 2 * lane], o1 = own[64 * j + 2 * lane + 1];
-      if ((x < W && o0 != uo) || (x + 1 < W && o1 != uo)) uniform = false;
-    }
-    uniform = __all_sync(0xFFFFFFFFu, uniform);
+  for (int j = 0; j < PJ; ++j) {
+    const uint2 e = ent[32 * j + lane];
+    if (e.x < kOffOpaque) lo = min(lo, e.x >> kOwnerShift), hi = max(hi, e.x >> kOwnerShift);
+    if (e.y < kOffOpaque) lo = min(lo, e.y >> kOwnerShift), hi = max(hi, e.y >> kOwnerShift);
   }
-  uniform = uniform && uo < kDevMaxImages;
+  lo = __reduce_min_sync(0xFFFFFFFFu, lo);
+  hi = __reduce_max_sync(0xFFFFFFFFu, hi);
+  const bool uniform = lo >= hi;  // one owner, or fills only
+  const int uo = lo < 8u ? int(lo) : 0;
   // Segments wholly inside the canvas and outside the skipped rect store without checks.
   const bool plain = x0 + 64 * PJ <= W && !(row_skip && x0 < a.skip_x1 && x0 + 64 * PJ > a.skip_x0);
   for (int b = 0; b < a.batch; ++b) {
@@ -120,14 +107,15 @@ __global__ void __launch_bounds__(256, 6) canvas_gather_kernel(const __grid_cons
         const uint2 e2 = ent[32 * j + lane];
 #pragma unroll
         for (int h = 0; h < 2; ++h) {
-          const int x = x0 + 64 * j + 2 * lane + h;
-          const int o = orow ? (x < W ? int(own[64 * j + 2 * lane + h]) : 0xFF) : a.P.default_owner;
-          uint32_t* d = pxw + 2 * (32 * j + lane) + h;
           const uint32_t e = h ? e2.y : e2.x;
-          if (o < kDevMaxImages && e < kOffOpaque)
-            cp_async4(d, reinterpret_cast<const uchar4*>(reinterpret_cast<const char*>(a.S.ptr[o]) + b * a.S.bstride[o]) + e);
-          else
+          uint32_t* d = pxw + 2 * (32 * j + lane) + h;
+          if (e < kOffOpaque) {
+            const int o = int(e >> kOwnerShift);
+            cp_async4(d, reinterpret_cast<const uchar4*>(reinterpret_cast<const char*>(a.S.ptr[o]) + b * a.S.bstride[o]) +
+                             (e & kOffMask));
+          } else {
             *d = fill_of(e);
+          }
         }
       }
     }
@@ -152,10 +140,10 @@ __global__ void __launch_bounds__(256, 6) canvas_gather_kernel(const __grid_cons
   }
 }
 
-// Resolves one plane's packed entries (raw.map) into offsets (res, same layout) for the frames'
-// geometry: owner o < n and (sx, sy) inside image o give sy * pitch / 4 + sx; anything else
-// kOffZero, or kOffOpaque under the soft-seam rule when the owner is valid and sx is not the 65535
-// sentinel.
+// Resolves one plane's packed entries (raw.map) for the frames' geometry (res, same layout):
+// owner o < n and (sx, sy) inside image o give o << 29 | (sy * pitch / 4 + sx); anything else
+// kOffZero, or kOffOpaque under the soft-seam rule when the owner is valid and sx is not the
+// 65535 sentinel. (Frames hold fewer than kOffMask - 1 pixels, so no offset meets a fill code.)
 __global__ void resolve_plane_kernel(const __grid_constant__ PlaneDev raw, uint32_t* res, const __grid_constant__ SrcSet S,
                                      int n, int opaque) {
   const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y;
@@ -166,7 +154,7 @@ __global__ void resolve_plane_kernel(const __grid_constant__ PlaneDev raw, uint3
   uint32_t r = kOffZero;
   if (o < n) {
     if (sx < S.w[o] && sy < S.h[o])
-      r = uint32_t(sy) * uint32_t(S.pitch[o] / 4) + uint32_t(sx);
+      r = (uint32_t(o) << kOwnerShift) | (uint32_t(sy) * uint32_t(S.pitch[o] / 4) + uint32_t(sx));
     else if (opaque && sx != 0xFFFF)
       r = kOffOpaque;
   }

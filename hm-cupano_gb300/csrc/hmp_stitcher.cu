@@ -405,8 +405,8 @@ struct hmp_stitcher {
       if (im.width <= 0 || im.height <= 0 || im.pitch < size_t(im.width) * 4 || im.pitch > size_t(INT_MAX) ||
           im.pitch % 4 != 0)
         return make_status(HMP_ERR_INVALID_VALUE, "input image has an invalid size or pitch");
-      if (size_t(im.height) * (im.pitch / 4) >= size_t(hmp::kOffOpaque))
-        return make_status(HMP_ERR_INVALID_VALUE, "input frame is larger than 4G pixels");
+      if (size_t(im.height) * (im.pitch / 4) >= size_t(hmp::kOffMask) - 1)
+        return make_status(HMP_ERR_NOT_SUPPORTED, "input frames must hold fewer than 2^29 - 2 pixels");
       if (im.width >= 65535 || im.height >= 65535)
         return make_status(HMP_ERR_INVALID_VALUE, "input images must be smaller than 65535 pixels per side");
     }
