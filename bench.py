@@ -196,6 +196,7 @@ def main() -> None:
     ap.add_argument("--levels", type=int, default=6)
     ap.add_argument("--storage", default="f32")
     ap.add_argument("--batch", type=int, default=1, help="frames per process() call")
+    ap.add_argument("--tile-down", type=int, default=0, help="pyramid down tile edge (32 or 64; 0 = default)")
     ap.add_argument("--filter", default="refbox", choices=["refbox", "binomial5"],
                     help="pyramid filter: the reference's 2x2 box / bilinear, or 5-tap binomial")
     ap.add_argument("--graph", action="store_true",
@@ -235,6 +236,8 @@ def main() -> None:
     pano = hmpano.CudaStitchPano(B, args.levels, _masks(rig), quiet=True, storage=args.storage, filter=args.filter)
     if not pano.status.ok():
         raise SystemExit(f"stitcher: {pano.status}")
+    if args.tile_down:
+        pano.set_tiles(args.tile_down)
     info = pano.info()
     W, H = rig.canvas_w, rig.canvas_h
     dev = torch.device("cuda", local)

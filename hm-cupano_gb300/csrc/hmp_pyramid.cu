@@ -1162,6 +1162,83 @@ __global__ void __launch_bounds__(256) pyr_fine_kernel(const __grid_constant__ P
   }
 }
 
+// pyr_fine for the N-way rule with level 0 kept by pyr_down: per pixel, only the block's active
+// slots (a run-time list; the blend never reads others) are visited. The label weights are one-hot,
+// so the blend is the Laplacian of one image: the label's image if it has alpha, else the first
+// image of strictly largest alpha, else zero (blend_pick0's N-way rule, streamed over the list in
+// slot order with two candidate pixels held). Shared memory holds R^1 and `a.fine_cap` G^1 tiles.
+template <typename Store>
+__global__ void __launch_bounds__(256) pyr_fine_n_kernel(const __grid_constant__ PyrArgs a) {
+  extern __shared__ float4 fsm[];
+  const int n = a.n, cap = a.fine_cap;
+  const int b = blockIdx.z;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int bx0 = (a.wx0 & ~1) + blockIdx.x * 64, by0 = (a.wy0 & ~1) + blockIdx.y * 16;
+  const int X = bx0 + 2 * lane, Y = by0 + 2 * warp;
+  const int lw0 = a.lw[0], lh0 = a.lh[0], lw1 = a.lw[1], lh1 = a.lh[1];
+  float4* rs = fsm;
+  Store* gs = reinterpret_cast<Store*>(fsm + kFineTA);
+  uint32_t list = 0;
+  int na = 0;
+  for (int k = 0; k < n; ++k) {
+    const PlaneDev& P = a.slot[k];
+    if (bx0 < P.x0 + P.w && P.x0 < bx0 + 66 && by0 < P.y0 + P.h && P.y0 < by0 + 18 && na < cap)
+      list |= uint32_t(k) << (4 * na++);
+  }
+  {
+    const int tx0 = bx0 >> 1, ty0 = by0 >> 1;
+    const long long fo = (long long)b * lw1 * lh1;
+    for (int j = tid; j < kFineTA; j += 256) {
+      const int y = min(ty0 + j / kFineTW, lh1 - 1), x = min(tx0 + j % kFineTW, lw1 - 1);
+      const long long o = fo + (long long)y * lw1 + x;
+      cp_async<16>(rs + j, a.R1 + o);
+      for (int c = 0; c < na; ++c)
+        cp_async<int(sizeof(Store))>(gs + c * kFineTA + j, static_cast<const Store*>(a.G[(list >> (4 * c)) & 15u][1]) + o);
+    }
+    asm volatile("cp.async.commit_group;\n" ::: "memory");
+    asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+    __syncthreads();
+  }
+  const int ti = warp * kFineTW + lane;
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    const int x = X + (q & 1), y = Y + (q >> 1);
+    if (!(x < lw0 && y < lh0 && x >= a.wx0 && x < a.wx1 && y >= a.wy0 && y < a.wy1)) continue;
+    const int v = int(__ldg(a.mask0 + (long long)y * a.mask0_pitch + x));
+    const bool ox = (q & 1) != 0, oy = (q >> 1) != 0;
+    int lab_c = -1, max_c = -1;
+    uint32_t lab_p = 0, max_p = 0;
+    float amax = 0.f;
+#pragma unroll 1
+    for (int c = 0; c < na; ++c) {
+      const int k = (list >> (4 * c)) & 15u;
+      const PlaneDev& P = a.slot[k];
+      const int rx = x - P.x0, ry = y - P.y0;
+      uint32_t p = 0u;
+      if ((unsigned)rx < (unsigned)P.w && (unsigned)ry < (unsigned)P.h)
+        p = __ldg(a.P0[k] + (long long)b * P.w * P.h + (long long)ry * P.w + rx);
+      const float al = float(p >> 24);
+      if (k == v && al != 0.f) lab_c = c, lab_p = p;
+      if (al > amax) amax = al, max_c = c, max_p = p;
+    }
+    const int pc = lab_c >= 0 ? lab_c : max_c;
+    const uint32_t pp = lab_c >= 0 ? lab_p : max_p;
+    float4 r = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (pc >= 0) {
+      float4 g = make_float4(float(pp & 0xFF), float((pp >> 8) & 0xFF), float((pp >> 16) & 0xFF), float(pp >> 24));
+      const float3 up = up_tile(gs + pc * kFineTA, ti, ox, oy);
+      r = make_float4(g.x - up.x, g.y - up.y, g.z - up.z, g.w);
+    }
+    const float3 up = up_tile(rs, ti, ox, oy);
+    r.x = up.x + r.x;
+    r.y = up.y + r.y;
+    r.z = up.z + r.z;
+    uchar4* crow = reinterpret_cast<uchar4*>(reinterpret_cast<char*>(a.C.ptr) + b * a.C.bstride +
+                                             (long long)(y + a.cy_off) * a.C.pitch);
+    crow[x + a.cx_off] = pack_rgba(r);
+  }
+}
+
 template <int NMAX, typename Store, int T>
 void set_down_attr() {
   cudaFuncSetAttribute(pyr_down_kernel<NMAX, Store, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
@@ -1226,7 +1303,10 @@ void fine_dispatch2(const PyrArgs& a, int rule, dim3 grid, size_t smem, cudaStre
 template <typename Store>
 void fine_dispatch(const PyrArgs& a, int rule, dim3 grid, cudaStream_t stream) {
   const size_t smem = a.levels > 1 ? size_t(kFineTA) * (sizeof(float4) + size_t(a.n) * sizeof(Store)) : 0;
-  if (a.use_p0)
+  if (rule == kRuleNway && a.use_p0 && a.fine_cap > 0 && a.levels > 1)
+    pyr_fine_n_kernel<Store><<<grid, 256, size_t(kFineTA) * (sizeof(float4) + size_t(a.fine_cap) * sizeof(Store)),
+                               stream>>>(a);
+  else if (a.use_p0)
     fine_dispatch2<Store, true>(a, rule, grid, smem, stream);
   else
     fine_dispatch2<Store, false>(a, rule, grid, smem, stream);

@@ -63,6 +63,7 @@ struct hmp_stitcher {
   int tile_down = 0, tile_coarse = 0;
   int down_cap = 0;  // N-way pyr_down: slots held in shared memory (the most any tile overlaps)
   int coarse_cap = 0;  // N-way pyr_coarse: likewise per coarse tile
+  int fine_cap = 0;    // N-way pyr_fine: likewise per 64 x 16 level-0 block and its upsample halo
   size_t coarse_smem = 0;
   float4* R1 = nullptr;
   bool b5 = false;  // Binomial5 filter with at least two levels
@@ -159,6 +160,25 @@ struct hmp_stitcher {
         for (int k = 0; k < p.n; ++k) {
           const hmp::PlaneDev& P = slot_planes[k];
           if (fx0 < P.x0 + P.w && P.x0 < fx1 && fy0 < P.y0 + P.h && P.y0 < fy1) ++c;
+        }
+        best = std::max(best, c);
+      }
+    return best;
+  }
+
+  // The most slot planes the footprint of any pyr_fine block (64 x 16 level-0 pixels of the write
+  // rect plus the 2-pixel upsample halo) overlaps; the same footprint rule as the kernel.
+  int fine_cap_for() const {
+    const hmp::Plan& p = plan;
+    const int wx0 = p.write.x - p.blend.x, wy0 = p.write.y - p.blend.y;
+    const int wx1 = wx0 + p.write.w, wy1 = wy0 + p.write.h;
+    int best = 1;
+    for (int by0 = wy0 & ~1; by0 < wy1; by0 += 16)
+      for (int bx0 = wx0 & ~1; bx0 < wx1; bx0 += 64) {
+        int c = 0;
+        for (int k = 0; k < p.n; ++k) {
+          const hmp::PlaneDev& P = slot_planes[k];
+          if (bx0 < P.x0 + P.w && P.x0 < bx0 + 66 && by0 < P.y0 + P.h && P.y0 < by0 + 18) ++c;
         }
         best = std::max(best, c);
       }
@@ -264,6 +284,7 @@ struct hmp_stitcher {
       // instead of a table lookup and a gather); with two it measured slower (the extra writes
       // lengthen pyr_down more than they shorten pyr_fine), so pyr_fine gathers again.
       use_p0 = L > 1 && !b5 && n >= 3;
+      fine_cap = (use_p0 && n > 3) ? fine_cap_for() : 0;
       for (int k = 0; use_p0 && k < n; ++k) {
         const hmp::PlaneDev& P = slot_planes[k];
         if (P.w <= 0 || P.h <= 0) continue;
@@ -496,6 +517,7 @@ struct hmp_stitcher {
     a.cx_off = p.blend.x;
     a.cy_off = p.blend.y;
     a.use_p0 = use_p0 ? 1 : 0;
+    a.fine_cap = fine_cap;
     for (int k = 0; k < p.n; ++k) a.P0[k] = P0[k];
     if (b5) {
       // Binomial5: the level-by-level chain (its time is reported under pyr_down).
