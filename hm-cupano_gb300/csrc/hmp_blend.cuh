@@ -222,6 +222,74 @@ __device__ __forceinline__ float4 blend_level(int n, const float4* lap, const fl
   }
 }
 
+// Mask class of an N-way pixel at level l >= 1, from the planner (same values as its MaskHot):
+// 0..n-1 = the one-hot image, kHotNone = all weights 0, kHotFrac = fractional weights.
+constexpr int kHotNone = 0xFE, kHotFrac = 0xFF;
+
+// One N-way blended Laplacian pixel at level l >= 1, visiting only a tile's compact slot list
+// (slot order; slots off the list read as zero there, so they change no pick, sum or alpha):
+//   pix(c)    : G^l pixel of list entry c;
+//   lap(c, g) : g minus entry c's upsampled G^(l+1) in colour (g itself at the coarsest level);
+//   hot       : the pixel's mask class; mk: its mask values, read only for kHotFrac.
+// The result equals blend_pick + blend_alpha, or blend_level for fractional weights (up to the
+// sign of a zero), restated over the list: the one-hot image when it has alpha, else the first
+// image of strictly largest alpha; for fractional weights blend_nway's normalised sums.
+template <class Pix, class Lap>
+__device__ __forceinline__ float4 nway_lap_blend(int n, int na, uint32_t list, uint32_t cmap, int hot,
+                                                 const float* mk, Pix pix, Lap lap) {
+  if (hot < 16) {
+    const uint32_t c = (cmap >> (4 * hot)) & 15u;
+    if (c < 15u) {
+      const float4 g = pix(int(c));
+      if (g.w != 0.f) return lap(int(c), g);
+    }
+  }
+  float amax = 0.f;
+  int mc = -1;
+  float4 mg = make_float4(0.f, 0.f, 0.f, 0.f);
+  if (hot != kHotFrac) {
+    for (int c = 0; c < na; ++c) {
+      const float4 g = pix(c);
+      if (g.w > amax) {
+        amax = g.w;
+        mc = c;
+        mg = g;
+      }
+    }
+    return mc >= 0 ? lap(mc, mg) : make_float4(0.f, 0.f, 0.f, 0.f);
+  }
+  float sumw = 0.f;
+  for (int k = 0; k < n; ++k) sumw += __ldg(mk + k);
+  float sumw2 = 0.f;
+  for (int c = 0; c < na; ++c) {
+    float w = __ldg(mk + ((list >> (4 * c)) & 15u));
+    if (sumw > 0.f) w /= sumw;
+    const float4 g = pix(c);
+    if (g.w > amax) {
+      amax = g.w;
+      mc = c;
+      mg = g;
+    }
+    if (g.w == 0.f) w = 0.f;
+    sumw2 += w;
+  }
+  if (!(sumw2 > 0.f)) return mc >= 0 ? lap(mc, mg) : make_float4(0.f, 0.f, 0.f, 0.f);
+  float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+  for (int c = 0; c < na; ++c) {
+    float w = __ldg(mk + ((list >> (4 * c)) & 15u));
+    if (sumw > 0.f) w /= sumw;
+    const float4 g = pix(c);
+    if (g.w == 0.f) w = 0.f;
+    w /= sumw2;
+    const float4 L = lap(c, g);
+    acc.x += w * L.x;
+    acc.y += w * L.y;
+    acc.z += w * L.z;
+    if (w != 0.f && L.w > acc.w) acc.w = L.w;
+  }
+  return acc;
+}
+
 // Blend of one level-0 pixel from its seam value (two-image weight) or label (one-hot).
 template <int RULE, int NMAX>
 __device__ __forceinline__ float4 blend_level0(int n, const float4* lap, int v) {

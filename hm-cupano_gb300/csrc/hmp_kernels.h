@@ -29,6 +29,7 @@ struct PyrArgs {
   const uint8_t* mask0;                   // level-0 weight value (two-image) or label, blend coords
   int mask0_pitch;
   const float* maskL[kDevMaxLevels];      // level l >= 1: [lh][lw][K]
+  const uint8_t* hotL[kDevMaxLevels];     // N-way rule, level l >= 1: [lh][lw] mask class
   int K;
   int opaque;
   int tile;  // tile edge (level 0 for pyr_down, level 1 for pyr_coarse)

@@ -24,6 +24,11 @@ constexpr int kMaxLevels = 7;          // levels one fused pyramid pass supports
 
 enum BlendRule : int { kRuleNway = 1, kRuleTwo = 2, kRuleThree = 3 };
 
+// Mask class of an N-way pixel at level l >= 1 (values shared with the kernels): 0..n-1 = the
+// image whose weight is 1 while the others are 0; kHotNone = every weight 0; kHotFrac = any other
+// weights (the blend then reads the K mask values).
+enum MaskHot : uint8_t { kHotNone = 0xFE, kHotFrac = 0xFF };
+
 struct Rect {
   int x = 0, y = 0, w = 0, h = 0;
   bool empty() const { return w <= 0 || h <= 0; }
@@ -59,6 +64,7 @@ struct Plan {
   std::vector<GatherPlane> slots;   // n, blend coordinates
   std::vector<uint8_t> mask0;       // blend.w * blend.h: two-image weight value or label
   std::vector<std::vector<float>> mask_levels;  // levels >= 1: lw*lh*mask_k floats
+  std::vector<std::vector<uint8_t>> mask_hot;   // N-way rule, levels >= 1: lw*lh MaskHot classes
   std::vector<int> lw, lh;          // level dims
   std::vector<int> src_w, src_h;    // expected source sizes (0 = unknown)
 };

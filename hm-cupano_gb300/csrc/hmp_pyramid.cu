@@ -764,11 +764,11 @@ __global__ void __launch_bounds__(256) pyr_coarse_kernel(const __grid_constant__
 
 // pyr_coarse for the N-way rule: the tile's active slots (those whose plane meets the footprint
 // of the regions read) form a run-time list, shared memory holds `a.coarse_cap` slots (the most
-// any tile has, from the planner), and level 1 reads only the alphas before the pick, then the
-// picked slot's pixel. Same arithmetic as pyr_coarse_kernel (inactive slots read as zero).
+// any tile has, from the planner) and no mask values: each pixel reads its mask class (one byte)
+// and, where the weights are one-hot, first the class image's pixel, which decides the pick when
+// it has alpha (nway_lap_blend). Same results as pyr_coarse_kernel (inactive slots read as zero).
 template <typename Store, int T1>
 __global__ void __launch_bounds__(256) pyr_coarse_n_kernel(const __grid_constant__ PyrArgs a) {
-  constexpr int NMAX = kDevMaxImages;
   extern __shared__ float4 sm[];
   char* smb = reinterpret_cast<char*>(sm);
   const int n = a.n, K = a.K, cap = a.coarse_cap;
@@ -776,7 +776,7 @@ __global__ void __launch_bounds__(256) pyr_coarse_n_kernel(const __grid_constant
   const int X1 = (a.tx0 + blockIdx.x) * T1, Y1 = (a.ty0 + blockIdx.y) * T1;
   const int L = a.levels, c = L - 1;
   const int tid = threadIdx.x;
-  const CoarseLayout lo = coarse_layout(cap, K, T1, L, int(sizeof(Store)));
+  const CoarseLayout lo = coarse_layout(cap, 0, T1, L, int(sizeof(Store)));
   int rax[kL], ray[kL], rbx[kL], rby[kL];
   {
     int ax = X1, ay = Y1, bx = min(X1 + T1, a.lw[1]), by = min(Y1 + T1, a.lh[1]);
@@ -831,15 +831,6 @@ __global__ void __launch_bounds__(256) pyr_coarse_n_kernel(const __grid_constant
         if (x < rw && y < rh) cp_async<int(sizeof(Store))>(gl + i, Gl + (long long)(lay + y) * lw + (lax + x));
       }
     }
-    const float* ml = a.maskL[l];
-    float* mb = reinterpret_cast<float*>(smb + lo.m[l]);
-    for (int p = tid; p < CAP; p += 256) {
-      const int x = p % CW, y = p / CW;
-      if (x < rw && y < rh) {
-        const float* src = ml + ((long long)(lay + y) * lw + (lax + x)) * K;
-        for (int q = 0; q < K; ++q) cp_async<4>(mb + p * K + q, src + q);
-      }
-    }
   }
   cp_async_commit_wait_all();
   __syncthreads();
@@ -849,9 +840,11 @@ __global__ void __launch_bounds__(256) pyr_coarse_n_kernel(const __grid_constant
     const int CW = up_cw(T1, l - 1), CAP = CW * CW;
     const int QW = (CW + 1) / 2, QC = QW * QW;
     const int lax = rax[l], lay = ray[l], rw = rbx[l] - lax, rh = rby[l] - lay;
+    const int lw = a.lw[l];
     const Store* gcur = reinterpret_cast<const Store*>(smb + lo.g[l]);
     float4* rcur = reinterpret_cast<float4*>(smb + lo.r[l]);
-    const float* mb = reinterpret_cast<const float*>(smb + lo.m[l]);
+    const uint8_t* hl = a.hotL[l];
+    const float* ml = a.maskL[l];
     const bool has_next = l < c;
     const int nl = l + 1 < kL ? l + 1 : l;
     const int CWN = up_cw(T1, nl - 1), CAPN = CWN * CWN;
@@ -865,43 +858,18 @@ __global__ void __launch_bounds__(256) pyr_coarse_n_kernel(const __grid_constant
       if (x >= rw || y >= rh) continue;
       const int i = y * CW + x;
       const int px = lax + x, py = lay + y;
-      float al[NMAX];
-#pragma unroll
-      for (int k = 0; k < NMAX; ++k) {
-        const uint32_t ci = (cmap >> (4 * k)) & 15u;
-        al[k] = (k < n && ci < 15u) ? load_level(gcur + ci * CAP + i).w : 0.f;
-      }
-      const int pk = blend_pick<kRuleNway, NMAX>(n, al, mb + i * K);
-      float4 r = make_float4(0.f, 0.f, 0.f, 0.f);
-      if (pk >= 0) {
-        const int ci = (cmap >> (4 * pk)) & 15u;  // picked: alpha > 0, so active
-        float4 g = load_level(gcur + ci * CAP + i);
+      const long long o = (long long)py * lw + px;
+      const auto pix = [&](int ci) { return load_level(gcur + ci * CAP + i); };
+      const auto lap = [&](int ci, float4 g) {
         if (has_next) {
           const float3 up = up_alpha(gnext + ci * CAPN, CWN, nax, nay, lwn, lhn, px, py);
           g.x = g.x - up.x;
           g.y = g.y - up.y;
           g.z = g.z - up.z;
         }
-        r = make_float4(g.x, g.y, g.z, blend_alpha<kRuleNway, NMAX>(al, pk));
-      } else if (pk == kPickAll) {
-        float4 lap[NMAX];
-#pragma unroll
-        for (int k = 0; k < NMAX; ++k) {
-          const uint32_t ci = (cmap >> (4 * k)) & 15u;
-          lap[k] = make_float4(0.f, 0.f, 0.f, 0.f);
-          if (k < n && ci < 15u) {
-            float4 g = load_level(gcur + ci * CAP + i);
-            if (has_next) {
-              const float3 up = up_alpha(gnext + ci * CAPN, CWN, nax, nay, lwn, lhn, px, py);
-              g.x = g.x - up.x;
-              g.y = g.y - up.y;
-              g.z = g.z - up.z;
-            }
-            lap[k] = g;
-          }
-        }
-        r = blend_level<kRuleNway, NMAX>(n, lap, mb + i * K);
-      }
+        return g;
+      };
+      float4 r = nway_lap_blend(n, na, list, cmap, int(__ldg(hl + o)), ml + o * K, pix, lap);
       if (has_next) {
         const float3 up = up_alpha(rnext, CWN, nax, nay, lwn, lhn, px, py);
         r.x = up.x + r.x;
@@ -920,7 +888,8 @@ __global__ void __launch_bounds__(256) pyr_coarse_n_kernel(const __grid_constant
   const int lw2 = a.lw[2 < kL ? 2 : 1], lh2 = a.lh[2 < kL ? 2 : 1];
   const Store* g2 = reinterpret_cast<const Store*>(smb + lo.g[2]);
   const float4* r2 = reinterpret_cast<const float4*>(smb + lo.r[2]);
-  float4* R1 = a.R1 + (long long)b * lw1 * lh1;
+  const long long boff = (long long)b * lw1 * lh1;
+  float4* R1 = a.R1 + boff;
 #pragma unroll 1
   for (int p = 0; p < PER; ++p) {
     const int i = p * 256 + tid;
@@ -928,44 +897,19 @@ __global__ void __launch_bounds__(256) pyr_coarse_n_kernel(const __grid_constant
     const int px = X1 + lx, py = Y1 + ly;
     if (px >= lw1 || py >= lh1) continue;
     const long long o1 = (long long)py * lw1 + px;
-    float m[NMAX], al[NMAX];
-#pragma unroll
-    for (int q = 0; q < NMAX; ++q) m[q] = q < K ? __ldg(a.maskL[1] + o1 * K + q) : 0.f;
-#pragma unroll
-    for (int k = 0; k < NMAX; ++k) {
-      const uint32_t ci = (cmap >> (4 * k)) & 15u;
-      al[k] = (k < n && ci < 15u) ? ldg_level(static_cast<const Store*>(a.G[k][1]) + (long long)b * lw1 * lh1 + o1).w : 0.f;
-    }
-    const int pk = blend_pick<kRuleNway, NMAX>(n, al, m);
-    float4 r = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (pk >= 0) {
-      const int ci = (cmap >> (4 * pk)) & 15u;
-      float4 g = ldg_level(static_cast<const Store*>(a.G[pk][1]) + (long long)b * lw1 * lh1 + o1);
+    const auto pix = [&](int ci) {
+      return ldg_level(static_cast<const Store*>(a.G[(list >> (4 * ci)) & 15u][1]) + boff + o1);
+    };
+    const auto lap = [&](int ci, float4 g) {
       if (has2) {
         const float3 up = up_alpha(g2 + ci * CAP2, CW2, nax, nay, lw2, lh2, px, py);
         g.x = g.x - up.x;
         g.y = g.y - up.y;
         g.z = g.z - up.z;
       }
-      r = make_float4(g.x, g.y, g.z, blend_alpha<kRuleNway, NMAX>(al, pk));
-    } else if (pk == kPickAll) {
-      float4 g1[NMAX];
-#pragma unroll
-      for (int k = 0; k < NMAX; ++k) {
-        const uint32_t ci = (cmap >> (4 * k)) & 15u;
-        g1[k] = make_float4(0.f, 0.f, 0.f, 0.f);
-        if (k < n && ci < 15u) {
-          g1[k] = ldg_level(static_cast<const Store*>(a.G[k][1]) + (long long)b * lw1 * lh1 + o1);
-          if (has2) {
-            const float3 up = up_alpha(g2 + ci * CAP2, CW2, nax, nay, lw2, lh2, px, py);
-            g1[k].x = g1[k].x - up.x;
-            g1[k].y = g1[k].y - up.y;
-            g1[k].z = g1[k].z - up.z;
-          }
-        }
-      }
-      r = blend_level<kRuleNway, NMAX>(n, g1, m);
-    }
+      return g;
+    };
+    float4 r = nway_lap_blend(n, na, list, cmap, int(__ldg(a.hotL[1] + o1)), a.maskL[1] + o1 * K, pix, lap);
     if (has2) {
       const float3 up = up_alpha(r2, CW2, nax, nay, lw2, lh2, px, py);
       r.x = up.x + r.x;
@@ -1162,11 +1106,11 @@ __global__ void __launch_bounds__(256) pyr_fine_kernel(const __grid_constant__ P
   }
 }
 
-// pyr_fine for the N-way rule with level 0 kept by pyr_down: per pixel, only the block's active
-// slots (a run-time list; the blend never reads others) are visited. The label weights are one-hot,
-// so the blend is the Laplacian of one image: the label's image if it has alpha, else the first
-// image of strictly largest alpha, else zero (blend_pick0's N-way rule, streamed over the list in
-// slot order with two candidate pixels held). Shared memory holds R^1 and `a.fine_cap` G^1 tiles.
+// pyr_fine for the N-way rule with level 0 kept by pyr_down: the block's active slots (those
+// whose plane meets its footprint with the upsample halo) form a run-time list, shared memory
+// holds R^1 and `a.fine_cap` G^1 tiles. The label weights are one-hot, so the blend is the
+// Laplacian of one image (blend_pick0): the label's image where it has alpha -- one load -- and
+// otherwise the first image of strictly largest alpha, found by walking the list in slot order.
 template <typename Store>
 __global__ void __launch_bounds__(256) pyr_fine_n_kernel(const __grid_constant__ PyrArgs a) {
   extern __shared__ float4 fsm[];
@@ -1178,12 +1122,15 @@ __global__ void __launch_bounds__(256) pyr_fine_n_kernel(const __grid_constant__
   const int lw0 = a.lw[0], lh0 = a.lh[0], lw1 = a.lw[1], lh1 = a.lh[1];
   float4* rs = fsm;
   Store* gs = reinterpret_cast<Store*>(fsm + kFineTA);
-  uint32_t list = 0;
+  uint32_t list = 0, cmap = 0xFFFFFFFFu;  // compact list (slot per nibble), slot -> compact index
   int na = 0;
   for (int k = 0; k < n; ++k) {
     const PlaneDev& P = a.slot[k];
-    if (bx0 < P.x0 + P.w && P.x0 < bx0 + 66 && by0 < P.y0 + P.h && P.y0 < by0 + 18 && na < cap)
-      list |= uint32_t(k) << (4 * na++);
+    if (bx0 < P.x0 + P.w && P.x0 < bx0 + 66 && by0 < P.y0 + P.h && P.y0 < by0 + 18 && na < cap) {
+      list |= uint32_t(k) << (4 * na);
+      cmap = (cmap & ~(0xFu << (4 * k))) | (uint32_t(na) << (4 * k));
+      ++na;
+    }
   }
   {
     const int tx0 = bx0 >> 1, ty0 = by0 >> 1;
@@ -1196,38 +1143,71 @@ __global__ void __launch_bounds__(256) pyr_fine_n_kernel(const __grid_constant__
         cp_async<int(sizeof(Store))>(gs + c * kFineTA + j, static_cast<const Store*>(a.G[(list >> (4 * c)) & 15u][1]) + o);
     }
     asm volatile("cp.async.commit_group;\n" ::: "memory");
-    asm volatile("cp.async.wait_group 0;\n" ::: "memory");
-    __syncthreads();
   }
   const int ti = warp * kFineTW + lane;
+  bool live[4], done[4];
+  int pc[4];
+  uint32_t pp[4];
+  {
+    int v[4];
+    uint32_t p[4];
 #pragma unroll
-  for (int q = 0; q < 4; ++q) {
-    const int x = X + (q & 1), y = Y + (q >> 1);
-    if (!(x < lw0 && y < lh0 && x >= a.wx0 && x < a.wx1 && y >= a.wy0 && y < a.wy1)) continue;
-    const int v = int(__ldg(a.mask0 + (long long)y * a.mask0_pitch + x));
-    const bool ox = (q & 1) != 0, oy = (q >> 1) != 0;
-    int lab_c = -1, max_c = -1;
-    uint32_t lab_p = 0, max_p = 0;
-    float amax = 0.f;
+    for (int q = 0; q < 4; ++q) {
+      const int x = X + (q & 1), y = Y + (q >> 1);
+      live[q] = x < lw0 && y < lh0 && x >= a.wx0 && x < a.wx1 && y >= a.wy0 && y < a.wy1;
+      v[q] = live[q] ? int(__ldg(a.mask0 + (long long)y * a.mask0_pitch + x)) : 15;
+      p[q] = 0u;
+      if (v[q] < n) {  // an inactive label's plane misses the pixel: its alpha is 0
+        const PlaneDev& P = a.slot[v[q]];
+        const int rx = x - P.x0, ry = y - P.y0;
+        if ((unsigned)rx < (unsigned)P.w && (unsigned)ry < (unsigned)P.h)
+          p[q] = __ldg(a.P0[v[q]] + (long long)b * P.w * P.h + (long long)ry * P.w + rx);
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      done[q] = !live[q] || (p[q] >> 24) != 0u;
+      pc[q] = (p[q] >> 24) != 0u ? int((cmap >> (4 * v[q])) & 15u) : -1;
+      pp[q] = p[q];
+    }
+  }
+  if (!(done[0] && done[1] && done[2] && done[3])) {
+    uint32_t amax[4] = {0u, 0u, 0u, 0u};
 #pragma unroll 1
     for (int c = 0; c < na; ++c) {
       const int k = (list >> (4 * c)) & 15u;
       const PlaneDev& P = a.slot[k];
-      const int rx = x - P.x0, ry = y - P.y0;
-      uint32_t p = 0u;
-      if ((unsigned)rx < (unsigned)P.w && (unsigned)ry < (unsigned)P.h)
-        p = __ldg(a.P0[k] + (long long)b * P.w * P.h + (long long)ry * P.w + rx);
-      const float al = float(p >> 24);
-      if (k == v && al != 0.f) lab_c = c, lab_p = p;
-      if (al > amax) amax = al, max_c = c, max_p = p;
+      const uint32_t* p0 = a.P0[k] + (long long)b * P.w * P.h;
+      uint32_t p[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const int rx = X + (q & 1) - P.x0, ry = Y + (q >> 1) - P.y0;
+        p[q] = 0u;
+        if (!done[q] && (unsigned)rx < (unsigned)P.w && (unsigned)ry < (unsigned)P.h)
+          p[q] = __ldg(p0 + (long long)ry * P.w + rx);
+      }
+#pragma unroll
+      for (int q = 0; q < 4; ++q)
+        if ((p[q] >> 24) > amax[q]) {
+          amax[q] = p[q] >> 24;
+          pc[q] = c;
+          pp[q] = p[q];
+        }
     }
-    const int pc = lab_c >= 0 ? lab_c : max_c;
-    const uint32_t pp = lab_c >= 0 ? lab_p : max_p;
+  }
+  asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+  __syncthreads();
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    if (!live[q]) continue;
+    const int x = X + (q & 1), y = Y + (q >> 1);
+    const bool ox = (q & 1) != 0, oy = (q >> 1) != 0;
     float4 r = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (pc >= 0) {
-      float4 g = make_float4(float(pp & 0xFF), float((pp >> 8) & 0xFF), float((pp >> 16) & 0xFF), float(pp >> 24));
-      const float3 up = up_tile(gs + pc * kFineTA, ti, ox, oy);
-      r = make_float4(g.x - up.x, g.y - up.y, g.z - up.z, g.w);
+    if (pc[q] >= 0) {
+      const uint32_t g = pp[q];
+      const float3 up = up_tile(gs + pc[q] * kFineTA, ti, ox, oy);
+      r = make_float4(float(g & 0xFF) - up.x, float((g >> 8) & 0xFF) - up.y, float((g >> 16) & 0xFF) - up.z,
+                      float(g >> 24));
     }
     const float3 up = up_tile(rs, ti, ox, oy);
     r.x = up.x + r.x;

@@ -58,6 +58,7 @@ struct hmp_stitcher {
   hmp::PlaneDev slot_planes[hmp::kDevMaxImages]{};
   void* G[hmp::kDevMaxImages][hmp::kDevMaxLevels]{};
   const float* maskL[hmp::kDevMaxLevels]{};
+  const uint8_t* hotL[hmp::kDevMaxLevels]{};
   const uint8_t* mask0 = nullptr;
   int mask0_pitch = 0;
   int tile_down = 0, tile_coarse = 0;
@@ -185,6 +186,13 @@ struct hmp_stitcher {
     return best;
   }
 
+  // pyr_coarse's shared memory: the N-way kernel holds `coarse_cap` slots and no mask values.
+  size_t coarse_smem_for(int t1) const {
+    const hmp::Plan& p = plan;
+    if (coarse_cap > 0) return hmp::pyr_coarse_smem(coarse_cap, 0, t1, p.levels, p.storage);
+    return hmp::pyr_coarse_smem(p.n, p.mask_k, t1, p.levels, p.storage);
+  }
+
   // The most slot planes any td x td level-0 tile of the blend region overlaps.
   int down_cap_for(int td) const {
     const hmp::Plan& p = plan;
@@ -242,6 +250,14 @@ struct hmp_stitcher {
         e = cudaMemcpy(mk, p.mask_levels[l].data(), mb, cudaMemcpyHostToDevice);
         if (e != cudaSuccess) return cuda_status(e, "mask pyramid upload");
         maskL[l] = static_cast<const float*>(mk);
+        if (l < int(p.mask_hot.size()) && !p.mask_hot[l].empty()) {
+          void* hk = nullptr;
+          e = alloc(&hk, p.mask_hot[l].size());
+          if (e != cudaSuccess) return cuda_status(e, "mask class allocation");
+          e = cudaMemcpy(hk, p.mask_hot[l].data(), p.mask_hot[l].size(), cudaMemcpyHostToDevice);
+          if (e != cudaSuccess) return cuda_status(e, "mask class upload");
+          hotL[l] = static_cast<const uint8_t*>(hk);
+        }
         for (int k = 0; k < n; ++k) {
           const size_t gb = size_t(B) * p.lw[l] * p.lh[l] * px_bytes;
           e = alloc(&G[k][l], gb);
@@ -272,7 +288,7 @@ struct hmp_stitcher {
       }
       tile_coarse = std::max(32, align / 2);
       coarse_cap = (n > 3 && L > 2) ? coarse_cap_for(tile_coarse) : 0;
-      coarse_smem = hmp::pyr_coarse_smem(coarse_cap > 0 ? coarse_cap : n, p.mask_k, tile_coarse, L, p.storage);
+      coarse_smem = coarse_smem_for(tile_coarse);
       b5 = p.filter == HMP_FILTER_BINOMIAL5 && L > 1;
       if (L > 1 && !b5) {
         void* r = nullptr;
@@ -329,6 +345,7 @@ struct hmp_stitcher {
     }
     std::vector<uint8_t>().swap(p.mask0);
     for (auto& m : p.mask_levels) std::vector<float>().swap(m);
+    for (auto& m : p.mask_hot) std::vector<uint8_t>().swap(m);
     return ok_status();
   }
 
@@ -503,6 +520,7 @@ struct hmp_stitcher {
       a.lw[l] = p.lw[l];
       a.lh[l] = p.lh[l];
       a.maskL[l] = maskL[l];
+      a.hotL[l] = hotL[l];
       for (int k = 0; k < p.n; ++k) a.G[k][l] = G[k][l];
     }
     a.mask0 = mask0;
@@ -669,7 +687,7 @@ HMP_API hmp_status hmp_stitcher_set_tiles(hmp_stitcher* st, int tile_down, int t
   st->tile_down = tile_down;
   st->down_cap = cap;
   st->tile_coarse = tile_coarse;
-  st->coarse_smem = hmp::pyr_coarse_smem(p.n, p.mask_k, tile_coarse, p.levels, p.storage);
+  st->coarse_smem = st->coarse_smem_for(tile_coarse);
   return make_status(HMP_OK, "");
 }
 
