@@ -77,6 +77,8 @@ WORKLOADS = [
     ("pano3_2704x1520_to_6000x1800", 3, 6, 0.25, True, 1, {}),
     ("pano3_2704x1520_to_6000x1800", 1, 6, 0.25, True, 1, {}),
     ("pano3_2704x1520_to_6000x1800", 3, 4, 0.25, True, 1, {"oob_fraction": 0.02}),
+    ("pano3_2704x1520_to_6000x1800", 3, 2, 0.25, True, 2, {}),
+    ("panon8_2000x1500_to_9000x2400", 1, 2, 0.25, True, 1, {}),
 ]
 
 
