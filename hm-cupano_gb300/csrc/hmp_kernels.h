@@ -42,6 +42,7 @@ struct PyrArgs {
   int slots_cap;  // N-way pyr_down: shared memory holds this many slots (the most any tile has)
   int coarse_cap; // N-way pyr_coarse: likewise, per coarse tile
   int fine_cap;   // N-way pyr_fine: likewise, per 64 x 16 level-0 block (with its upsample halo)
+  int pdl;        // launch pyr_coarse / pyr_fine as programmatic dependents of the kernel before them
   CanvasDev C;
   int wx0, wy0, wx1, wy1;  // write rect, blend coordinates, end exclusive
   int cx_off, cy_off;      // canvas = blend + offset

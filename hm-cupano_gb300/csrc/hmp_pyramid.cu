@@ -115,6 +115,13 @@ __device__ __forceinline__ Store* level_of(const PyrArgs& a, int k, int l, int b
 // previous level in shared memory (levels 3, 5 reuse the level-0 buffer). Every level >= 1 goes
 // to HBM. A slot whose plane misses the tile produces zeros, which its level buffers already
 // hold, so it is skipped entirely.
+// Programmatic dependent launch: pyr_coarse and pyr_fine are launched with programmatic stream
+// serialization, so their CTAs can be scheduled as the kernel before them on the stream drains
+// (its CTAs trigger implicitly at exit; an explicit early trigger measured slower beside the
+// canvas gather, the waiting CTAs holding SM resources). griddepcontrol.wait returns once that
+// kernel has completed and its writes are visible (at once after a normal launch).
+__device__ __forceinline__ void grid_dep_wait() { asm volatile("griddepcontrol.wait;\n" ::: "memory"); }
+
 template <int NMAX, typename Store, int TD>
 __global__ void __launch_bounds__(256) pyr_down_kernel(const __grid_constant__ PyrArgs a) {
   // Only the three- and N-image kernels keep level 0 for pyr_fine; the two-image kernel is
@@ -555,6 +562,7 @@ template <int RULE, int NMAX, typename Store, int T1>
 __global__ void __launch_bounds__(256) pyr_coarse_kernel(const __grid_constant__ PyrArgs a) {
   extern __shared__ float4 sm[];
   char* smb = reinterpret_cast<char*>(sm);
+  grid_dep_wait();  // G^l of pyr_down
   const int n = RULE == kRuleNway ? a.n : NMAX;
   const int K = RULE == kRuleTwo ? 1 : (RULE == kRuleThree ? 3 : a.K);
   const int b = blockIdx.z;
@@ -771,6 +779,7 @@ template <typename Store, int T1>
 __global__ void __launch_bounds__(256) pyr_coarse_n_kernel(const __grid_constant__ PyrArgs a) {
   extern __shared__ float4 sm[];
   char* smb = reinterpret_cast<char*>(sm);
+  grid_dep_wait();  // G^l of pyr_down
   const int n = a.n, K = a.K, cap = a.coarse_cap;
   const int b = blockIdx.z;
   const int X1 = (a.tx0 + blockIdx.x) * T1, Y1 = (a.ty0 + blockIdx.y) * T1;
@@ -991,20 +1000,7 @@ __global__ void __launch_bounds__(256) pyr_fine_kernel(const __grid_constant__ P
     const PlaneDev& P = a.slot[k];
     if (k < n && bx0 < P.x0 + P.w && P.x0 < bx0 + 66 && by0 < P.y0 + P.h && P.y0 < by0 + 18) amask |= 1u << k;
   }
-  if (has1) {
-    const int tx0 = bx0 >> 1, ty0 = by0 >> 1;
-    const long long fo = (long long)b * lw1 * lh1;
-    for (int j = tid; j < kFineTA; j += 256) {
-      const int y = min(ty0 + j / kFineTW, lh1 - 1), x = min(tx0 + j % kFineTW, lw1 - 1);
-      const long long o = fo + (long long)y * lw1 + x;
-      cp_async<16>(rs + j, a.R1 + o);
-#pragma unroll
-      for (int k = 0; k < NMAX; ++k)
-        if ((amask >> k) & 1u)
-          cp_async<int(sizeof(Store))>(gs + k * kFineTA + j, static_cast<const Store*>(a.G[k][1]) + o);
-    }
-    asm volatile("cp.async.commit_group;\n" ::: "memory");
-  }
+  if (P0M) grid_dep_wait();  // level 0 of pyr_down
   // Pixels of the quad are processed QB at a time: all four (every lookup and gather in flight
   // together) for up to three images; one at a time for the N-way kernel, whose eight images'
   // arrays would not fit in registers four times over.
@@ -1036,6 +1032,23 @@ __global__ void __launch_bounds__(256) pyr_fine_kernel(const __grid_constant__ P
           slot_lookup(a.slot[k], k, x, y, own[u][k], ent[u][k]);
         }
       }
+    }
+    // The tiles (R^1 of pyr_coarse, G^1 of pyr_down) are requested after the first lookups, which
+    // read only the tables and the frames and so overlap the wait for pyr_coarse.
+    if (q0 == 0 && has1) {
+      if (!P0M) grid_dep_wait();
+      const int tx0 = bx0 >> 1, ty0 = by0 >> 1;
+      const long long fo = (long long)b * lw1 * lh1;
+      for (int j = tid; j < kFineTA; j += 256) {
+        const int y = min(ty0 + j / kFineTW, lh1 - 1), x = min(tx0 + j % kFineTW, lw1 - 1);
+        const long long o = fo + (long long)y * lw1 + x;
+        cp_async<16>(rs + j, a.R1 + o);
+#pragma unroll
+        for (int k = 0; k < NMAX; ++k)
+          if ((amask >> k) & 1u)
+            cp_async<int(sizeof(Store))>(gs + k * kFineTA + j, static_cast<const Store*>(a.G[k][1]) + o);
+      }
+      asm volatile("cp.async.commit_group;\n" ::: "memory");
     }
     uchar4 src[QB][NMAX];
 #pragma unroll
@@ -1114,6 +1127,7 @@ __global__ void __launch_bounds__(256) pyr_fine_kernel(const __grid_constant__ P
 template <typename Store>
 __global__ void __launch_bounds__(256) pyr_fine_n_kernel(const __grid_constant__ PyrArgs a) {
   extern __shared__ float4 fsm[];
+  grid_dep_wait();  // R^1 of pyr_coarse; G^1 and level 0 of pyr_down
   const int n = a.n, cap = a.fine_cap;
   const int b = blockIdx.z;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -1258,34 +1272,51 @@ void down_dispatch(const PyrArgs& a, dim3 grid, size_t smem, cudaStream_t stream
     pyr_down_kernel<8, Store, T><<<grid, 256, smem, stream>>>(a);
 }
 
+// Launches a pyramid kernel; with a.pdl as a programmatic dependent of the kernel before it on
+// the stream (the kernel waits for that kernel's results with grid_dep_wait).
+template <typename Kern>
+void launch_pyr(Kern k, dim3 grid, size_t smem, cudaStream_t stream, const PyrArgs& a) {
+  cudaLaunchConfig_t cfg{};
+  cfg.gridDim = grid;
+  cfg.blockDim = dim3(256);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = stream;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = a.pdl ? 1 : 0;
+  cudaLaunchKernelEx(&cfg, k, a);
+}
+
 template <typename Store, int T>
 void coarse_dispatch(const PyrArgs& a, int rule, dim3 grid, size_t smem, cudaStream_t stream) {
   if (rule == kRuleTwo)
-    pyr_coarse_kernel<kRuleTwo, 2, Store, T><<<grid, 256, smem, stream>>>(a);
+    launch_pyr(pyr_coarse_kernel<kRuleTwo, 2, Store, T>, grid, smem, stream, a);
   else if (rule == kRuleThree)
-    pyr_coarse_kernel<kRuleThree, 3, Store, T><<<grid, 256, smem, stream>>>(a);
+    launch_pyr(pyr_coarse_kernel<kRuleThree, 3, Store, T>, grid, smem, stream, a);
   else if (a.coarse_cap > 0)
-    pyr_coarse_n_kernel<Store, T><<<grid, 256, smem, stream>>>(a);
+    launch_pyr(pyr_coarse_n_kernel<Store, T>, grid, smem, stream, a);
   else
-    pyr_coarse_kernel<kRuleNway, 8, Store, T><<<grid, 256, smem, stream>>>(a);
+    launch_pyr(pyr_coarse_kernel<kRuleNway, 8, Store, T>, grid, smem, stream, a);
 }
 
 template <typename Store, bool P0M>
 void fine_dispatch2(const PyrArgs& a, int rule, dim3 grid, size_t smem, cudaStream_t stream) {
   if (rule == kRuleTwo)
-    pyr_fine_kernel<kRuleTwo, 2, Store, P0M><<<grid, 256, smem, stream>>>(a);
+    launch_pyr(pyr_fine_kernel<kRuleTwo, 2, Store, P0M>, grid, smem, stream, a);
   else if (rule == kRuleThree)
-    pyr_fine_kernel<kRuleThree, 3, Store, P0M><<<grid, 256, smem, stream>>>(a);
+    launch_pyr(pyr_fine_kernel<kRuleThree, 3, Store, P0M>, grid, smem, stream, a);
   else
-    pyr_fine_kernel<kRuleNway, 8, Store, P0M><<<grid, 256, smem, stream>>>(a);
+    launch_pyr(pyr_fine_kernel<kRuleNway, 8, Store, P0M>, grid, smem, stream, a);
 }
 
 template <typename Store>
 void fine_dispatch(const PyrArgs& a, int rule, dim3 grid, cudaStream_t stream) {
   const size_t smem = a.levels > 1 ? size_t(kFineTA) * (sizeof(float4) + size_t(a.n) * sizeof(Store)) : 0;
   if (rule == kRuleNway && a.use_p0 && a.fine_cap > 0 && a.levels > 1)
-    pyr_fine_n_kernel<Store><<<grid, 256, size_t(kFineTA) * (sizeof(float4) + size_t(a.fine_cap) * sizeof(Store)),
-                               stream>>>(a);
+    launch_pyr(pyr_fine_n_kernel<Store>, grid, size_t(kFineTA) * (sizeof(float4) + size_t(a.fine_cap) * sizeof(Store)),
+               stream, a);
   else if (a.use_p0)
     fine_dispatch2<Store, true>(a, rule, grid, smem, stream);
   else

@@ -536,6 +536,7 @@ struct hmp_stitcher {
     a.cy_off = p.blend.y;
     a.use_p0 = use_p0 ? 1 : 0;
     a.fine_cap = fine_cap;
+    a.pdl = p.levels > 1 && !b5 ? 1 : 0;  // pyr_coarse follows pyr_down, pyr_fine pyr_coarse
     for (int k = 0; k < p.n; ++k) a.P0[k] = P0[k];
     if (b5) {
       // Binomial5: the level-by-level chain (its time is reported under pyr_down).
