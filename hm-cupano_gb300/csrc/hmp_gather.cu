@@ -3,12 +3,13 @@
 // Replaces, per frame, the reference's canvas memset plus one remap launch per image
 // (src/pano/cudaPano.inl:186-359 with src/cuda/cudaRemap.cu:203-294; the three-image fused hard
 // seam src/cuda/cudaFusedKernels3.cu:124-217; the N-image fused hard seam cudaRemap.cu:251-294).
-// One pass over the canvas: each warp owns a 256-pixel row segment, copies its owner bytes and
-// packed table entries into shared memory, copies the source pixels they select (cp.async, for
-// every frame of the batch) and stores them in full lines. Pixels with no owner get zero, so no
-// memset is needed. Table entries are resolved offsets (resolve_plane_kernel below), so a pixel
-// costs one compare and one multiply-add besides its copies.
-// HBM-bound: 1 + 4 + 4 + 4 = 13 bytes per canvas pixel.
+// One pass over the canvas: each warp owns a 256-pixel row segment, copies its table entries into
+// shared memory, copies the source pixels they select (cp.async, for every frame of the batch) and
+// stores them in full lines. Pixels with no owner get zero, so no memset is needed. Table entries
+// are resolved (resolve_plane_kernel below) to the owner and the pixel offset in its frame, and the
+// resolve pass also records each segment's owner when it has only one, so a pixel costs one
+// compare and one multiply-add besides its copies.
+// HBM-bound: 4 (entry) + 4 (source) + 4 (canvas) = 12 bytes per canvas pixel.
 #include <algorithm>
 
 #include "hmp_kernels.h"
@@ -54,6 +55,7 @@ __device__ __forceinline__ void gather_one(uint32_t* dst, const uchar4* base, ui
 // crosses) resolves the owner's frame once per warp.
 __global__ void __launch_bounds__(256, 6) canvas_gather_kernel(const __grid_constant__ GatherArgs a) {
   constexpr int PJ = 4;  // 64-pixel steps per segment
+  static_assert(64 * PJ == kSegPixels, "a warp's segment is the resolve pass's segment");
   __shared__ __align__(16) uint2 s_ent[8][PJ][32];
   __shared__ __align__(16) uint2 s_px[8][PJ][32];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -75,19 +77,11 @@ __global__ void __launch_bounds__(256, 6) canvas_gather_kernel(const __grid_cons
       ent[32 * j + lane] = make_uint2(x < W ? __ldg(mrow + x) : kOffZero, kOffZero);
   }
   cp_async_commit();
+  // The segment's owner, from the resolve pass: one for all its entries (or only fills), or mixed.
+  const unsigned so = __ldg(a.seg_owner + (long long)y * a.seg_pitch + blockIdx.x);
   cp_async_wait<0>();
-  // Owners of this lane's entries (fills carry none), then the warp's range of owners.
-  unsigned lo = 8u, hi = 0u;
-#pragma unroll
-  for (int j = 0; j < PJ; ++j) {
-    const uint2 e = ent[32 * j + lane];
-    if (e.x < kOffOpaque) lo = min(lo, e.x >> kOwnerShift), hi = max(hi, e.x >> kOwnerShift);
-    if (e.y < kOffOpaque) lo = min(lo, e.y >> kOwnerShift), hi = max(hi, e.y >> kOwnerShift);
-  }
-  lo = __reduce_min_sync(0xFFFFFFFFu, lo);
-  hi = __reduce_max_sync(0xFFFFFFFFu, hi);
-  const bool uniform = lo >= hi;  // one owner, or fills only
-  const int uo = lo < 8u ? int(lo) : 0;
+  const bool uniform = so != kSegMixed;
+  const int uo = uniform ? int(so) : 0;
   // Segments wholly inside the canvas and outside the skipped rect store without checks.
   const bool plain = x0 + 64 * PJ <= W && !(row_skip && x0 < a.skip_x1 && x0 + 64 * PJ > a.skip_x0);
   for (int b = 0; b < a.batch; ++b) {
@@ -144,29 +138,51 @@ __global__ void __launch_bounds__(256, 6) canvas_gather_kernel(const __grid_cons
 // owner o < n and (sx, sy) inside image o give o << 29 | (sy * pitch / 4 + sx); anything else
 // kOffZero, or kOffOpaque under the soft-seam rule when the owner is valid and sx is not the
 // 65535 sentinel. (Frames hold fewer than kOffMask - 1 pixels, so no offset meets a fill code.)
-__global__ void resolve_plane_kernel(const __grid_constant__ PlaneDev raw, uint32_t* res, const __grid_constant__ SrcSet S,
-                                     int n, int opaque) {
-  const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y;
-  if (x >= raw.w || y >= raw.h) return;
-  const int o = raw.owner ? int(raw.owner[(long long)y * raw.owner_pitch + x]) : raw.default_owner;
-  const uint32_t e = raw.map[(long long)y * raw.map_pitch + x];
-  const int sx = int(e & 0xFFFFu), sy = int(e >> 16);
+__global__ void __launch_bounds__(kSegPixels) resolve_plane_kernel(const __grid_constant__ PlaneDev raw, uint32_t* res,
+                                                                   uint8_t* seg_owner, int seg_pitch,
+                                                                   const __grid_constant__ SrcSet S, int n, int opaque) {
+  // One CTA per 256-pixel row segment, the gather's unit.
+  const int x = blockIdx.x * kSegPixels + threadIdx.x, y = blockIdx.y;
   uint32_t r = kOffZero;
-  if (o < n) {
-    if (sx < S.w[o] && sy < S.h[o])
-      r = (uint32_t(o) << kOwnerShift) | (uint32_t(sy) * uint32_t(S.pitch[o] / 4) + uint32_t(sx));
-    else if (opaque && sx != 0xFFFF)
-      r = kOffOpaque;
+  const bool in = x < raw.w;
+  if (in) {
+    const int o = raw.owner ? int(raw.owner[(long long)y * raw.owner_pitch + x]) : raw.default_owner;
+    const uint32_t e = raw.map[(long long)y * raw.map_pitch + x];
+    const int sx = int(e & 0xFFFFu), sy = int(e >> 16);
+    if (o < n) {
+      if (sx < S.w[o] && sy < S.h[o])
+        r = (uint32_t(o) << kOwnerShift) | (uint32_t(sy) * uint32_t(S.pitch[o] / 4) + uint32_t(sx));
+      else if (opaque && sx != 0xFFFF)
+        r = kOffOpaque;
+    }
+    res[(long long)y * raw.map_pitch + x] = r;
   }
-  res[(long long)y * raw.map_pitch + x] = r;
+  // The segment's range of owners (fills carry none).
+  __shared__ unsigned s_lo[kSegPixels / 32], s_hi[kSegPixels / 32];
+  unsigned lo = r < kOffOpaque ? r >> kOwnerShift : 8u, hi = r < kOffOpaque ? r >> kOwnerShift : 0u;
+  lo = __reduce_min_sync(0xFFFFFFFFu, lo);
+  hi = __reduce_max_sync(0xFFFFFFFFu, hi);
+  if ((threadIdx.x & 31) == 0) {
+    s_lo[threadIdx.x >> 5] = lo;
+    s_hi[threadIdx.x >> 5] = hi;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0 && seg_owner) {
+    for (int w = 1; w < kSegPixels / 32; ++w) {
+      lo = min(lo, s_lo[w]);
+      hi = max(hi, s_hi[w]);
+    }
+    seg_owner[(long long)y * seg_pitch + blockIdx.x] = lo >= hi ? uint8_t(lo < 8u ? lo : 0u) : kSegMixed;
+  }
 }
 
 }  // namespace
 
-cudaError_t launch_resolve_plane(const PlaneDev& raw, uint32_t* res, const SrcSet& S, int n, bool opaque,
-                                 cudaStream_t stream) {
+cudaError_t launch_resolve_plane(const PlaneDev& raw, uint32_t* res, uint8_t* seg_owner, int seg_pitch, const SrcSet& S,
+                                 int n, bool opaque, cudaStream_t stream) {
   if (raw.w <= 0 || raw.h <= 0) return cudaSuccess;
-  resolve_plane_kernel<<<dim3((raw.w + 255) / 256, raw.h), 256, 0, stream>>>(raw, res, S, n, opaque ? 1 : 0);
+  resolve_plane_kernel<<<dim3((raw.w + kSegPixels - 1) / kSegPixels, raw.h), kSegPixels, 0, stream>>>(
+      raw, res, seg_owner, seg_pitch, S, n, opaque ? 1 : 0);
   return cudaGetLastError();
 }
 

@@ -15,7 +15,13 @@ struct GatherArgs {
   int batch;
   int skip_x0, skip_y0, skip_x1, skip_y1;  // pixels written by the pyramid (end exclusive)
   int n_owners;  // images the plane can select (owners are < n_owners)
+  // Per 256-pixel row segment [y][x / 256] (written with the resolved plane): the one owner of its
+  // entries (0 if it holds only fills), or kSegMixed.
+  const uint8_t* seg_owner;
+  int seg_pitch;
 };
+constexpr int kSegPixels = 256;
+constexpr uint8_t kSegMixed = 0xFF;
 
 // Shared by the Gaussian-pyramid (down) and blend/reconstruct (up) kernels.
 struct PyrArgs {
@@ -54,8 +60,9 @@ cudaError_t kernels_init();
 
 // Resolves a plane's packed entries (raw.map) into offsets for the frames S (res: raw's layout).
 // opaque: the soft-seam rule for entries outside their source.
-cudaError_t launch_resolve_plane(const PlaneDev& raw, uint32_t* res, const SrcSet& S, int n, bool opaque,
-                                 cudaStream_t stream);
+// Also writes seg_owner (see GatherArgs) for the plane's 256-pixel row segments.
+cudaError_t launch_resolve_plane(const PlaneDev& raw, uint32_t* res, uint8_t* seg_owner, int seg_pitch, const SrcSet& S,
+                                 int n, bool opaque, cudaStream_t stream);
 
 cudaError_t launch_canvas_gather(const GatherArgs& a, cudaStream_t stream);
 

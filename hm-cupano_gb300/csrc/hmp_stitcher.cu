@@ -53,6 +53,8 @@ struct hmp_stitcher {
   // geometry) and with the planned packed entries it is resolved from.
   hmp::PlaneDev canvas_plane{}, canvas_raw{};
   bool resolved = false;  // canvas_plane holds offsets for the geometry below
+  uint8_t* seg_owner = nullptr;  // per 256-pixel canvas row segment, written with the resolve
+  int seg_pitch = 0;
   int geo_w[hmp::kDevMaxImages]{}, geo_h[hmp::kDevMaxImages]{};
   long long geo_pitch[hmp::kDevMaxImages]{};
   hmp::PlaneDev slot_planes[hmp::kDevMaxImages]{};
@@ -224,6 +226,11 @@ struct hmp_stitcher {
         e = alloc(&r, size_t(canvas_plane.map_pitch) * 4 * canvas_plane.h);
         if (e != cudaSuccess) return cuda_status(e, "canvas plane allocation");
         canvas_plane.map = static_cast<const uint32_t*>(r);
+        seg_pitch = round_up((canvas_plane.w + hmp::kSegPixels - 1) / hmp::kSegPixels, 16);
+        void* so = nullptr;
+        e = alloc(&so, size_t(seg_pitch) * canvas_plane.h);
+        if (e != cudaSuccess) return cuda_status(e, "canvas segment allocation");
+        seg_owner = static_cast<uint8_t*>(so);
       }
     }
     launches = p.canvas_plane_used ? 1 : 0;
@@ -460,8 +467,8 @@ struct hmp_stitcher {
       for (int i = 0; i < p.n; ++i)
         same = same && S.w[i] == geo_w[i] && S.h[i] == geo_h[i] && S.pitch[i] == geo_pitch[i];
       if (!same) {
-        const cudaError_t re = hmp::launch_resolve_plane(canvas_raw, const_cast<uint32_t*>(canvas_plane.map), S, p.n,
-                                                         p.canvas_opaque, s);
+        const cudaError_t re = hmp::launch_resolve_plane(canvas_raw, const_cast<uint32_t*>(canvas_plane.map), seg_owner,
+                                                         seg_pitch, S, p.n, p.canvas_opaque, s);
         if (re != cudaSuccess) return cuda_status(re, "canvas plane resolve launch");
         for (int i = 0; i < p.n; ++i) {
           geo_w[i] = S.w[i];
@@ -485,6 +492,8 @@ struct hmp_stitcher {
       ga.C = C;
       ga.batch = p.batch;
       ga.n_owners = p.n;
+      ga.seg_owner = seg_owner;
+      ga.seg_pitch = seg_pitch;
       if (p.levels > 0) {
         ga.skip_x0 = p.write.x;
         ga.skip_y0 = p.write.y;

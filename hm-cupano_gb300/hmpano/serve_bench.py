@@ -1,6 +1,10 @@
 """Serving benchmark: Poisson arrivals of stitch requests over a mix of seeded pano configurations,
 served by hmp_server (continuous batching, resident stitchers, HBM-budget admission).
 
+Also, per configuration of the mix alone (`python -m hmpano.serve_bench [--config SUBSTRING]`, with
+hm-cupano_gb300 on the path and the library built): frame time on one stream and per-kernel
+CUDA-event times from a pass with the kernels serialised.
+
 The mix is 12 configurations: four seeded rigs (2 x 1280x720 -> 2200x800, 2 x 5120x2880 ->
 8500x3300, 8 x 2000x1500 -> 9000x2400, 3 x 2704x1520 -> 6000x1800) at levels 0, 3 and 6. Each
 request picks a configuration uniformly at random. Reported per offered rate: achieved canvas
@@ -163,3 +167,59 @@ def sweep(device, budget_gb: float = 150.0, slots: int = 8, per_config: int = 2,
             "saturation": sat, "plain_path": plain, "rates": rates,
             "p50_ms_at_75pct": mid["p50_ms"], "p99_ms_at_75pct": mid["p99_ms"],
             "speedup_vs_plain": round(sat["achieved_mpix_s"] / plain["mpix_s"], 3)}
+
+
+def per_config(device, match: str = "", reps: int = 50, warmup: int = 5) -> list[dict]:
+    """Each configuration of the mix alone: microseconds per frame (batch 1, one stream, CUDA
+    events over `reps` frames) and per-kernel times from a serialised pass."""
+    import torch
+
+    out = []
+    stream = torch.cuda.Stream(device)
+    sp = C.c_void_p(stream.cuda_stream)
+    fn = _lib.lib().hmp_stitcher_process
+    for m in build_mix(device):
+        if match not in m["name"]:
+            continue
+        cls = {2: pano.CudaStitchPano, 3: pano.CudaStitchPano3}.get(m["kind"], pano.CudaStitchPanoN)
+        st = cls(1, m["levels"], m["masks"], quiet=True)
+        if not st.status.ok():
+            raise pano.CudaStatusError(st.status)
+
+        def go(k):
+            for j in range(k):
+                s = fn(st._handle, m["imgs"], len(m["frames"]), C.byref(m["cimgs"][j % len(m["cimgs"])]), sp)
+                if s.code:
+                    raise RuntimeError(s.message.decode())
+
+        go(warmup)
+        torch.cuda.synchronize(device)
+        st.set_timing(True, serialize=True)
+        go(20)
+        torch.cuda.synchronize(device)
+        kt = st.kernel_times()
+        st.set_timing(False)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        go(reps)
+        e1.record(stream)
+        torch.cuda.synchronize(device)
+        us = e0.elapsed_time(e1) / reps * 1e3
+        out.append({"config": m["name"], "us_per_frame": round(us, 1), "gpix_s": round(m["mpix"] / us * 1e3, 1),
+                    "kernel_us_serialized": {k: round(v[0] / max(v[1], 1) * 1e3, 1) for k, v in kt.items()}})
+        del st
+    return out
+
+
+if __name__ == "__main__":
+    import argparse
+    import json
+
+    import torch
+
+    ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
+    ap.add_argument("--config", default="", help="only configurations whose name contains this")
+    ap.add_argument("--reps", type=int, default=50)
+    args = ap.parse_args()
+    for r in per_config(torch.device("cuda", 0), args.config, args.reps):
+        print(json.dumps(r), flush=True)
