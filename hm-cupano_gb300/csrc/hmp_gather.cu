@@ -38,7 +38,7 @@ __device__ __forceinline__ void cp_async8(void* dst, const void* src) {
 // a 4-byte copy into *dst, or its fill.
 __device__ __forceinline__ void gather_one(uint32_t* dst, const uchar4* base, uint32_t e) {
   if (e < kOffOpaque)
-    cp_async4(dst, base + (e & kOffMask));
+    cp_async4(dst, base + e);
   else
     *dst = fill_of(e);
 }
@@ -81,19 +81,29 @@ __global__ void __launch_bounds__(256, 6) canvas_gather_kernel(const __grid_cons
   const unsigned so = __ldg(a.seg_owner + (long long)y * a.seg_pitch + blockIdx.x);
   cp_async_wait<0>();
   const bool uniform = so != kSegMixed;
-  const int uo = uniform ? int(so) : 0;
+  const int uo = int(so & (kSegFills - 1));
   // Segments wholly inside the canvas and outside the skipped rect store without checks.
   const bool plain = x0 + 64 * PJ <= W && !(row_skip && x0 < a.skip_x1 && x0 + 64 * PJ > a.skip_x0);
   for (int b = 0; b < a.batch; ++b) {
     uint32_t* pxw = reinterpret_cast<uint32_t*>(px);
     if (uniform) {
+      // One owner: the entries are plain offsets into its frame (or fills, if the segment has any).
       const uchar4* base =
           reinterpret_cast<const uchar4*>(reinterpret_cast<const char*>(a.S.ptr[uo]) + b * a.S.bstride[uo]);
+      if (so & kSegFills) {
 #pragma unroll
-      for (int j = 0; j < PJ; ++j) {
-        const uint2 e = ent[32 * j + lane];
-        gather_one(pxw + 2 * (32 * j + lane), base, e.x);
-        gather_one(pxw + 2 * (32 * j + lane) + 1, base, e.y);
+        for (int j = 0; j < PJ; ++j) {
+          const uint2 e = ent[32 * j + lane];
+          gather_one(pxw + 2 * (32 * j + lane), base, e.x);
+          gather_one(pxw + 2 * (32 * j + lane) + 1, base, e.y);
+        }
+      } else {
+#pragma unroll
+        for (int j = 0; j < PJ; ++j) {
+          const uint2 e = ent[32 * j + lane];
+          cp_async4(pxw + 2 * (32 * j + lane), base + e.x);
+          cp_async4(pxw + 2 * (32 * j + lane) + 1, base + e.y);
+        }
       }
     } else {
 #pragma unroll
@@ -143,7 +153,7 @@ __global__ void __launch_bounds__(kSegPixels) resolve_plane_kernel(const __grid_
                                                                    const __grid_constant__ SrcSet S, int n, int opaque) {
   // One CTA per 256-pixel row segment, the gather's unit.
   const int x = blockIdx.x * kSegPixels + threadIdx.x, y = blockIdx.y;
-  uint32_t r = kOffZero;
+  uint32_t r = kOffZero;  // pixels past the plane's width read as fills
   const bool in = x < raw.w;
   if (in) {
     const int o = raw.owner ? int(raw.owner[(long long)y * raw.owner_pitch + x]) : raw.default_owner;
@@ -155,25 +165,33 @@ __global__ void __launch_bounds__(kSegPixels) resolve_plane_kernel(const __grid_
       else if (opaque && sx != 0xFFFF)
         r = kOffOpaque;
     }
-    res[(long long)y * raw.map_pitch + x] = r;
   }
-  // The segment's range of owners (fills carry none).
-  __shared__ unsigned s_lo[kSegPixels / 32], s_hi[kSegPixels / 32];
+  // The segment's range of owners and whether it holds fills.
+  __shared__ unsigned s_lo[kSegPixels / 32], s_hi[kSegPixels / 32], s_fill[kSegPixels / 32];
+  __shared__ unsigned s_code;
   unsigned lo = r < kOffOpaque ? r >> kOwnerShift : 8u, hi = r < kOffOpaque ? r >> kOwnerShift : 0u;
   lo = __reduce_min_sync(0xFFFFFFFFu, lo);
   hi = __reduce_max_sync(0xFFFFFFFFu, hi);
+  const unsigned fill = __reduce_or_sync(0xFFFFFFFFu, r >= kOffOpaque ? 1u : 0u);
   if ((threadIdx.x & 31) == 0) {
     s_lo[threadIdx.x >> 5] = lo;
     s_hi[threadIdx.x >> 5] = hi;
+    s_fill[threadIdx.x >> 5] = fill;
   }
   __syncthreads();
-  if (threadIdx.x == 0 && seg_owner) {
+  if (threadIdx.x == 0) {
+    unsigned f = fill;
     for (int w = 1; w < kSegPixels / 32; ++w) {
       lo = min(lo, s_lo[w]);
       hi = max(hi, s_hi[w]);
+      f |= s_fill[w];
     }
-    seg_owner[(long long)y * seg_pitch + blockIdx.x] = lo >= hi ? uint8_t(lo < 8u ? lo : 0u) : kSegMixed;
+    s_code = lo >= hi ? ((lo < 8u ? lo : 0u) | (f ? kSegFills : 0u)) : kSegMixed;
+    if (seg_owner) seg_owner[(long long)y * seg_pitch + blockIdx.x] = uint8_t(s_code);
   }
+  __syncthreads();
+  // Entries of a one-owner segment are stored without their owner (the segment has it).
+  if (in) res[(long long)y * raw.map_pitch + x] = (s_code != kSegMixed && r < kOffOpaque) ? (r & kOffMask) : r;
 }
 
 }  // namespace

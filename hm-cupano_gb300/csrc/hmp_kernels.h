@@ -15,13 +15,14 @@ struct GatherArgs {
   int batch;
   int skip_x0, skip_y0, skip_x1, skip_y1;  // pixels written by the pyramid (end exclusive)
   int n_owners;  // images the plane can select (owners are < n_owners)
-  // Per 256-pixel row segment [y][x / 256] (written with the resolved plane): the one owner of its
-  // entries (0 if it holds only fills), or kSegMixed.
+  // Per 256-pixel row segment [y][x / 256] (written with the resolved plane): kSegMixed if its
+  // entries have several owners; else their one owner (0 if only fills), plus kSegFills if any
+  // entry is a fill. A one-owner segment's entries are stored without the owner bits.
   const uint8_t* seg_owner;
   int seg_pitch;
 };
 constexpr int kSegPixels = 256;
-constexpr uint8_t kSegMixed = 0xFF;
+constexpr unsigned kSegFills = 8u, kSegMixed = 0xFFu;
 
 // Shared by the Gaussian-pyramid (down) and blend/reconstruct (up) kernels.
 struct PyrArgs {
