@@ -3,12 +3,12 @@
 // Replaces, per frame, the reference's canvas memset plus one remap launch per image
 // (src/pano/cudaPano.inl:186-359 with src/cuda/cudaRemap.cu:203-294; the three-image fused hard
 // seam src/cuda/cudaFusedKernels3.cu:124-217; the N-image fused hard seam cudaRemap.cu:251-294).
-// One pass over the canvas: each warp owns a 256-pixel row segment, copies its table entries into
-// shared memory, copies the source pixels they select (cp.async, for every frame of the batch) and
-// stores them in full lines. Pixels with no owner get zero, so no memset is needed. Table entries
-// are resolved (resolve_plane_kernel below) to the owner and the pixel offset in its frame, and the
-// resolve pass also records each segment's owner when it has only one, so a pixel costs one
-// compare and one multiply-add besides its copies.
+// One pass over the canvas: each warp owns a 256-pixel row segment, loads its table entries, reads
+// the source pixels they select (for every frame of the batch) and stores them in full lines.
+// Pixels with no owner get zero, so no memset is needed. Table entries are resolved
+// (resolve_plane_kernel below) to the owner and the pixel offset in its frame, and the resolve pass
+// also records each segment's owner when it has only one and whether it holds fills, so a pixel of
+// a fill-free one-owner segment costs a multiply-add besides its load and store.
 // HBM-bound: 4 (entry) + 4 (source) + 4 (canvas) = 12 bytes per canvas pixel.
 #include <algorithm>
 
@@ -30,10 +30,6 @@ __device__ __forceinline__ void cp_async_wait() {
   asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
 }
 
-__device__ __forceinline__ void cp_async8(void* dst, const void* src) {
-  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(smem_addr(dst)), "l"(src));
-}
-
 // Source pixel of a canvas pixel with resolved entry e in the frame at base (the entry's owner):
 // a 4-byte copy into *dst, or its fill.
 __device__ __forceinline__ void gather_one(uint32_t* dst, const uchar4* base, uint32_t e) {
@@ -45,18 +41,21 @@ __device__ __forceinline__ void gather_one(uint32_t* dst, const uchar4* base, ui
 
 // Each warp owns a 256-pixel segment of one canvas row; lane l handles the pixel pairs
 // (2l, 2l+1) + 64j, j = 0..3, so every warp instruction below touches 64 consecutive pixels:
-// table entries are 8-byte copies (256 bytes per instruction), the source gathers of
-// neighbouring canvas pixels land in the same few source lines, and the canvas stores are
-// 8-byte streaming stores of full lines. All loads are cp.async copies into shared memory laid
-// out [pixel step][lane] (conflict-free), so they need no destination registers and stay in
-// flight together: table entries first, then one 4-byte copy per source pixel and frame. Each
-// lane reads back only what it copied itself. Entries carry their owner (owner << 29 | offset),
-// so no owner plane is read; a segment whose entries share one owner (all but those a seam
-// crosses) resolves the owner's frame once per warp.
+// table entries are 8-byte loads (256 bytes per instruction), the source reads of neighbouring
+// canvas pixels land in the same few source lines, and the canvas stores are 8-byte streaming
+// stores of full lines. The segment's code from the resolve pass picks the path:
+//   - one owner, no fills, whole segment stored (most of a canvas): the eight source pixels are
+//     loaded into registers, all in flight together, and stored in pairs;
+//   - otherwise they are cp.async copies into shared memory laid out [pixel step][lane]
+//     (conflict-free; each lane reads back only what it copied), with fills written directly and
+//     the owner taken per pixel from the entry (owner << 29 | offset) where a seam crosses the
+//     segment.
+// Measured: loading the entries into registers instead of staging them in shared memory, and the
+// register path, each took about 4 % off the two-image 8500x3300 frame (fewer shared-memory
+// instructions in the queue that the pyramid kernels running beside the gather also use).
 __global__ void __launch_bounds__(256, 6) canvas_gather_kernel(const __grid_constant__ GatherArgs a) {
   constexpr int PJ = 4;  // 64-pixel steps per segment
   static_assert(64 * PJ == kSegPixels, "a warp's segment is the resolve pass's segment");
-  __shared__ __align__(16) uint2 s_ent[8][PJ][32];
   __shared__ __align__(16) uint2 s_px[8][PJ][32];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int x0 = blockIdx.x * (64 * PJ);
@@ -66,26 +65,40 @@ __global__ void __launch_bounds__(256, 6) canvas_gather_kernel(const __grid_cons
   const bool row_skip = y >= a.skip_y0 && y < a.skip_y1;
   if (row_skip && x0 >= a.skip_x0 && x0 + 64 * PJ <= a.skip_x1) return;
   const uint32_t* mrow = a.P.map + (long long)y * a.P.map_pitch;
-  uint2* ent = &s_ent[w][0][0];
   uint2* px = &s_px[w][0][0];
+  uint2 er[PJ];
 #pragma unroll
   for (int j = 0; j < PJ; ++j) {
     const int x = x0 + 64 * j + 2 * lane;
     if (x + 1 < W)
-      cp_async8(ent + 32 * j + lane, mrow + x);  // map rows: 8-entry aligned pitch, x even
+      er[j] = __ldg(reinterpret_cast<const uint2*>(mrow + x));  // map rows: 8-entry aligned pitch, x even
     else
-      ent[32 * j + lane] = make_uint2(x < W ? __ldg(mrow + x) : kOffZero, kOffZero);
+      er[j] = make_uint2(x < W ? __ldg(mrow + x) : kOffZero, kOffZero);
   }
-  cp_async_commit();
   // The segment's owner, from the resolve pass: one for all its entries (or only fills), or mixed.
   const unsigned so = __ldg(a.seg_owner + (long long)y * a.seg_pitch + blockIdx.x);
-  cp_async_wait<0>();
   const bool uniform = so != kSegMixed;
   const int uo = int(so & (kSegFills - 1));
   // Segments wholly inside the canvas and outside the skipped rect store without checks.
   const bool plain = x0 + 64 * PJ <= W && !(row_skip && x0 < a.skip_x1 && x0 + 64 * PJ > a.skip_x0);
   for (int b = 0; b < a.batch; ++b) {
     uint32_t* pxw = reinterpret_cast<uint32_t*>(px);
+    uint32_t* crow = reinterpret_cast<uint32_t*>(reinterpret_cast<char*>(a.C.ptr) + b * a.C.bstride + y * a.C.pitch);
+    if (so < kSegFills && plain && (reinterpret_cast<uintptr_t>(crow) & 7) == 0) {
+      // One owner, no fills, whole segment stored: every load in flight from registers.
+      const uint32_t* base =
+          reinterpret_cast<const uint32_t*>(reinterpret_cast<const char*>(a.S.ptr[uo]) + b * a.S.bstride[uo]);
+      uint32_t v[2 * PJ];
+#pragma unroll
+      for (int j = 0; j < PJ; ++j) {
+        v[2 * j] = __ldg(base + er[j].x);
+        v[2 * j + 1] = __ldg(base + er[j].y);
+      }
+#pragma unroll
+      for (int j = 0; j < PJ; ++j)
+        __stcs(reinterpret_cast<uint2*>(crow + x0 + 64 * j + 2 * lane), make_uint2(v[2 * j], v[2 * j + 1]));
+      continue;
+    }
     if (uniform) {
       // One owner: the entries are plain offsets into its frame (or fills, if the segment has any).
       const uchar4* base =
@@ -93,14 +106,14 @@ __global__ void __launch_bounds__(256, 6) canvas_gather_kernel(const __grid_cons
       if (so & kSegFills) {
 #pragma unroll
         for (int j = 0; j < PJ; ++j) {
-          const uint2 e = ent[32 * j + lane];
+          const uint2 e = er[j];
           gather_one(pxw + 2 * (32 * j + lane), base, e.x);
           gather_one(pxw + 2 * (32 * j + lane) + 1, base, e.y);
         }
       } else {
 #pragma unroll
         for (int j = 0; j < PJ; ++j) {
-          const uint2 e = ent[32 * j + lane];
+          const uint2 e = er[j];
           cp_async4(pxw + 2 * (32 * j + lane), base + e.x);
           cp_async4(pxw + 2 * (32 * j + lane) + 1, base + e.y);
         }
@@ -108,7 +121,7 @@ __global__ void __launch_bounds__(256, 6) canvas_gather_kernel(const __grid_cons
     } else {
 #pragma unroll
       for (int j = 0; j < PJ; ++j) {
-        const uint2 e2 = ent[32 * j + lane];
+        const uint2 e2 = er[j];
 #pragma unroll
         for (int h = 0; h < 2; ++h) {
           const uint32_t e = h ? e2.y : e2.x;
@@ -125,7 +138,6 @@ __global__ void __launch_bounds__(256, 6) canvas_gather_kernel(const __grid_cons
     }
     cp_async_commit();
     cp_async_wait<0>();
-    uint32_t* crow = reinterpret_cast<uint32_t*>(reinterpret_cast<char*>(a.C.ptr) + b * a.C.bstride + y * a.C.pitch);
     if (plain && (reinterpret_cast<uintptr_t>(crow) & 7) == 0) {
 #pragma unroll
       for (int j = 0; j < PJ; ++j)
