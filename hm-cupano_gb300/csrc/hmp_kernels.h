@@ -56,6 +56,17 @@ struct PyrArgs {
   int tx0, ty0;            // first up-tile index
 };
 
+// Pyramid dump (two-image box filter): the levels the fused kernels keep on chip, materialised
+// as float4 [batch][lh][lw] buffers by plain kernels that use the same device functions.
+cudaError_t launch_dump_level0(const PyrArgs& a, int k, float4* out, int batch, cudaStream_t stream);
+cudaError_t launch_dump_widen(const void* level, int storage, long long n, float4* out, cudaStream_t stream);
+cudaError_t launch_dump_lap(const float4* hi, int hw, int hh, const float4* lo, int lw, int lh, float4* lap, int batch,
+                            cudaStream_t stream);
+cudaError_t launch_dump_blend2(const float4* l0, const float4* l1, const float* m, const uint8_t* m0, int m0_pitch, int w,
+                               int h, float4* out, int batch, cudaStream_t stream);
+cudaError_t launch_dump_recon(const float4* lo, int lw, int lh, const float4* bl, int w, int h, float4* out, int batch,
+                              cudaStream_t stream);
+
 // One-time attribute setup (dynamic shared memory limits). Call before capture.
 cudaError_t kernels_init();
 

@@ -1323,6 +1323,65 @@ void fine_dispatch(const PyrArgs& a, int rule, dim3 grid, cudaStream_t stream) {
     fine_dispatch2<Store, false>(a, rule, grid, smem, stream);
 }
 
+// ---- Pyramid dump (hmp_stitcher_dump_pyramid): the levels the fused kernels never store, each
+// materialised by a plain kernel with the same device functions, for inspection only. ----
+
+// Gaussian level 0 of slot k over the blend region: the level-0 gather of pyr_down.
+__global__ void dump_level0_kernel(const __grid_constant__ PyrArgs a, int k, float4* out) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y, b = blockIdx.z;
+  const int lw0 = a.lw[0], lh0 = a.lh[0];
+  if (x >= lw0) return;
+  const PlaneDev& P = a.slot[k];
+  const int rx = x - P.x0, ry = y - P.y0;
+  uint32_t e = 0xFFFFFFFFu;
+  int o = P.owner != nullptr ? 0xFF : k;
+  if ((unsigned)rx < (unsigned)P.w && (unsigned)ry < (unsigned)P.h) {
+    e = __ldg(P.map + (long long)ry * P.map_pitch + rx);
+    if (P.owner != nullptr) o = int(__ldg(P.owner + (long long)ry * P.owner_pitch + rx));
+  }
+  uint32_t fill;
+  const uchar4* sp = slot_src<kDevMaxImages>(a, k, o, e, b, a.opaque != 0, fill);
+  out[((long long)b * lh0 + y) * lw0 + x] = sp ? to_f4(__ldg(sp)) : u32_to_f4(fill);
+}
+
+template <typename Store>
+__global__ void dump_widen_kernel(const Store* in, long long n, float4* out) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = load_level(in + i);
+}
+
+// Laplacian: colour minus the alpha-aware upsample of the next level, the level's alpha.
+__global__ void dump_lap_kernel(const float4* hi, int hw, int hh, const float4* lo, int lw, int lh, float4* lap) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y, b = blockIdx.z;
+  if (x >= hw) return;
+  const long long i = ((long long)b * hh + y) * hw + x;
+  const float4 g = hi[i];
+  const float3 up = up_alpha(lo + (long long)b * lw * lh, lw, 0, 0, lw, lh, x, y);
+  lap[i] = make_float4(g.x - up.x, g.y - up.y, g.z - up.z, g.w);
+}
+
+// Two-image blend of one level: mask values m (levels >= 1) or the level-0 seam weights.
+__global__ void dump_blend2_kernel(const float4* l0, const float4* l1, const float* m, const uint8_t* m0, int m0_pitch,
+                                   int w, int h, float4* out) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y, b = blockIdx.z;
+  if (x >= w) return;
+  const long long i = ((long long)b * h + y) * w + x;
+  const float mv = m ? m[(long long)y * w + x] : float(m0[(long long)y * m0_pitch + x]);
+  out[i] = blend_two(l0[i], l1[i], mv);
+}
+
+// Reconstruction: the alpha-aware upsample of the next level's reconstruction plus the blend.
+__global__ void dump_recon_kernel(const float4* lo, int lw, int lh, const float4* bl, int w, int h, float4* out) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y, b = blockIdx.z;
+  if (x >= w) return;
+  const long long i = ((long long)b * h + y) * w + x;
+  const float4 v = bl[i];
+  const float3 up = up_alpha(lo + (long long)b * lw * lh, lw, 0, 0, lw, lh, x, y);
+  out[i] = make_float4(up.x + v.x, up.y + v.y, up.z + v.z, v.w);
+}
+
+dim3 dump_grid(int w, int h, int batch) { return dim3((w + 255) / 256, h, batch); }
+
 }  // namespace
 
 size_t pyr_down_smem(int n, int tile) {
@@ -1380,6 +1439,38 @@ cudaError_t launch_pyr_fine(const PyrArgs& a, int rule, int storage, dim3 grid, 
     fine_dispatch<half4>(a, rule, grid, stream);
   else
     fine_dispatch<float4>(a, rule, grid, stream);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_dump_level0(const PyrArgs& a, int k, float4* out, int batch, cudaStream_t stream) {
+  dump_level0_kernel<<<dump_grid(a.lw[0], a.lh[0], batch), 256, 0, stream>>>(a, k, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_dump_widen(const void* level, int storage, long long n, float4* out, cudaStream_t stream) {
+  const unsigned blocks = unsigned((n + 255) / 256);
+  if (storage == 1)
+    dump_widen_kernel<half4><<<blocks, 256, 0, stream>>>(static_cast<const half4*>(level), n, out);
+  else
+    dump_widen_kernel<float4><<<blocks, 256, 0, stream>>>(static_cast<const float4*>(level), n, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_dump_lap(const float4* hi, int hw, int hh, const float4* lo, int lw, int lh, float4* lap, int batch,
+                            cudaStream_t stream) {
+  dump_lap_kernel<<<dump_grid(hw, hh, batch), 256, 0, stream>>>(hi, hw, hh, lo, lw, lh, lap);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_dump_blend2(const float4* l0, const float4* l1, const float* m, const uint8_t* m0, int m0_pitch, int w,
+                               int h, float4* out, int batch, cudaStream_t stream) {
+  dump_blend2_kernel<<<dump_grid(w, h, batch), 256, 0, stream>>>(l0, l1, m, m0, m0_pitch, w, h, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_dump_recon(const float4* lo, int lw, int lh, const float4* bl, int w, int h, float4* out, int batch,
+                              cudaStream_t stream) {
+  dump_recon_kernel<<<dump_grid(w, h, batch), 256, 0, stream>>>(lo, lw, lh, bl, w, h, out);
   return cudaGetLastError();
 }
 

@@ -16,6 +16,8 @@
 #include <climits>
 #include <cstdio>
 #include <cstring>
+#include <filesystem>
+#include <fstream>
 #include <new>
 #include <string>
 #include <vector>
@@ -40,6 +42,58 @@ hmp_status cuda_status(cudaError_t e, const char* what) {
 }
 
 inline int round_up(int v, int a) { return (v + a - 1) / a * a; }
+
+// Little-endian baseline TIFF of float32 samples, uncompressed, one strip: ch = 1 (grey) or 4
+// (RGBA, unassociated alpha), rows top to bottom, `px` holding ch floats per pixel.
+bool write_tiff_f32(const std::string& path, int w, int h, int ch, const float* px) {
+  std::vector<uint8_t> b;
+  const auto u16 = [&](uint32_t v) {
+    b.push_back(uint8_t(v));
+    b.push_back(uint8_t(v >> 8));
+  };
+  const auto u32 = [&](uint32_t v) {
+    u16(v & 0xFFFFu);
+    u16(v >> 16);
+  };
+  const uint32_t n_tags = ch == 4 ? 12 : 11;
+  const uint32_t ifd = 8, arrays = ifd + 2 + 12 * n_tags + 4;
+  const uint32_t bits_at = arrays, fmt_at = arrays + 2 * ch, data_at = fmt_at + 2 * ch;
+  const uint64_t data_bytes = uint64_t(w) * h * ch * 4;
+  if (data_at + data_bytes > 0xFFFFFFFFull) return false;
+  b.push_back('I');
+  b.push_back('I');
+  u16(42);
+  u32(ifd);
+  u16(n_tags);
+  const auto tag = [&](uint32_t id, uint32_t type, uint32_t count, uint32_t value) {
+    u16(id);
+    u16(type);
+    u32(count);
+    u32(value);  // a SHORT value sits in the low half, little-endian
+  };
+  constexpr uint32_t kShort = 3, kLong = 4;
+  tag(256, kLong, 1, uint32_t(w));
+  tag(257, kLong, 1, uint32_t(h));
+  tag(258, kShort, ch, ch == 1 ? 32u : bits_at);     // BitsPerSample
+  tag(259, kShort, 1, 1);                            // no compression
+  tag(262, kShort, 1, ch == 4 ? 2u : 1u);           // RGB / BlackIsZero
+  tag(273, kLong, 1, data_at);                       // StripOffsets
+  tag(277, kShort, 1, uint32_t(ch));                 // SamplesPerPixel
+  tag(278, kLong, 1, uint32_t(h));                   // RowsPerStrip
+  tag(279, kLong, 1, uint32_t(data_bytes));          // StripByteCounts
+  tag(284, kShort, 1, 1);                            // PlanarConfiguration: contiguous
+  if (ch == 4) tag(338, kShort, 1, 2);               // ExtraSamples: unassociated alpha
+  tag(339, kShort, ch, ch == 1 ? 3u : fmt_at);      // SampleFormat: IEEE float
+  u32(0);                                            // no next IFD
+  for (int i = 0; i < ch; ++i) u16(32);
+  for (int i = 0; i < ch; ++i) u16(3);
+  if (ch == 1) b.resize(data_at);  // the arrays are inline for one sample
+  std::ofstream f(path, std::ios::binary);
+  if (!f) return false;
+  f.write(reinterpret_cast<const char*>(b.data()), std::streamsize(b.size()));
+  f.write(reinterpret_cast<const char*>(px), std::streamsize(data_bytes));
+  return bool(f);
+}
 
 }  // namespace
 
@@ -77,6 +131,8 @@ struct hmp_stitcher {
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   double m0_bytes = 0;
   int launches = 0;
+  hmp::SrcSet last_src{};  // frames of the last process(), for the pyramid dump
+  bool have_last = false;
   // Optional per-kernel event timing (hmp_stitcher_set_timing).
   static constexpr int kTimingSlots = 4096;
   static constexpr int kTimed = 4;
@@ -374,6 +430,128 @@ struct hmp_stitcher {
     m0_bytes = bytes;
   }
 
+  // The soft-blend pyramid of the last process() (cudaPano.inl:420-458): every level of the two
+  // Gaussian pyramids, the mask, both Laplacians, the blend and the reconstruction, as float32 TIFF
+  // files `<label>/level_<l>_batch_<b>.tiff` (`mask/level_<l>.tiff`) plus metadata.txt. The fused
+  // kernels keep these levels on chip, so they are recomputed here from the last frames (which must
+  // still hold them) by plain kernels using the same device functions; not a per-frame call.
+  hmp_status dump_pyramid(const char* directory, cudaStream_t s) {
+    const hmp::Plan& p = plan;
+    if (!directory) return make_status(HMP_ERR_INVALID_VALUE, "directory is null");
+    if (p.levels == 0)
+      return make_status(HMP_ERR_INVALID_VALUE, "Soft-blend pyramid is only available when num_levels > 0");
+    if (p.rule != hmp::kRuleTwo || b5)
+      return make_status(HMP_ERR_NOT_SUPPORTED, "the pyramid dump covers the two-image stitcher with the box filter");
+    if (!have_last) return make_status(HMP_ERR_INVALID_VALUE, "No Laplacian workspace is populated yet: call process() first");
+    int dev = -1;
+    cudaGetDevice(&dev);
+    if (dev != device) return make_status(HMP_ERR_INVALID_VALUE, "dump called on another device");
+    cudaError_t e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return cuda_status(e, "stream synchronize");
+    namespace fs = std::filesystem;
+    const fs::path root(directory);
+    std::error_code ec;
+    for (const char* sub : {"", "gauss1", "gauss2", "mask", "lap1", "lap2", "blend", "reconstruct"}) {
+      fs::create_directories(root / sub, ec);
+      if (ec) return make_status(HMP_ERR_UNKNOWN, "Unable to create directory " + (root / sub).string() + ": " + ec.message());
+    }
+    const int L = p.levels, B = p.batch;
+    std::vector<void*> owned;
+    struct Free {
+      std::vector<void*>& v;
+      ~Free() {
+        for (void* q : v) cudaFree(q);
+      }
+    } free_all{owned};
+    const auto level_bytes = [&](int l) { return size_t(B) * p.lw[l] * p.lh[l] * sizeof(float4); };
+    std::vector<float4*> g[2], lap[2], bl(L), rc(L);
+    for (int l = 0; l < L; ++l) {
+      for (float4** slot : {&bl[l], &rc[l]}) {
+        void* q = nullptr;
+        if ((e = cudaMalloc(&q, level_bytes(l))) != cudaSuccess) return cuda_status(e, "dump allocation");
+        owned.push_back(q);
+        *slot = static_cast<float4*>(q);
+      }
+      for (int k = 0; k < 2; ++k)
+        for (auto* v : {&g[k], &lap[k]}) {
+          void* q = nullptr;
+          if ((e = cudaMalloc(&q, level_bytes(l))) != cudaSuccess) return cuda_status(e, "dump allocation");
+          owned.push_back(q);
+          v->push_back(static_cast<float4*>(q));
+        }
+    }
+    hmp::PyrArgs a{};
+    a.S = last_src;
+    for (int k = 0; k < p.n; ++k) a.slot[k] = slot_planes[k];
+    a.n = p.n;
+    a.levels = L;
+    for (int l = 0; l < L; ++l) {
+      a.lw[l] = p.lw[l];
+      a.lh[l] = p.lh[l];
+    }
+    a.opaque = p.slot_opaque ? 1 : 0;
+    for (int k = 0; k < 2 && e == cudaSuccess; ++k) {
+      e = hmp::launch_dump_level0(a, k, g[k][0], B, s);
+      for (int l = 1; l < L && e == cudaSuccess; ++l)
+        e = hmp::launch_dump_widen(G[k][l], p.storage, (long long)B * p.lw[l] * p.lh[l], g[k][l], s);
+      for (int l = 0; l + 1 < L && e == cudaSuccess; ++l)
+        e = hmp::launch_dump_lap(g[k][l], p.lw[l], p.lh[l], g[k][l + 1], p.lw[l + 1], p.lh[l + 1], lap[k][l], B, s);
+      if (e == cudaSuccess)  // the coarsest Laplacian is the Gaussian itself
+        e = cudaMemcpyAsync(lap[k][L - 1], g[k][L - 1], level_bytes(L - 1), cudaMemcpyDeviceToDevice, s);
+    }
+    for (int l = 0; l < L && e == cudaSuccess; ++l)
+      e = hmp::launch_dump_blend2(lap[0][l], lap[1][l], l ? maskL[l] : nullptr, mask0, mask0_pitch, p.lw[l], p.lh[l], bl[l],
+                                  B, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(rc[L - 1], bl[L - 1], level_bytes(L - 1), cudaMemcpyDeviceToDevice, s);
+    for (int l = L - 2; l >= 0 && e == cudaSuccess; --l)
+      e = hmp::launch_dump_recon(rc[l + 1], p.lw[l + 1], p.lh[l + 1], bl[l], p.lw[l], p.lh[l], rc[l], B, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return cuda_status(e, "pyramid dump");
+    {
+      std::ofstream meta(root / "metadata.txt");
+      meta << "num_levels=" << L << "\n" << "batch_size=" << B << "\n" << "channels=4\n";
+      for (int l = 0; l < L; ++l) meta << "level_" << l << "=" << p.lw[l] << "x" << p.lh[l] << "\n";
+      if (!meta) return make_status(HMP_ERR_UNKNOWN, "Unable to write " + (root / "metadata.txt").string());
+    }
+    std::vector<float> host;
+    const auto write_level = [&](const float4* d, int l, const char* label) -> hmp_status {
+      const size_t px = size_t(p.lw[l]) * p.lh[l];
+      host.resize(px * 4 * B);
+      const cudaError_t ce = cudaMemcpy(host.data(), d, level_bytes(l), cudaMemcpyDeviceToHost);
+      if (ce != cudaSuccess) return cuda_status(ce, "pyramid dump copy");
+      for (int b = 0; b < B; ++b) {
+        const fs::path f = root / label / ("level_" + std::to_string(l) + "_batch_" + std::to_string(b) + ".tiff");
+        if (!write_tiff_f32(f.string(), p.lw[l], p.lh[l], 4, host.data() + px * 4 * b))
+          return make_status(HMP_ERR_UNKNOWN, "Unable to write " + f.string());
+      }
+      return ok_status();
+    };
+    for (int l = 0; l < L; ++l) {
+      const std::pair<const float4*, const char*> items[] = {{g[0][l], "gauss1"}, {g[1][l], "gauss2"}, {lap[0][l], "lap1"},
+                                                             {lap[1][l], "lap2"},  {bl[l], "blend"},     {rc[l], "reconstruct"}};
+      for (const auto& it : items) {
+        const hmp_status st = write_level(it.first, l, it.second);
+        if (st.code != HMP_OK) return st;
+      }
+      // Mask level: the seam weights of image 1 at level 0, the mask pyramid above.
+      const size_t px = size_t(p.lw[l]) * p.lh[l];
+      std::vector<float> m(px);
+      if (l == 0) {
+        std::vector<uint8_t> m8(size_t(mask0_pitch) * p.lh[0]);
+        e = cudaMemcpy(m8.data(), mask0, m8.size(), cudaMemcpyDeviceToHost);
+        for (int y = 0; y < p.lh[0]; ++y)
+          for (int x = 0; x < p.lw[0]; ++x) m[size_t(y) * p.lw[0] + x] = float(m8[size_t(y) * mask0_pitch + x]);
+      } else {
+        e = cudaMemcpy(m.data(), maskL[l], px * sizeof(float), cudaMemcpyDeviceToHost);
+      }
+      if (e != cudaSuccess) return cuda_status(e, "pyramid dump copy");
+      const fs::path f = root / "mask" / ("level_" + std::to_string(l) + ".tiff");
+      if (!write_tiff_f32(f.string(), p.lw[l], p.lh[l], 1, m.data()))
+        return make_status(HMP_ERR_UNKNOWN, "Unable to write " + f.string());
+    }
+    return ok_status();
+  }
+
   cudaError_t timing_enable(int mode) {
     const bool on = mode != 0;
     serialize = mode == 2;
@@ -460,6 +638,8 @@ struct hmp_stitcher {
     if (dev != device) return make_status(HMP_ERR_INVALID_VALUE, "process() called on another device");
 
     const hmp::SrcSet S = sources(inputs);
+    last_src = S;
+    have_last = true;
     if (p.canvas_plane_used) {
       // The gather reads the canvas plane as offsets into these frames: resolve it for their
       // geometry on the first call and whenever a size or pitch changes.
@@ -706,6 +886,12 @@ HMP_API hmp_status hmp_stitcher_set_timing(hmp_stitcher* st, int enable) {
   const cudaError_t e = st->timing_enable(enable);
   if (e != cudaSuccess) return cuda_status(e, "timing events");
   return ok_status();
+}
+
+HMP_API hmp_status hmp_stitcher_dump_pyramid(hmp_stitcher* st, const char* directory, void* stream) {
+  if (!st) return make_status(HMP_ERR_INVALID_VALUE, "stitcher is null");
+  if (st->status.code != HMP_OK) return st->status;
+  return st->dump_pyramid(directory, static_cast<cudaStream_t>(stream));
 }
 
 HMP_API hmp_status hmp_stitcher_get_timing(hmp_stitcher* st, hmp_kernel_timing* out) {

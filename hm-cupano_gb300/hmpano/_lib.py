@@ -115,6 +115,7 @@ SIGNATURES = {
     "hmp_stitcher_process": ([C.c_void_p, C.POINTER(Image), C.c_int, C.POINTER(Image), C.c_void_p], Status),
     "hmp_stitcher_set_timing": ([C.c_void_p, C.c_int], Status),
     "hmp_stitcher_set_tiles": ([C.c_void_p, C.c_int, C.c_int], Status),
+    "hmp_stitcher_dump_pyramid": ([C.c_void_p, C.c_char_p, C.c_void_p], Status),
     "hmp_stitcher_get_timing": ([C.c_void_p, C.POINTER(KernelTiming)], Status),
     "hmp_plan_geometry": ([C.POINTER(Config), C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)], Status),
     "hmp_server_create": ([C.POINTER(ServerOptions), C.POINTER(C.c_void_p)], Status),

@@ -309,6 +309,23 @@ class CudaStitchPano(_Stitcher):
     def process(self, input_image_1, input_image_2, canvas=None, stream=None):
         return self._run([input_image_1, input_image_2], canvas, stream)
 
+    def dump_soft_blend_pyramid(self, directory, *, device=None, channels=None, stream=None) -> None:
+        """Write the soft-blend pyramid of the last process() under `directory`
+        (cupano/pano.py:466-551, src/pano/cudaPano.inl:420-458): metadata.txt and float32 TIFF
+        files gauss1 / gauss2 / lap1 / lap2 / blend / reconstruct `level_<l>_batch_<b>.tiff` and
+        mask `level_<l>.tiff`. The last call's input tensors must still hold their frames.
+        `device` and `channels` are accepted for the reference's signature (one device, RGBA)."""
+        import torch
+
+        del device, channels
+        if stream is None:
+            stream = torch.cuda.current_stream().cuda_stream
+        elif hasattr(stream, "cuda_stream"):
+            stream = stream.cuda_stream
+        s = _status(_lib.lib().hmp_stitcher_dump_pyramid(self._handle, str(directory).encode(), C.c_void_p(stream)))
+        if not s.ok():
+            raise CudaStatusError(s)
+
 
 class CudaStitchPano3(_Stitcher):
     """Three-image stitcher (src/pano/cudaPano3.h:64-182). ``fused`` picks the reference's fused

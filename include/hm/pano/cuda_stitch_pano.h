@@ -296,6 +296,12 @@ class CudaStitchPano : public detail::StitcherBase {
                                                              std::unique_ptr<CudaMat<T_pipeline>>&& canvas) {
     return run<T_pipeline>({&inputImage1, &inputImage2}, stream, std::move(canvas));
   }
+  // Writes the soft-blend pyramid of the last process() under `directory` (cudaPano.h:101):
+  // metadata.txt and float32 TIFF levels; see hmp_stitcher_dump_pyramid.
+  CudaStatus dump_soft_blend_pyramid(const std::string& directory, cudaStream_t stream) const {
+    if (!st_) return status();
+    return CudaStatus::FromC(hmp_stitcher_dump_pyramid(st_, directory.c_str(), stream));
+  }
 };
 
 // Three-image stitcher (src/pano/cudaPano3.h:64-182).

@@ -15,8 +15,10 @@
  *                                                                    src/pano/cudaPano3.h:99-107
  *                            CudaStitchPanoN::process(inputs, stream, canvas)
  *                                                                    src/pano/cudaPanoN.h:97-101
- *   hmp_stitcher_status   <- CudaStitchPano*::status()               src/pano/cudaPano.h:101-103
- *   hmp_stitcher_canvas_* <- canvas_width() / canvas_height()        src/pano/cudaPano.h:105-111
+ *   hmp_stitcher_status   <- CudaStitchPano*::status()               src/pano/cudaPano.h:91-93
+ *   hmp_stitcher_canvas_* <- canvas_width() / canvas_height()        src/pano/cudaPano.h:79-85
+ *   hmp_stitcher_dump_pyramid <- CudaStitchPano::dump_soft_blend_pyramid(directory, stream)
+ *                                                                    src/pano/cudaPano.h:101
  *   hmp_stitcher_destroy  <- ~CudaStitchPano*()
  *
  * Error convention (src/cuda/cudaStatus.h:12-75): every call returns an hmp_status whose code is
@@ -69,6 +71,7 @@ extern "C" {
 #define HMP_ERR_FILE_NOT_FOUND 301     /* cudaErrorFileNotFound: masks not loaded (cudaPano.inl:28-31) */
 #define HMP_ERR_NOT_SUPPORTED 801      /* cudaErrorNotSupported */
 #define HMP_ERR_TIMEOUT 909            /* cudaErrorTimeout: a bounded wait gave up */
+#define HMP_ERR_UNKNOWN 999            /* cudaErrorUnknown: a file or directory could not be written */
 
 typedef struct hmp_status {
   int code;          /* cudaError_t value, 0 = success */
@@ -149,6 +152,17 @@ HMP_API hmp_status hmp_stitcher_get_info(const hmp_stitcher* st, hmp_stitcher_in
  * legacy default stream). Every canvas pixel is written, so the canvas needs no clearing. */
 HMP_API hmp_status hmp_stitcher_process(hmp_stitcher* st, const hmp_image* inputs, int n_inputs,
                                         const hmp_image* canvas, void* stream);
+
+/* Replaces CudaStitchPano::dump_soft_blend_pyramid(directory, stream) (src/pano/cudaPano.h:101,
+ * src/pano/cudaPano.inl:420-458): synchronises `stream`, then writes the soft-blend pyramid of the
+ * last process() under `directory`: metadata.txt (num_levels, batch_size, channels, level_<l>=WxH)
+ * and float32 TIFF files gauss1, gauss2, lap1, lap2, blend, reconstruct
+ * `<label>/level_<l>_batch_<b>.tiff` (RGBA) and `mask/level_<l>.tiff` (weight of image 1). The
+ * per-frame kernels keep these levels on chip, so the dump recomputes them from the last call's
+ * frames, which must still hold their contents. Two-image stitchers with the reference box filter;
+ * HMP_ERR_INVALID_VALUE when num_levels is 0 or no frame was processed yet, HMP_ERR_UNKNOWN when a
+ * file cannot be written. A debugging call: it allocates and synchronises. */
+HMP_API hmp_status hmp_stitcher_dump_pyramid(hmp_stitcher* st, const char* directory, void* stream);
 
 /* Tile edges of the pyramid kernels (a tuning knob, results are identical for every choice):
  * tile_down 32 or 64 level-0 pixels (a multiple of 2^(levels-1)), tile_coarse 32 level-1

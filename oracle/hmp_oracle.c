@@ -379,6 +379,10 @@ void hmpo_blend_nway_f32(const float* const* laps, int n, const float* mask, int
   blend_nway_f32(laps, n, mask, w, h, out, 1);
 }
 
+void hmpo_blend_two_f32(const float* l1, const float* l2, const float* mask, int w, int h, float* out) {
+  blend_two_f32(l1, l2, mask, w, h, out, 1);
+}
+
 int hmpo_laplacian_blend_f32(const float* const* inputs, int n, const float* mask, int k, int w, int h, int levels,
                              int rule, float* out) {
   if (n < 2 || n > 8 || levels < 1)

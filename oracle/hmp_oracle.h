@@ -95,6 +95,8 @@ void hmpo_reconstruct_rgba_f32(const float* low, const float* lap, int hw, int h
 void hmpo_downsample_mask_f32(const float* in, int iw, int ih, int k, float* out);
 /* Level-wise N-way blend with a K=n mask (cudaBlendN.cu:199-288). */
 void hmpo_blend_nway_f32(const float* const* laps, int n, const float* mask, int w, int h, float* out);
+/* Two-image blend of one level (src/cuda/cudaBlend.cu:520-576), mask = weight of image 1. */
+void hmpo_blend_two_f32(const float* l1, const float* l2, const float* mask, int w, int h, float* out);
 /* Full Laplacian blend of n full buffers (rule: 2 = two-image, 3 = three-image, 1 = N-way). */
 int hmpo_laplacian_blend_f32(const float* const* inputs, int n, const float* mask, int k, int w, int h, int levels,
                              int rule, float* out);

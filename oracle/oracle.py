@@ -73,6 +73,7 @@ def lib() -> C.CDLL:
         L.hmpo_downsample_rgba_f32.argtypes = [P(C.c_float), C.c_int, C.c_int, P(C.c_float)]
         L.hmpo_laplacian_rgba_f32.argtypes = [P(C.c_float), C.c_int, C.c_int, P(C.c_float), P(C.c_float)]
         L.hmpo_reconstruct_rgba_f32.argtypes = [P(C.c_float), P(C.c_float), C.c_int, C.c_int, P(C.c_float)]
+        L.hmpo_blend_two_f32.argtypes = [P(C.c_float), P(C.c_float), P(C.c_float), C.c_int, C.c_int, P(C.c_float)]
         L.hmpo_downsample_mask_f32.argtypes = [P(C.c_float), C.c_int, C.c_int, C.c_int, P(C.c_float)]
         L.hmpo_set_threads.argtypes = [C.c_int]
         L.hmpo_get_threads.restype = C.c_int
@@ -185,6 +186,18 @@ def reconstruct_rgba(low: np.ndarray, lap: np.ndarray) -> np.ndarray:
     h, w = lap.shape[-3], lap.shape[-2]
     out = np.zeros((h, w, 4), dtype=np.float32)
     lib().hmpo_reconstruct_rgba_f32(_ptr(low, C.c_float), _ptr(lap, C.c_float), w, h, _ptr(out, C.c_float))
+    return out
+
+
+def blend_two_rgba(l1: np.ndarray, l2: np.ndarray, mask: np.ndarray) -> np.ndarray:
+    """One level of the two-image blend; mask [h, w] (or [h, w, 1]) is the weight of image 1."""
+    l1 = np.ascontiguousarray(l1, dtype=np.float32)
+    l2 = np.ascontiguousarray(l2, dtype=np.float32)
+    mask = np.ascontiguousarray(mask, dtype=np.float32)
+    h, w = l1.shape[-3], l1.shape[-2]
+    out = np.zeros((h, w, 4), dtype=np.float32)
+    lib().hmpo_blend_two_f32(_ptr(l1, C.c_float), _ptr(l2, C.c_float), _ptr(mask, C.c_float), w, h,
+                             _ptr(out, C.c_float))
     return out
 
 
