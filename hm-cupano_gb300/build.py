@@ -33,6 +33,7 @@ UNITS = {
     "hmp_noalloc.cu": ["-fmad=false"],
     "hmp_binomial.cu": ["-fmad=false"],
     "hmp_server.cpp": [],
+    "hmp_control_dir.cpp": [],
 }
 HEADERS = ["hmp_plan.h", "hmp_device.cuh", "hmp_kernels.h", "hmp_blend.cuh", "hmp_admission.h"]
 

@@ -15,7 +15,10 @@ from .pano import (
     CudaStitchPanoN,
     SpatialTiff,
     StitchServer,
+    load_control_dir,
     plan_geometry,
+    read_seam_png,
+    read_tiff_u16,
 )
 
 __all__ = [
@@ -30,5 +33,8 @@ __all__ = [
     "SpatialTiff",
     "StitchServer",
     "UNMAPPED_POSITION_VALUE",
+    "load_control_dir",
     "plan_geometry",
+    "read_seam_png",
+    "read_tiff_u16",
 ]

@@ -102,6 +102,23 @@ class ServerStats(C.Structure):
     ]
 
 
+class ControlDir(C.Structure):
+    _fields_ = [
+        ("kind", C.c_int),
+        ("n", C.c_int),
+        ("map_width", C.c_int * 8),
+        ("map_height", C.c_int * 8),
+        ("map_x", C.POINTER(C.c_uint16) * 8),
+        ("map_y", C.POINTER(C.c_uint16) * 8),
+        ("xpos", C.c_float * 8),
+        ("ypos", C.c_float * 8),
+        ("seam_width", C.c_int),
+        ("seam_height", C.c_int),
+        ("seam", C.POINTER(C.c_uint8)),
+        ("internal", C.c_void_p),
+    ]
+
+
 # Every symbol include/hmpano.h declares, with its signature.
 SIGNATURES = {
     "hmp_version": ([], C.c_char_p),
@@ -129,6 +146,11 @@ SIGNATURES = {
     "hmp_server_reset_stats": ([C.c_void_p], None),
     "hmp_blend2_noalloc": ([C.POINTER(Image), C.POINTER(Image), C.c_void_p, C.c_size_t, C.c_int, C.c_int,
                             C.POINTER(Image), C.c_void_p], Status),
+    "hmp_control_dir_load": ([C.c_char_p, C.c_int, C.c_int, C.POINTER(C.POINTER(ControlDir))], Status),
+    "hmp_control_dir_free": ([C.POINTER(ControlDir)], None),
+    "hmp_read_seam_png": ([C.c_char_p, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int), C.c_void_p,
+                           C.c_size_t], Status),
+    "hmp_read_tiff_u16": ([C.c_char_p, C.POINTER(C.c_int), C.POINTER(C.c_int), C.c_void_p, C.c_size_t], Status),
 }
 
 NOALLOC_SCRATCH_BYTES = 48 * 1024 * 1024  # HMP_NOALLOC_SCRATCH_BYTES

@@ -57,6 +57,62 @@ def _normalize_positions(positions: Sequence[SpatialTiff]) -> list[tuple[int, in
     return [(int(p.xpos), int(p.ypos)) for p in positions]
 
 
+def load_control_dir(directory, kind: int, n_images: int = 0) -> dict:
+    """Read a control directory through hmp_control_dir_load (src/pano/controlMasks.cpp:133-326 and
+    its three- and N-image forms): {"map_x": [...], "map_y": [...], "positions": [SpatialTiff],
+    "seam": array}, the seam processed for `kind`. Raises CudaStatusError on failure."""
+    L = _lib.lib()
+    out = C.POINTER(_lib.ControlDir)()
+    s = _status(L.hmp_control_dir_load(str(directory).encode(), kind, n_images, C.byref(out)))
+    if not s.ok():
+        raise CudaStatusError(s)
+    try:
+        d = out.contents
+
+        def arr(ptr, h, w, dtype):
+            return np.ctypeslib.as_array(ptr, shape=(h, w)).astype(dtype, copy=True)
+
+        n = d.n
+        return {
+            "map_x": [arr(d.map_x[i], d.map_height[i], d.map_width[i], np.uint16) for i in range(n)],
+            "map_y": [arr(d.map_y[i], d.map_height[i], d.map_width[i], np.uint16) for i in range(n)],
+            "positions": [SpatialTiff(float(d.xpos[i]), float(d.ypos[i])) for i in range(n)],
+            "seam": arr(d.seam, d.seam_height, d.seam_width, np.uint8),
+        }
+    finally:
+        L.hmp_control_dir_free(out)
+
+
+def read_seam_png(path) -> tuple[np.ndarray, bool]:
+    """Decode a seam PNG: (palette indices or grayscale [h, w] uint8, whether it was 8-bit paletted)."""
+    L = _lib.lib()
+    w, h, pal = C.c_int(), C.c_int(), C.c_int()
+    s = _status(L.hmp_read_seam_png(str(path).encode(), C.byref(w), C.byref(h), C.byref(pal), None, 0))
+    if not s.ok():
+        raise CudaStatusError(s)
+    out = np.empty((h.value, w.value), np.uint8)
+    s = _status(L.hmp_read_seam_png(str(path).encode(), C.byref(w), C.byref(h), C.byref(pal),
+                                    out.ctypes.data_as(C.c_void_p), out.size))
+    if not s.ok():
+        raise CudaStatusError(s)
+    return out, bool(pal.value)
+
+
+def read_tiff_u16(path) -> np.ndarray:
+    """Decode a single-channel 16-bit TIFF (a coordinate table)."""
+    L = _lib.lib()
+    w, h = C.c_int(), C.c_int()
+    s = _status(L.hmp_read_tiff_u16(str(path).encode(), C.byref(w), C.byref(h), None, 0))
+    if not s.ok():
+        raise CudaStatusError(s)
+    out = np.empty((h.value, w.value), np.uint16)
+    s = _status(L.hmp_read_tiff_u16(str(path).encode(), C.byref(w), C.byref(h), out.ctypes.data_as(C.c_void_p),
+                                    out.size))
+    if not s.ok():
+        raise CudaStatusError(s)
+    return out
+
+
 @dataclass
 class ControlMasks:
     """Two-image control data (src/pano/controlMasks.h:30-66)."""
@@ -81,6 +137,25 @@ class ControlMasks:
     def _tables(self):
         return [self.img1_col, self.img2_col], [self.img1_row, self.img2_row], self.whole_seam_mask_image
 
+    def load(self, game_dir) -> bool:
+        """Read mapping_000{0,1}{,_x,_y}.tif and seam_file.png (src/pano/controlMasks.cpp:265-326); the
+        seam is inverted (smallest value -> 1 = image 1). False if anything is missing or invalid."""
+        try:
+            d = load_control_dir(game_dir, _lib.KIND_PANO2)
+        except CudaStatusError:
+            return False
+        self.img1_col, self.img2_col = d["map_x"]
+        self.img1_row, self.img2_row = d["map_y"]
+        self.whole_seam_mask_image = d["seam"]
+        self.positions = d["positions"]
+        return self.is_valid()
+
+    @classmethod
+    def from_directory(cls, game_dir) -> "ControlMasks":
+        m = cls()
+        m.load(game_dir)
+        return m
+
 
 @dataclass
 class ControlMasks3:
@@ -102,6 +177,25 @@ class ControlMasks3:
     def _tables(self):
         return ([self.img0_col, self.img1_col, self.img2_col], [self.img0_row, self.img1_row, self.img2_row],
                 self.whole_seam_mask_image)
+
+    def load(self, game_dir) -> bool:
+        """Read mapping_000{0,1,2}{,_x,_y}.tif and seam_file.png (src/pano/controlMasks3.cpp:219-300); the
+        seam must be 8-bit paletted with labels 0, 1, 2."""
+        try:
+            d = load_control_dir(game_dir, _lib.KIND_PANO3)
+        except CudaStatusError:
+            return False
+        self.img0_col, self.img1_col, self.img2_col = d["map_x"]
+        self.img0_row, self.img1_row, self.img2_row = d["map_y"]
+        self.whole_seam_mask_image = d["seam"]
+        self.positions = d["positions"]
+        return self.is_valid()
+
+    @classmethod
+    def from_directory(cls, game_dir) -> "ControlMasks3":
+        m = cls()
+        m.load(game_dir)
+        return m
 
 
 @dataclass
@@ -129,6 +223,25 @@ class ControlMasksN:
 
     def _tables(self):
         return list(self.img_col), list(self.img_row), self.whole_seam_mask_indexed
+
+    def load(self, directory, n_images: int) -> bool:
+        """Read mapping_%04d{,_x,_y}.tif for n_images images and seam_file.png
+        (src/pano/controlMasksN.cpp:126-193); seam values are remapped to 0..n_images-1 and must
+        number exactly n_images."""
+        try:
+            d = load_control_dir(directory, _lib.KIND_PANON, n_images)
+        except CudaStatusError:
+            return False
+        self.img_col, self.img_row = d["map_x"], d["map_y"]
+        self.whole_seam_mask_indexed = d["seam"]
+        self.positions = d["positions"]
+        return self.is_valid()
+
+    @classmethod
+    def from_directory(cls, directory, n_images: int) -> "ControlMasksN":
+        m = cls()
+        m.load(directory, n_images)
+        return m
 
 
 _STORAGE = {"f32": _lib.STORAGE_F32, "fp32": _lib.STORAGE_F32, "f16": _lib.STORAGE_F16, "fp16": _lib.STORAGE_F16}

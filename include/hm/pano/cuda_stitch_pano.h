@@ -20,6 +20,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <cstdio>
 #include <cstring>
 #include <memory>
 #include <stdexcept>
@@ -175,10 +176,56 @@ struct SpatialTiff {
   float ypos{0};
 };
 
+namespace detail {
+
+// Reads a control directory through hmp_control_dir_load; false (with the reason on stderr, as
+// the reference loaders print it) when a file is missing or invalid.
+inline bool load_control_dir(const std::string& dir, int kind, int n_images, std::vector<HostImage<uint16_t>>& cols,
+                             std::vector<HostImage<uint16_t>>& rows, HostImage<uint8_t>& seam,
+                             std::vector<SpatialTiff>& positions) {
+  hmp_control_dir* d = nullptr;
+  const hmp_status s = hmp_control_dir_load(dir.c_str(), kind, n_images, &d);
+  if (s.code != HMP_OK) {
+    std::fprintf(stderr, "Unable to load control directory %s: %s\n", dir.c_str(), s.message);
+    return false;
+  }
+  const auto copy = [](const auto* p, int w, int h, auto& img) {
+    img.cols = w;
+    img.rows = h;
+    img.data.assign(p, p + size_t(w) * h);
+  };
+  cols.assign(size_t(d->n), {});
+  rows.assign(size_t(d->n), {});
+  positions.clear();
+  for (int i = 0; i < d->n; ++i) {
+    copy(d->map_x[i], d->map_width[i], d->map_height[i], cols[size_t(i)]);
+    copy(d->map_y[i], d->map_width[i], d->map_height[i], rows[size_t(i)]);
+    positions.push_back(SpatialTiff{d->xpos[i], d->ypos[i]});
+  }
+  copy(d->seam, d->seam_width, d->seam_height, seam);
+  hmp_control_dir_free(d);
+  return true;
+}
+
+}  // namespace detail
+
+// Control data of a stitcher: the tables, the seam and the canvas positions. load() reads a
+// control directory (mapping_000i{,_x,_y}.tif and seam_file.png, controlMasks.cpp:265-326).
 struct ControlMasks {
   HostImage<uint16_t> img1_col, img1_row, img2_col, img2_row;
   HostImage<uint8_t> whole_seam_mask_image;  // inverted: 1 = image 1 (controlMasks.cpp:225-250)
   std::vector<SpatialTiff> positions;
+  ControlMasks() = default;
+  explicit ControlMasks(const std::string& game_dir) { (void)load(game_dir); }
+  bool load(const std::string& game_dir) {
+    std::vector<HostImage<uint16_t>> c, r;
+    if (!detail::load_control_dir(game_dir, HMP_KIND_PANO2, 2, c, r, whole_seam_mask_image, positions)) return false;
+    img1_col = std::move(c[0]);
+    img2_col = std::move(c[1]);
+    img1_row = std::move(r[0]);
+    img2_row = std::move(r[1]);
+    return is_valid();
+  }
   bool is_valid() const {
     return !img1_col.empty() && !img1_row.empty() && !img2_col.empty() && !img2_row.empty() &&
            !whole_seam_mask_image.empty() && positions.size() == 2;
@@ -189,6 +236,19 @@ struct ControlMasks3 {
   HostImage<uint16_t> img0_col, img0_row, img1_col, img1_row, img2_col, img2_row;
   HostImage<uint8_t> whole_seam_mask_image;  // labels 0..2
   std::vector<SpatialTiff> positions;
+  ControlMasks3() = default;
+  explicit ControlMasks3(const std::string& game_dir) { (void)load(game_dir); }
+  bool load(const std::string& game_dir) {  // controlMasks3.cpp:219-300
+    std::vector<HostImage<uint16_t>> c, r;
+    if (!detail::load_control_dir(game_dir, HMP_KIND_PANO3, 3, c, r, whole_seam_mask_image, positions)) return false;
+    img0_col = std::move(c[0]);
+    img1_col = std::move(c[1]);
+    img2_col = std::move(c[2]);
+    img0_row = std::move(r[0]);
+    img1_row = std::move(r[1]);
+    img2_row = std::move(r[2]);
+    return is_valid();
+  }
   bool is_valid() const {
     return !img0_col.empty() && !img1_col.empty() && !img2_col.empty() && !whole_seam_mask_image.empty() &&
            positions.size() == 3;
@@ -199,6 +259,13 @@ struct ControlMasksN {
   std::vector<HostImage<uint16_t>> img_col, img_row;
   HostImage<uint8_t> whole_seam_mask_indexed;  // labels 0..N-1
   std::vector<SpatialTiff> positions;
+  ControlMasksN() = default;
+  ControlMasksN(const std::string& dir, int n_images) { (void)load(dir, n_images); }
+  bool load(const std::string& dir, int n_images) {  // controlMasksN.cpp:126-193
+    return detail::load_control_dir(dir, HMP_KIND_PANON, n_images, img_col, img_row, whole_seam_mask_indexed,
+                                    positions) &&
+           is_valid();
+  }
   bool is_valid() const {
     return !img_col.empty() && img_col.size() == img_row.size() && positions.size() == img_col.size() &&
            !whole_seam_mask_indexed.empty();

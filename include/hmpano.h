@@ -129,6 +129,40 @@ typedef struct hmp_stitcher_info {
   double device_bytes; /* device memory held by the stitcher */
 } hmp_stitcher_info;
 
+/* ---- Control directory (host only; no GPU needed) ----
+ * Replaces ControlMasks::load / ControlMasks3::load / ControlMasksN::load
+ * (src/pano/controlMasks.cpp:133-326, src/pano/controlMasks3.cpp:186-300,
+ * src/pano/controlMasksN.cpp:22-193): reads mapping_000i_x.tif / mapping_000i_y.tif (16-bit
+ * coordinate tables; uncompressed, LZW, Deflate or PackBits, strips or tiles), the XPosition /
+ * YPosition x resolution tags of mapping_000i.tif (normalised so that the smallest is 0) and
+ * seam_file.png (8-bit palette indices, else grayscale). The seam is processed as the reference
+ * does for `kind`: two images -> smallest value 1 (weight of image 1), largest 0; three images ->
+ * an 8-bit paletted seam with labels exactly 0, 1, 2; N images -> exactly n_images distinct values
+ * remapped to 0..n_images-1. Errors: HMP_ERR_FILE_NOT_FOUND for a missing file,
+ * HMP_ERR_NOT_SUPPORTED for an unsupported encoding, HMP_ERR_INVALID_VALUE otherwise. */
+typedef struct hmp_control_dir {
+  int kind;                  /* HMP_KIND_* the seam was processed for */
+  int n;                     /* images */
+  int map_width[8], map_height[8];
+  const uint16_t* map_x[8];  /* [map_height][map_width] source column, 65535 = unmapped */
+  const uint16_t* map_y[8];  /* source row */
+  float xpos[8], ypos[8];    /* canvas position of each table */
+  int seam_width, seam_height;
+  const uint8_t* seam;       /* [seam_height][seam_width] */
+  void* internal;            /* owner of the arrays */
+} hmp_control_dir;
+
+/* n_images is used for HMP_KIND_PANON (2 and 3 are implied by the other kinds). */
+HMP_API hmp_status hmp_control_dir_load(const char* directory, int kind, int n_images, hmp_control_dir** out);
+HMP_API void hmp_control_dir_free(hmp_control_dir* dir);
+
+/* The loader's decoders on their own: a seam PNG (palette indices if 8-bit paletted, else
+ * grayscale) and a single-channel 16-bit TIFF. With out == NULL only the size is returned;
+ * otherwise out must hold width * height samples (`capacity`). */
+HMP_API hmp_status hmp_read_seam_png(const char* path, int* width, int* height, int* paletted, uint8_t* out,
+                                     size_t capacity);
+HMP_API hmp_status hmp_read_tiff_u16(const char* path, int* width, int* height, uint16_t* out, size_t capacity);
+
 /* Library version string. */
 HMP_API const char* hmp_version(void);
 
