@@ -34,6 +34,10 @@ typedef struct {
 } geom_t;
 
 static int g_threads = 0;
+/* Pixel channels of the stitch in progress: 4 (RGBA) or 3 (RGB, no alpha: plain means, plain
+ * bilinear upsampling, blends without alpha tests, zero fill for out-of-range entries). The
+ * op-level entry points below always run with 4. */
+static int g_ch = 4;
 
 void hmpo_set_threads(int n) {
   g_threads = n;
@@ -281,7 +285,7 @@ int hmpo_blend_geometry(const hmpo_config* cfg, int* out9) {
 static void hard_seam(const hmpo_config* cfg, const geom_t* g, const uint8_t* const* inputs, const int* in_w,
                       const int* in_h, uint8_t* canvas) {
   const int W = g->canvas_w, H = g->canvas_h, n = cfg->n_images;
-  memset(canvas, 0, (size_t)W * H * 4 * cfg->batch);
+  memset(canvas, 0, (size_t)W * H * g_ch * cfg->batch);
   for (int b = 0; b < cfg->batch; ++b) {
 #pragma omp parallel for schedule(static)
     for (int y = 0; y < H; ++y)
@@ -300,8 +304,8 @@ static void hard_seam(const hmpo_config* cfg, const geom_t* g, const uint8_t* co
         const int sx = cfg->map_x[o][(size_t)ry * cfg->map_w[o] + rx];
         const int sy = cfg->map_y[o][(size_t)ry * cfg->map_w[o] + rx];
         if (sx < in_w[o] && sy < in_h[o])
-          memcpy(canvas + (((size_t)b * H + y) * W + x) * 4,
-                 inputs[o] + (((size_t)b * in_h[o] + sy) * in_w[o] + sx) * 4, 4);
+          memcpy(canvas + (((size_t)b * H + y) * W + x) * g_ch,
+                 inputs[o] + (((size_t)b * in_h[o] + sy) * in_w[o] + sx) * g_ch, g_ch);
       }
   }
 }
@@ -318,11 +322,9 @@ static void hard_seam(const hmpo_config* cfg, const geom_t* g, const uint8_t* co
 #undef REAL
 #undef SFX
 
-static int stitch_any(const hmpo_config* cfg, const uint8_t* const* inputs, const int* in_w, const int* in_h,
-                      uint8_t* canvas, int dbl) {
-  int rc = validate(cfg);
-  if (rc != HMPO_OK)
-    return rc;
+static int stitch_any_ch(const hmpo_config* cfg, const uint8_t* const* inputs, const int* in_w, const int* in_h,
+                         uint8_t* canvas, int dbl) {
+  int rc = HMPO_OK;
   for (int i = 0; i < cfg->n_images; ++i)
     if (!inputs[i] || in_w[i] <= 0 || in_h[i] <= 0 || in_w[i] >= 65535)
       return HMPO_EINVAL;
@@ -337,6 +339,21 @@ static int stitch_any(const hmpo_config* cfg, const uint8_t* const* inputs, cons
   }
   return dbl ? stitch_soft_f64(cfg, inputs, in_w, in_h, canvas, NULL)
              : stitch_soft_f32(cfg, inputs, in_w, in_h, canvas, NULL);
+}
+
+static int stitch_any(const hmpo_config* cfg, const uint8_t* const* inputs, const int* in_w, const int* in_h,
+                      uint8_t* canvas, int dbl) {
+  int rc = validate(cfg);
+  if (rc != HMPO_OK)
+    return rc;
+  if (cfg->channels != 0 && cfg->channels != 3 && cfg->channels != 4)
+    return HMPO_EINVAL;
+  if (cfg->channels == 3 && cfg->filter != HMPO_FILTER_REFBOX)
+    return HMPO_EINVAL;
+  g_ch = cfg->channels == 3 ? 3 : 4;
+  rc = stitch_any_ch(cfg, inputs, in_w, in_h, canvas, dbl);
+  g_ch = 4;
+  return rc;
 }
 
 int hmpo_stitch_f32(const hmpo_config* cfg, const uint8_t* const* inputs, const int* in_w, const int* in_h,

@@ -66,6 +66,7 @@ typedef struct hmpo_config {
   const uint8_t* seam; /* PANO2: inverted seam (1 = image 1); PANO3/PANON: labels */
   int seam_w;
   int seam_h;
+  int channels; /* pixel channels of frames and canvas: 4 (RGBA; 0 means 4) or 3 (RGB, box filter only) */
 } hmpo_config;
 
 /* Canvas size = max(pos + map size) (src/pano/controlMasks.cpp:265-271). */

@@ -11,7 +11,7 @@
 #define CAT(a, b) CAT2(a, b)
 #define FN(name) CAT(name, SFX)
 
-/* Alpha-aware 2x2 box downsample of a batch of RGBA images.
+/* Alpha-aware 2x2 box downsample of a batch of RGBA images (3-channel pixels: the plain mean).
  * src/cuda/cudaBlend.cu:46-144 (2-image), cudaBlendN.cu:53-113 (N), cudaBlend3.cu:100-215 (3):
  * over in-bounds (2x+dx, 2y+dy), dy outer / dx inner; alpha is max-pooled; rgb is the mean
  * over pixels with alpha != 0 (0 if none). */
@@ -24,6 +24,25 @@ static void FN(down_rgba)(const REAL* in, int iw, int ih, REAL* out, int ow, int
       for (int x = 0; x < ow; ++x) {
         REAL s0 = 0, s1 = 0, s2 = 0, amax = 0;
         int cnt = 0;
+        if (g_ch == 3) { /* no alpha: the mean of the in-bounds pixels */
+          for (int dy = 0; dy < 2; ++dy)
+            for (int dx = 0; dx < 2; ++dx) {
+              const int ix = 2 * x + dx, iy = 2 * y + dy;
+              if (ix >= iw || iy >= ih)
+                continue;
+              const REAL* p = src + ((size_t)iy * iw + ix) * 4;
+              s0 += p[0];
+              s1 += p[1];
+              s2 += p[2];
+              ++cnt;
+            }
+          REAL* o = dst + ((size_t)y * ow + x) * 4;
+          o[0] = s0 / (REAL)cnt;
+          o[1] = s1 / (REAL)cnt;
+          o[2] = s2 / (REAL)cnt;
+          o[3] = 0;
+          continue;
+        }
         for (int dy = 0; dy < 2; ++dy) {
           for (int dx = 0; dx < 2; ++dx) {
             const int ix = 2 * x + dx, iy = 2 * y + dy;
@@ -98,6 +117,14 @@ static inline void FN(up_alpha)(const REAL* low, int lw, int lh, int x, int y, R
   const REAL w[4] = {(one - dx) * (one - dy), dx * (one - dy), (one - dx) * dy, dx * dy};
   const REAL* p[4] = {low + ((size_t)gyi * lw + gxi) * 4, low + ((size_t)gyi * lw + gxi1) * 4,
                       low + ((size_t)gyi1 * lw + gxi) * 4, low + ((size_t)gyi1 * lw + gxi1) * 4};
+  if (g_ch == 3) { /* no alpha: separable bilinear, x then y (cudaBlend.cu:445-448) */
+    for (int c = 0; c < 3; ++c) {
+      const REAL v0 = p[0][c] * (one - dx) + p[1][c] * dx;
+      const REAL v1 = p[2][c] * (one - dx) + p[3][c] * dx;
+      out3[c] = v0 * (one - dy) + v1 * dy;
+    }
+    return;
+  }
   for (int c = 0; c < 3; ++c) {
     REAL sw = 0, sv = 0;
     for (int t = 0; t < 4; ++t) {
@@ -167,6 +194,15 @@ static void FN(blend_two)(const REAL* l1, const REAL* l2, const REAL* mask, int 
         REAL* o = out + off + i * 4;
         const REAL m = mask[i];
         const REAL mm1 = (REAL)1 - m;
+        if (g_ch == 3) { /* no alpha bypass */
+          for (int ch = 0; ch < 3; ++ch) {
+            const REAL t1 = m * a[ch];
+            const REAL t2 = mm1 * c[ch];
+            o[ch] = t1 + t2;
+          }
+          o[3] = 0;
+          continue;
+        }
         if (a[3] == 0) {
           o[0] = c[0];
           o[1] = c[1];
@@ -202,6 +238,16 @@ static void FN(blend_three)(const REAL* const* laps, const REAL* mask, int w, in
         const REAL* L[3] = {laps[0] + off + i * 4, laps[1] + off + i * 4, laps[2] + off + i * 4};
         REAL* o = out + off + i * 4;
         REAL m[3] = {mask[i * 3 + 0], mask[i * 3 + 1], mask[i * 3 + 2]};
+        if (g_ch == 3) { /* no alpha: the raw weights, not normalised (cudaBlend3.cu:468-480) */
+          for (int c = 0; c < 3; ++c) {
+            const REAL t0 = m[0] * L[0][c];
+            const REAL t1 = m[1] * L[1][c];
+            const REAL t2 = m[2] * L[2][c];
+            o[c] = (t0 + t1) + t2;
+          }
+          o[3] = 0;
+          continue;
+        }
         for (int k = 0; k < 3; ++k)
           if (L[k][3] == 0)
             m[k] = 0;
@@ -256,6 +302,19 @@ static void FN(blend_nway)(const REAL* const* laps, int n, const REAL* mask, int
         if (sumw > 0)
           for (int k = 0; k < n; ++k)
             wt[k] /= sumw;
+        if (g_ch == 3) { /* no alpha: the normalised weights as they are */
+          REAL* o3 = out + off + i * 4;
+          for (int c = 0; c < 3; ++c) {
+            REAL acc = 0;
+            for (int k = 0; k < n; ++k) {
+              const REAL t = wt[k] * laps[k][off + i * 4 + c];
+              acc += t;
+            }
+            o3[c] = acc;
+          }
+          o3[3] = 0;
+          continue;
+        }
         REAL sumw2 = 0, amax = 0;
         int aidx = -1;
         for (int k = 0; k < n; ++k) {
@@ -547,7 +606,7 @@ static void FN(remap_into)(const uint8_t* src, int sw, int sh, const uint16_t* m
                            int roi_x, int roi_y, int roi_w, int roi_h, int off_x, int off_y, REAL* dst, int dw,
                            int dh, int batch, int skip_invalid) {
   for (int b = 0; b < batch; ++b) {
-    const uint8_t* S = src + (size_t)b * sw * sh * 4;
+    const uint8_t* S = src + (size_t)b * sw * sh * g_ch;
     REAL* D = dst + (size_t)b * dw * dh * 4;
 #pragma omp parallel for schedule(static)
     for (int y = 0; y < roi_h; ++y)
@@ -561,14 +620,14 @@ static void FN(remap_into)(const uint8_t* src, int sw, int sh, const uint16_t* m
         const int sx = mx[(size_t)myp * mw + mxp], sy = my[(size_t)myp * mw + mxp];
         REAL* o = D + ((size_t)dy * dw + dx) * 4;
         if (sx < sw && sy < sh) {
-          const uint8_t* p = S + ((size_t)sy * sw + sx) * 4;
+          const uint8_t* p = S + ((size_t)sy * sw + sx) * g_ch;
           o[0] = p[0];
           o[1] = p[1];
           o[2] = p[2];
-          o[3] = p[3];
+          o[3] = g_ch == 4 ? p[3] : 0;
         } else if (!skip_invalid) {
           o[0] = o[1] = o[2] = 0;
-          o[3] = sx == 65535 ? (REAL)0 : (REAL)255;
+          o[3] = (sx == 65535 || g_ch == 3) ? (REAL)0 : (REAL)255;
         }
       }
   }
@@ -589,7 +648,7 @@ static void FN(paste)(const REAL* src, int sw, int sh, int region_w, int region_
                       uint8_t* canvas, int cw, int ch, int off_x, int off_y, int batch) {
   for (int b = 0; b < batch; ++b) {
     const REAL* S = src + (size_t)b * sw * sh * 4;
-    uint8_t* C = canvas + (size_t)b * cw * ch * 4;
+    uint8_t* C = canvas + (size_t)b * cw * ch * g_ch;
 #pragma omp parallel for schedule(static)
     for (int y = 0; y < region_h; ++y)
       for (int x = 0; x < region_w; ++x) {
@@ -599,8 +658,8 @@ static void FN(paste)(const REAL* src, int sw, int sh, int region_w, int region_
         const int dx = off_x + x, dy = off_y + y;
         if (dx < 0 || dy < 0 || dx >= cw || dy >= ch)
           continue;
-        for (int c = 0; c < 4; ++c)
-          C[((size_t)dy * cw + dx) * 4 + c] = FN(pack)(S[((size_t)sy * sw + sx) * 4 + c]);
+        for (int c = 0; c < g_ch; ++c)
+          C[((size_t)dy * cw + dx) * g_ch + c] = FN(pack)(S[((size_t)sy * sw + sx) * 4 + c]);
       }
   }
 }
@@ -676,8 +735,9 @@ static int FN(stitch_soft)(const hmpo_config* cfg, const uint8_t* const* inputs,
             }
         /* Canvas outside the blend strip: image 2 over image 1 (uint8 copies). */
         if (canvas)
-          for (size_t p = 0; p < (size_t)W * H * 4 * B; ++p)
-            canvas[p] = FN(pack)(cv[p]);
+          for (size_t p = 0; p < (size_t)W * H * B; ++p)
+            for (int c = 0; c < g_ch; ++c)
+              canvas[p * g_ch + c] = FN(pack)(cv[p * 4 + c]);
         free(cv);
       }
     } else if (cfg->kind == HMPO_KIND_PANON && g.minimized) {
@@ -694,7 +754,7 @@ static int FN(stitch_soft)(const hmpo_config* cfg, const uint8_t* const* inputs,
     } else {
       /* Full-canvas blend (PANO2/PANON without minimisation, PANO3). */
       if (canvas)
-        memset(canvas, 0, (size_t)W * H * 4 * B);
+        memset(canvas, 0, (size_t)W * H * g_ch * B);
       const int skip = cfg->kind == HMPO_KIND_PANO3 && cfg->fused3;
       for (int i = 0; i < n; ++i)
         FN(remap_into)(inputs[i], in_w[i], in_h[i], cfg->map_x[i], cfg->map_y[i], cfg->map_w[i], cfg->map_h[i], 0, 0,

@@ -52,6 +52,7 @@ class _Config(C.Structure):
         ("seam", C.POINTER(C.c_uint8)),
         ("seam_w", C.c_int),
         ("seam_h", C.c_int),
+        ("channels", C.c_int),
     ]
 
 
@@ -125,10 +126,14 @@ class Stitch:
         return {"blend": tuple(v[0:4]), "write": tuple(v[4:8]), "levels": v[8]}
 
     def _inputs(self, frames):
+        """Frames [batch, h, w, c] uint8 with c = 4 (RGBA) or 3 (RGB); sets the config's channels."""
         fr = [np.ascontiguousarray(f, dtype=np.uint8) for f in frames]
+        ch = fr[0].shape[-1] if fr and fr[0].ndim == 4 else 0
         for f in fr:
-            if f.ndim != 4 or f.shape[0] != self.batch or f.shape[3] != 4:
-                raise ValueError("frames must be [batch, h, w, 4] uint8")
+            if f.ndim != 4 or f.shape[0] != self.batch or f.shape[3] != ch or ch not in (3, 4):
+                raise ValueError("frames must be [batch, h, w, 4 or 3] uint8 with one channel count")
+        self.cfg.channels = ch
+        self.channels = ch
         ptrs = (C.POINTER(C.c_uint8) * self.n)(*[_ptr(f, C.c_uint8) for f in fr])
         ws = (C.c_int * self.n)(*[f.shape[2] for f in fr])
         hs = (C.c_int * self.n)(*[f.shape[1] for f in fr])
@@ -136,7 +141,7 @@ class Stitch:
 
     def run(self, frames, precision: str = "f32") -> np.ndarray:
         fr, ptrs, ws, hs = self._inputs(frames)
-        out = np.zeros((self.batch, self.canvas_h, self.canvas_w, 4), dtype=np.uint8)
+        out = np.zeros((self.batch, self.canvas_h, self.canvas_w, self.channels), dtype=np.uint8)
         fn = lib().hmpo_stitch_f32 if precision == "f32" else lib().hmpo_stitch_f64
         rc = fn(C.byref(self.cfg), ptrs, ws, hs, _ptr(out, C.c_uint8))
         if rc != 0:

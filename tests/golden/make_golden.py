@@ -17,7 +17,10 @@ reference's CUDA kernels divide by the count (src/cuda/cudaBlend.cu:268-296,
 src/cuda/cudaBlendN.cu:19-48), and so does the port's own non-workspace path. The generator
 writes the mean into ``buf``, which makes the workspace path equal to the non-workspace path
 and to the CUDA semantics. Without it, two-image blends with >= 2 levels extrapolate by the
-mask sum.
+mask sum. The same holds for ``_downsample_image_torch`` with 3-channel (RGB) pixels (its
+4-channel branch writes the mean into ``out``; the 3-channel branch returns ``out / count`` and
+leaves the 2x2 sum in ``out``, cupano/ops.py:445-492), and the same correction is applied, as the
+CUDA kernels divide by the count (src/cuda/cudaBlend.cu:46-144).
 
 The reference tree is only needed to regenerate the fixture; the tests read ``golden.npz``.
 """
@@ -72,6 +75,23 @@ def _cases():
         ("panon3_l3_full", pn3, 3, False, 1, 0.0, 23),
         ("panon4_l2_min_oob", pn4, 2, True, 1, 0.05, 24),
         ("panon4_l5_min_b2", pn4, 5, True, 2, 0.0, 25),
+    ]
+
+
+def _rgb_cases():
+    """3-channel (RGB, no alpha) cases: the same rigs with the frames' alpha dropped."""
+    p2 = dict(canvas_w=480, canvas_h=40, n=2, src_w=230, src_h=36, overlap=90, yaw_step_deg=50.0)
+    p2odd = dict(canvas_w=497, canvas_h=45, n=2, src_w=241, src_h=37, overlap=85, yaw_step_deg=50.0)
+    pn3 = dict(canvas_w=420, canvas_h=48, n=3, src_w=160, src_h=40, overlap=0.25, yaw_step_deg=40.0)
+    pn4 = dict(canvas_w=515, canvas_h=37, n=4, src_w=150, src_h=30, overlap=0.3, yaw_step_deg=35.0)
+    return [
+        ("rgb_pano2_l0", p2, 0, True, 1, 0.0, 31),
+        ("rgb_pano2_l3", p2, 3, True, 1, 0.0, 32),
+        ("rgb_pano2_l6_odd_oob", p2odd, 6, True, 1, 0.05, 33),
+        ("rgb_pano2_l4_full_b2", p2, 4, False, 2, 0.0, 34),
+        ("rgb_panon3_l0", pn3, 0, True, 1, 0.0, 35),
+        ("rgb_panon3_l3_min", pn3, 3, True, 1, 0.0, 36),
+        ("rgb_panon4_l5_full_b2", pn4, 5, False, 2, 0.05, 37),
     ]
 
 
@@ -185,6 +205,16 @@ def main() -> None:
         return result
 
     ref_ops._downsample_mask_torch = _downsample_mask_mean
+    _image_sum_only = ref_ops._downsample_image_torch
+
+    def _downsample_image_mean(image, out=None):
+        result = _image_sum_only(image, out=out)
+        if out is not None and result is not out:
+            out.copy_(result)
+            return out
+        return result
+
+    ref_ops._downsample_image_torch = _downsample_image_mean
 
     store: dict[str, np.ndarray] = {}
     names = []
@@ -210,6 +240,12 @@ def main() -> None:
         frames = [synth.make_frame(rig.src_w[i], rig.src_h[i], fseed * 10 + i, batch) for i in range(rig.n)]
         put(name, rig, frames, levels, minimize, batch)
     for name, rig, frames, levels, minimize, batch in _known_answer_cases(cupano):
+        put(name, rig, frames, levels, minimize, batch)
+    for name, params, levels, minimize, batch, oob, fseed in _rgb_cases():
+        kind = 2 if params["n"] == 2 else 1
+        rig = synth.make_rig(seed=zlib.crc32(name.encode()) % 10000 + 7, kind=kind, oob_fraction=oob, **params)
+        frames = [synth.make_frame(rig.src_w[i], rig.src_h[i], fseed * 10 + i, batch)[..., :3].copy()
+                  for i in range(rig.n)]
         put(name, rig, frames, levels, minimize, batch)
 
     # Op-level known answer: the alpha-renormalised Laplacian (test_pytorch_pano.py:192-201).
