@@ -34,6 +34,7 @@ UNITS = {
     "hmp_binomial.cu": ["-fmad=false"],
     "hmp_server.cpp": [],
     "hmp_control_dir.cpp": [],
+    "hmp_generic.cu": ["-fmad=false"],
 }
 HEADERS = ["hmp_plan.h", "hmp_device.cuh", "hmp_kernels.h", "hmp_blend.cuh", "hmp_admission.h"]
 

@@ -67,6 +67,31 @@ cudaError_t launch_dump_blend2(const float4* l0, const float4* l1, const float* 
 cudaError_t launch_dump_recon(const float4* lo, int lw, int lh, const float4* bl, int w, int h, float4* out, int batch,
                               cudaStream_t stream);
 
+// Level-by-level stitch of the uchar3 / float4 / float3 pipelines (hmp_generic.cu).
+struct GenArgs {
+  SrcSet S;  // frames; ptr is the first pixel of any sample type
+  PlaneDev slot[kDevMaxImages];
+  int n;
+  int levels;
+  int lw[kDevMaxLevels + 1];
+  int lh[kDevMaxLevels + 1];
+  float4* G[kDevMaxImages][kDevMaxLevels];  // level l of slot k (level 0 included), [batch][lh][lw]
+  const uint8_t* mask0;
+  int mask0_pitch;
+  const float* maskL[kDevMaxLevels];
+  int K;
+  int opaque;
+  CanvasDev C;             // ptr is the first pixel of any sample type
+  int wx0, wy0, wx1, wy1;  // write rect, blend coordinates, end exclusive
+  int cx_off, cy_off;      // canvas = blend + offset
+};
+// r[0], r[1]: reconstruction buffers of level-1 size (levels alternate between them).
+cudaError_t launch_generic_pyramid(const GenArgs& a, int channels, bool is_float, int rule, int batch,
+                                   float4* const* r, cudaStream_t stream);
+// The canvas outside g's skip rect from the raw (packed) canvas plane g.P.
+cudaError_t launch_generic_canvas(const GatherArgs& g, int channels, bool is_float, bool opaque, cudaStream_t stream);
+int generic_launches(int levels, bool canvas);
+
 // One-time attribute setup (dynamic shared memory limits). Call before capture.
 cudaError_t kernels_init();
 

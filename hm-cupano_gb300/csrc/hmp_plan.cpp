@@ -97,7 +97,12 @@ int validate(const hmp_config& c, std::string& m) {
     return fail(m, HMP_ERR_INVALID_VALUE, "Unsupported N for blend (supported 2..8)");
   if (c.num_levels < 0 || c.num_levels > 30) return fail(m, HMP_ERR_INVALID_VALUE, "num_levels out of range");
   if (c.batch_size < 1) return fail(m, HMP_ERR_INVALID_VALUE, "batch_size must be >= 1");
-  if (c.channels != 4) return fail(m, HMP_ERR_NOT_SUPPORTED, "only 4-channel (RGBA) pixels are supported");
+  if (c.channels != 4 && c.channels != 3) return fail(m, HMP_ERR_NOT_SUPPORTED, "only 3- and 4-channel pixels are supported");
+  if (c.pixel_format != HMP_PIXEL_U8 && c.pixel_format != HMP_PIXEL_F32)
+    return fail(m, HMP_ERR_INVALID_VALUE, "unknown pixel format");
+  if ((c.channels != 4 || c.pixel_format != HMP_PIXEL_U8) &&
+      (c.storage != HMP_STORAGE_F32 || c.filter != HMP_FILTER_REFBOX))
+    return fail(m, HMP_ERR_NOT_SUPPORTED, "FP16 storage and the Binomial5 filter are RGBA8-only");
   if (c.storage != HMP_STORAGE_F32 && c.storage != HMP_STORAGE_F16)
     return fail(m, HMP_ERR_INVALID_VALUE, "unknown pyramid storage");
   if (c.filter != HMP_FILTER_REFBOX && c.filter != HMP_FILTER_BINOMIAL5)
@@ -218,6 +223,8 @@ int plan_geometry(const hmp_config& c, Plan& p, std::string& m) {
   p.levels_requested = c.num_levels;
   p.storage = c.storage;
   p.filter = c.filter;
+  p.channels = c.channels;
+  p.pixel_float = c.pixel_format == HMP_PIXEL_F32;
   // Canvas = max(position + table size) (src/pano/controlMasks.cpp:265-271).
   for (int i = 0; i < p.n; ++i) {
     p.canvas_w = std::max(p.canvas_w, c.remaps[i].xpos + c.remaps[i].width);

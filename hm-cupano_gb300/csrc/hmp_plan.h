@@ -54,6 +54,11 @@ struct Plan {
   int filter = HMP_FILTER_REFBOX;
   int rule = kRuleTwo;
   int mask_k = 1;        // mask channels of the pyramid blend
+  int channels = 4;      // 4 (RGBA) or 3 (RGB)
+  bool pixel_float = false;  // float samples (HMP_PIXEL_F32) instead of uint8
+  // Everything but RGBA8 runs the level-by-level kernels (hmp_generic.cu).
+  bool generic() const { return channels != 4 || pixel_float; }
+  int pixel_bytes() const { return channels * (pixel_float ? 4 : 1); }
   bool minimized = false;
   bool slot_opaque = true;    // soft-seam rule: out-of-range, non-sentinel entries give alpha 255
   bool canvas_opaque = false; // same rule for the canvas plane

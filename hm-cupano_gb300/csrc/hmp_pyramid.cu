@@ -44,29 +44,6 @@ __device__ __forceinline__ void cp_async_commit_wait_all() {
   asm volatile("cp.async.wait_group 0;\n" ::: "memory");
 }
 
-// Alpha-aware 2x2 mean of four level-l pixels (src/cuda/cudaBlend.cu:46-144).
-struct DownAcc {
-  float s0 = 0.f, s1 = 0.f, s2 = 0.f, amax = 0.f;
-  int cnt = 0;
-  __device__ __forceinline__ void add(const float4 p) {
-    if (p.w > amax) amax = p.w;
-    if (p.w != 0.f) {
-      s0 += p.x;
-      s1 += p.y;
-      s2 += p.z;
-      ++cnt;
-    }
-  }
-  // s / count. Division by 1, 2 or 4 equals the (correctly rounded) product with 1, 0.5 or 0.25,
-  // so only a count of 3 needs a division.
-  __device__ __forceinline__ float4 result() const {
-    if (cnt == 4) return make_float4(s0 * 0.25f, s1 * 0.25f, s2 * 0.25f, amax);
-    if (cnt == 0) return make_float4(0.f, 0.f, 0.f, amax);
-    if (cnt == 2) return make_float4(s0 * 0.5f, s1 * 0.5f, s2 * 0.5f, amax);
-    if (cnt == 1) return make_float4(s0, s1, s2, amax);
-    return make_float4(s0 / 3.f, s1 / 3.f, s2 / 3.f, amax);
-  }
-};
 
 // Source pixel address of slot k for table entry e (owner o when the slot has an owner plane),
 // or nullptr with the pixel to store instead: zero, or alpha 255 under the soft-seam ("opaque")
@@ -471,58 +448,6 @@ __global__ void __launch_bounds__(256) pyr_down_n_kernel(const __grid_constant__
   }
 }
 
-// Alpha-aware bilinear upsample of a shared-memory region (origin ax, ay; row stride cw) of a
-// level of size lw x lh, sampled for high-res pixel (x, y): top-left aligned, gx = x/2, taps
-// floor and floor+1 clamped to the level, only taps with alpha != 0, renormalised
-// (src/cuda/cudaBlend.cu:389-455, 581-672). Callers order pixels so that the parity of (x, y) is
-// the same across a warp, which keeps the branches below uniform.
-//
-// Same bits as the reference, with less work. The weights are products of {1, 0.5}, so a tap of
-// weight 0 adds an exact zero and is skipped (the remaining taps keep their order; skipping can
-// only turn a -0 sum into +0, and the uint8 pack maps both to 0). Every other product v*w is
-// exact. The weight sum is 1, 0.5, 0.25 or 0.75; dividing by the first three is an exact scaling
-// by 1, 2 or 4, so only a 0.75 sum (three of four taps valid) needs a division.
-template <typename T>
-__device__ __forceinline__ float3 up_alpha(const T* buf, int cw, int ax, int ay, int lw, int lh, int x, int y) {
-  const int gxi = x >> 1, gyi = y >> 1;
-  const T* r0 = buf + (gyi - ay) * cw - ax;
-  const float4 p00 = load_level(r0 + gxi);
-  const bool ox = (x & 1) != 0, oy = (y & 1) != 0;
-  if (!ox && !oy) {
-    if (p00.w != 0.f) return make_float3(p00.x, p00.y, p00.z);
-    return make_float3(0.f, 0.f, 0.f);
-  }
-  if (ox != oy) {
-    // Two taps of weight 0.5: (00, 10) for odd x, (00, 01) for odd y.
-    const float4 p1 = ox ? load_level(r0 + min(gxi + 1, lw - 1)) : load_level(buf + (min(gyi + 1, lh - 1) - ay) * cw + (gxi - ax));
-    const bool v0 = p00.w != 0.f, v1 = p1.w != 0.f;
-    if (v0 && v1)  // (p00*0.5 + p1*0.5) / 1
-      return make_float3(p00.x * 0.5f + p1.x * 0.5f, p00.y * 0.5f + p1.y * 0.5f, p00.z * 0.5f + p1.z * 0.5f);
-    // (p*0.5) / 0.5: dividing by 0.5 is an exact doubling (kept explicit for subnormal p)
-    if (v0) return make_float3((p00.x * 0.5f) * 2.f, (p00.y * 0.5f) * 2.f, (p00.z * 0.5f) * 2.f);
-    if (v1) return make_float3((p1.x * 0.5f) * 2.f, (p1.y * 0.5f) * 2.f, (p1.z * 0.5f) * 2.f);
-    return make_float3(0.f, 0.f, 0.f);
-  }
-  // Four taps of weight 0.25.
-  const int gxi1 = min(gxi + 1, lw - 1), gyi1 = min(gyi + 1, lh - 1);
-  const T* r1 = buf + (gyi1 - ay) * cw - ax;
-  const float4 q[4] = {p00, load_level(r0 + gxi1), load_level(r1 + gxi), load_level(r1 + gxi1)};
-  float sw = 0.f, s0 = 0.f, s1 = 0.f, s2 = 0.f;
-#pragma unroll
-  for (int i = 0; i < 4; ++i) {
-    if (q[i].w != 0.f) {
-      sw += 0.25f;
-      s0 += q[i].x * 0.25f;
-      s1 += q[i].y * 0.25f;
-      s2 += q[i].z * 0.25f;
-    }
-  }
-  if (sw == 1.f) return make_float3(s0, s1, s2);
-  if (sw == 0.5f) return make_float3(s0 * 2.f, s1 * 2.f, s2 * 2.f);
-  if (sw == 0.25f) return make_float3(s0 * 4.f, s1 * 4.f, s2 * 4.f);
-  if (sw > 0.f) return make_float3(s0 / sw, s1 / sw, s2 / sw);
-  return make_float3(0.f, 0.f, 0.f);
-}
 
 // Shared-memory row stride and capacity (pixels) of level l >= 1 for an up-tile of edge TU: the
 // tile's footprint at that level plus the upsample halo.

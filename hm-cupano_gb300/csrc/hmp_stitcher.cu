@@ -133,6 +133,9 @@ struct hmp_stitcher {
   int launches = 0;
   hmp::SrcSet last_src{};  // frames of the last process(), for the pyramid dump
   bool have_last = false;
+  bool generic = false;    // uchar3 / float4 / float3 pixels: the level-by-level kernels
+  float4* G0[hmp::kDevMaxImages]{};  // generic: level 0 per slot
+  float4* Rg[2]{};                   // generic: reconstruction buffers (level-1 size)
   // Optional per-kernel event timing (hmp_stitcher_set_timing).
   static constexpr int kTimingSlots = 4096;
   static constexpr int kTimed = 4;
@@ -269,6 +272,7 @@ struct hmp_stitcher {
 
   hmp_status setup() {
     hmp::Plan& p = plan;
+    generic = p.generic();
     cudaError_t e = cudaGetDevice(&device);
     if (e != cudaSuccess) return cuda_status(e, "cudaGetDevice");
     e = hmp::kernels_init();
@@ -277,7 +281,7 @@ struct hmp_stitcher {
       e = upload_plane(p.canvas, canvas_plane);
       if (e != cudaSuccess) return cuda_status(e, "canvas plane upload");
       canvas_raw = canvas_plane;
-      if (canvas_plane.w > 0) {
+      if (canvas_plane.w > 0 && !p.generic()) {
         void* r = nullptr;
         e = alloc(&r, size_t(canvas_plane.map_pitch) * 4 * canvas_plane.h);
         if (e != cudaSuccess) return cuda_status(e, "canvas plane allocation");
@@ -330,6 +334,20 @@ struct hmp_stitcher {
           if (e != cudaSuccess) return cuda_status(e, "pyramid clear");
         }
       }
+      if (generic) {
+        for (int k = 0; k < n; ++k) {
+          void* q = nullptr;
+          e = alloc(&q, size_t(B) * p.lw[0] * p.lh[0] * sizeof(float4));
+          if (e != cudaSuccess) return cuda_status(e, "pyramid allocation");
+          G0[k] = static_cast<float4*>(q);
+        }
+        for (int i = 0; i < 2 && L > 1; ++i) {
+          void* q = nullptr;
+          e = alloc(&q, size_t(B) * p.lw[1] * p.lh[1] * sizeof(float4));
+          if (e != cudaSuccess) return cuda_status(e, "reconstruction buffer");
+          Rg[i] = static_cast<float4*>(q);
+        }
+      }
       // Tiles: level-0 edge a multiple of 2^(L-1); smaller up-tiles for many images keep the
       // per-CTA shared memory (n+1 images' worth of two levels) within the SM.
       const int align = 1 << (L - 1);
@@ -353,7 +371,7 @@ struct hmp_stitcher {
       coarse_cap = (n > 3 && L > 2) ? coarse_cap_for(tile_coarse) : 0;
       coarse_smem = coarse_smem_for(tile_coarse);
       b5 = p.filter == HMP_FILTER_BINOMIAL5 && L > 1;
-      if (L > 1 && !b5) {
+      if (L > 1 && !b5 && !generic) {
         void* r = nullptr;
         e = alloc(&r, size_t(B) * p.lw[1] * p.lh[1] * sizeof(float4));
         if (e != cudaSuccess) return cuda_status(e, "reconstruction buffer");
@@ -362,7 +380,7 @@ struct hmp_stitcher {
       // With three or more images pyr_down keeps the level-0 pixels for pyr_fine (one load per slot
       // instead of a table lookup and a gather); with two it measured slower (the extra writes
       // lengthen pyr_down more than they shorten pyr_fine), so pyr_fine gathers again.
-      use_p0 = L > 1 && !b5 && n >= 3;
+      use_p0 = L > 1 && !b5 && n >= 3 && !generic;
       fine_cap = (use_p0 && n > 3) ? fine_cap_for() : 0;
       for (int k = 0; use_p0 && k < n; ++k) {
         const hmp::PlaneDev& P = slot_planes[k];
@@ -384,7 +402,8 @@ struct hmp_stitcher {
         return make_status(HMP_ERR_NOT_SUPPORTED, "pyramid tile does not fit in shared memory");
       launches += b5 ? hmp::b5_launches(L) : (L > 1 ? 2 : 0) + 1;
     }
-    if (p.canvas_plane_used && p.levels > 0) {
+    if (generic) launches = hmp::generic_launches(p.levels, p.canvas_plane_used);
+    if (p.canvas_plane_used && p.levels > 0 && !generic) {
       // The pyramid chain (latency-bound, few CTAs) runs on a high-priority stream so that its
       // CTAs are dispatched ahead of the bandwidth-bound canvas gather sharing the SMs.
       int least = 0, greatest = 0;
@@ -412,20 +431,22 @@ struct hmp_stitcher {
     return ok_status();
   }
 
-  // Compulsory bytes per process(): outside the write rect, 4 (table) + 1 (seam) + 4 (source)
-  // + 4 (canvas) per canvas pixel; inside it, 4 + 4 per mapped slot pixel, 1 (seam) + 4 (canvas)
-  // per pixel. Tables and seam are read once per call, sources and canvas once per frame.
+  // Compulsory bytes per process(): outside the write rect, 4 (table) + 1 (seam) + a source and
+  // a canvas pixel per canvas pixel; inside it, 4 + a source pixel per mapped slot pixel, 1 (seam)
+  // + a canvas pixel per pixel (4 bytes for RGBA8). Tables and seam are read once per call,
+  // sources and canvas once per frame.
   void compute_m0() {
     const hmp::Plan& p = plan;
     const double B = p.batch;
     const double canvas_px = double(p.canvas_w) * p.canvas_h;
     const double a0 = p.levels > 0 ? double(p.write.w) * p.write.h : 0.0;
-    double bytes = (canvas_px - a0) * (5.0 + 8.0 * B);
+    const double px = p.pixel_bytes();
+    double bytes = (canvas_px - a0) * (5.0 + 2.0 * px * B);
     if (p.levels > 0) {
       double mapped = 0;
       for (const auto& s : p.slots)
         for (uint32_t e : s.map) mapped += e != hmp::kNoEntry;
-      bytes += mapped * (4.0 + 4.0 * B) + a0 * (1.0 + 4.0 * B);
+      bytes += mapped * (4.0 + px * B) + a0 * (1.0 + px * B);
     }
     m0_bytes = bytes;
   }
@@ -440,8 +461,9 @@ struct hmp_stitcher {
     if (!directory) return make_status(HMP_ERR_INVALID_VALUE, "directory is null");
     if (p.levels == 0)
       return make_status(HMP_ERR_INVALID_VALUE, "Soft-blend pyramid is only available when num_levels > 0");
-    if (p.rule != hmp::kRuleTwo || b5)
-      return make_status(HMP_ERR_NOT_SUPPORTED, "the pyramid dump covers the two-image stitcher with the box filter");
+    if (p.rule != hmp::kRuleTwo || b5 || generic)
+      return make_status(HMP_ERR_NOT_SUPPORTED,
+                         "the pyramid dump covers the two-image RGBA8 stitcher with the box filter");
     if (!have_last) return make_status(HMP_ERR_INVALID_VALUE, "No Laplacian workspace is populated yet: call process() first");
     int dev = -1;
     cudaGetDevice(&dev);
@@ -616,19 +638,77 @@ struct hmp_stitcher {
     return S;
   }
 
+  // uchar3 / float4 / float3 pixels: the canvas outside the write rect, then the pyramid level by
+  // level, all on the caller's stream (hmp_generic.cu).
+  hmp_status process_generic(const hmp::SrcSet& S, const hmp_image* canvas, cudaStream_t s) {
+    const hmp::Plan& p = plan;
+    hmp::CanvasDev C;
+    C.ptr = static_cast<uchar4*>(canvas->data);
+    C.pitch = (long long)canvas->pitch;
+    C.bstride = (long long)canvas->pitch * canvas->height;
+    C.w = canvas->width;
+    C.h = canvas->height;
+    cudaError_t e = cudaSuccess;
+    if (p.canvas_plane_used) {
+      hmp::GatherArgs g{};
+      g.S = S;
+      g.P = canvas_raw;
+      g.C = C;
+      g.batch = p.batch;
+      g.n_owners = p.n;
+      if (p.levels > 0) {
+        g.skip_x0 = p.write.x;
+        g.skip_y0 = p.write.y;
+        g.skip_x1 = p.write.x + p.write.w;
+        g.skip_y1 = p.write.y + p.write.h;
+      }
+      e = hmp::launch_generic_canvas(g, p.channels, p.pixel_float, p.canvas_opaque, s);
+      if (e != cudaSuccess) return cuda_status(e, "canvas launch");
+    }
+    if (p.levels > 0) {
+      hmp::GenArgs a{};
+      a.S = S;
+      for (int k = 0; k < p.n; ++k) a.slot[k] = slot_planes[k];
+      a.n = p.n;
+      a.levels = p.levels;
+      for (int l = 0; l < p.levels; ++l) {
+        a.lw[l] = p.lw[l];
+        a.lh[l] = p.lh[l];
+        a.maskL[l] = maskL[l];
+        for (int k = 0; k < p.n; ++k) a.G[k][l] = l == 0 ? G0[k] : static_cast<float4*>(G[k][l]);
+      }
+      a.mask0 = mask0;
+      a.mask0_pitch = mask0_pitch;
+      a.K = p.mask_k;
+      a.opaque = p.slot_opaque ? 1 : 0;
+      a.C = C;
+      a.wx0 = p.write.x - p.blend.x;
+      a.wy0 = p.write.y - p.blend.y;
+      a.wx1 = a.wx0 + p.write.w;
+      a.wy1 = a.wy0 + p.write.h;
+      a.cx_off = p.blend.x;
+      a.cy_off = p.blend.y;
+      e = hmp::launch_generic_pyramid(a, p.channels, p.pixel_float, p.rule, p.batch, Rg, s);
+      if (e != cudaSuccess) return cuda_status(e, "pyramid launch");
+    }
+    return ok_status();
+  }
+
   hmp_status process(const hmp_image* inputs, int n_inputs, const hmp_image* canvas, cudaStream_t s) {
     const hmp::Plan& p = plan;
     if (!inputs || n_inputs != p.n) return make_status(HMP_ERR_INVALID_VALUE, "inputs size != N");
     if (!canvas || !canvas->data) return make_status(HMP_ERR_INVALID_DEVICE_POINTER, "Canvas must be provided");
-    if (canvas->width != p.canvas_w || canvas->height != p.canvas_h || canvas->pitch < size_t(canvas->width) * 4)
+    const size_t pxb = size_t(p.pixel_bytes()), align = p.pixel_float ? 4 : (generic ? 1 : 4);
+    if (canvas->width != p.canvas_w || canvas->height != p.canvas_h || canvas->pitch < size_t(canvas->width) * pxb ||
+        canvas->pitch % align != 0)
       return make_status(HMP_ERR_INVALID_VALUE, "canvas size does not match the stitcher");
     for (int i = 0; i < n_inputs; ++i) {
       const hmp_image& im = inputs[i];
       if (!im.data) return make_status(HMP_ERR_INVALID_DEVICE_POINTER, "input image is null");
-      if (im.width <= 0 || im.height <= 0 || im.pitch < size_t(im.width) * 4 || im.pitch > size_t(INT_MAX) ||
-          im.pitch % 4 != 0)
+      if (im.width <= 0 || im.height <= 0 || im.pitch < size_t(im.width) * pxb || im.pitch > size_t(INT_MAX) ||
+          im.pitch % align != 0)
         return make_status(HMP_ERR_INVALID_VALUE, "input image has an invalid size or pitch");
-      if (size_t(im.height) * (im.pitch / 4) >= size_t(hmp::kOffMask) - 1)
+      if (!generic && size_t(im.height) * (im.pitch / 4) >= size_t(hmp::kOffMask) - 1)
         return make_status(HMP_ERR_NOT_SUPPORTED, "input frames must hold fewer than 2^29 - 2 pixels");
       if (im.width >= 65535 || im.height >= 65535)
         return make_status(HMP_ERR_INVALID_VALUE, "input images must be smaller than 65535 pixels per side");
@@ -640,6 +720,7 @@ struct hmp_stitcher {
     const hmp::SrcSet S = sources(inputs);
     last_src = S;
     have_last = true;
+    if (generic) return process_generic(S, canvas, s);
     if (p.canvas_plane_used) {
       // The gather reads the canvas plane as offsets into these frames: resolve it for their
       // geometry on the first call and whenever a size or pitch changes.

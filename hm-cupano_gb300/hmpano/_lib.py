@@ -15,6 +15,8 @@ LIB_PATH = Path(os.environ.get("HMPANO_LIB", PKG_ROOT / "lib" / "libhmpano.so"))
 KIND_PANON = 1
 KIND_PANO2 = 2
 KIND_PANO3 = 3
+PIXEL_U8 = 0
+PIXEL_F32 = 1
 STORAGE_F32 = 0
 STORAGE_F16 = 1
 FILTER_REFBOX = 0
@@ -51,6 +53,7 @@ class Config(C.Structure):
         ("seam", C.POINTER(C.c_uint8)),
         ("seam_width", C.c_int),
         ("seam_height", C.c_int),
+        ("pixel_format", C.c_int),
     ]
 
 

@@ -249,7 +249,8 @@ _FILTER = {"refbox": _lib.FILTER_REFBOX, "box": _lib.FILTER_REFBOX, "binomial5":
 
 
 def build_config(kind: int, control_masks, num_levels: int, batch_size: int, minimize_blend: bool = True,
-                 fused: bool = True, storage: str = "f32", filter: str = "refbox"):
+                 fused: bool = True, storage: str = "f32", filter: str = "refbox", channels: int = 4,
+                 float_pixels: bool = False):
     """Marshal control masks into an hmp_config; returns (config, keep-alive list)."""
     cols, rows, seam = control_masks._tables()
     positions = _normalize_positions(control_masks.positions)
@@ -266,10 +267,11 @@ def build_config(kind: int, control_masks, num_levels: int, batch_size: int, min
                           int(mx.shape[1]), int(mx.shape[0]), positions[i][0], positions[i][1])
     seam_u8 = np.ascontiguousarray(seam, dtype=np.uint8)
     keep += [seam_u8, remaps]
-    cfg = Config(kind, n, int(num_levels), int(batch_size), 4, int(bool(minimize_blend)), int(bool(fused)),
+    cfg = Config(kind, n, int(num_levels), int(batch_size), int(channels), int(bool(minimize_blend)), int(bool(fused)),
                  _STORAGE[storage.lower()], _FILTER[filter.lower()], remaps,
                  seam_u8.ctypes.data_as(C.POINTER(C.c_uint8)), int(seam_u8.shape[1]) if seam_u8.ndim == 2 else 0,
-                 int(seam_u8.shape[0]) if seam_u8.ndim == 2 else 0)
+                 int(seam_u8.shape[0]) if seam_u8.ndim == 2 else 0,
+                 _lib.PIXEL_F32 if float_pixels else _lib.PIXEL_U8)
     return cfg, keep
 
 
@@ -281,18 +283,25 @@ def _ensure_batched(t):
     return t
 
 
-def _image(t) -> Image:
-    """hmp_image over a [B, H, W, 4] uint8 CUDA tensor with dense rows and frames."""
+def _pixel_type(t) -> tuple[int, bool]:
+    """(channels, float samples) of a [.., H, W, C] tensor: uint8 or float32, 3 or 4 channels."""
     import torch
 
-    if t.dtype != torch.uint8 or t.shape[-1] != 4:
-        raise ValueError("images must be RGBA uint8 tensors [B, H, W, 4]")
+    if t.shape[-1] not in (3, 4) or t.dtype not in (torch.uint8, torch.float32):
+        raise ValueError("images must be uint8 or float32 tensors with 3 or 4 channels [B, H, W, C]")
+    return int(t.shape[-1]), t.dtype == torch.float32
+
+
+def _image(t) -> Image:
+    """hmp_image over a [B, H, W, C] CUDA tensor (C = 4 or 3; uint8 or float32) with dense pixels
+    and frames (the row pitch may exceed the row)."""
+    ch, _ = _pixel_type(t)
     if not t.is_cuda:
         raise ValueError("images must live on a CUDA device")
     B, H, W, _ = t.shape
-    if t.stride(3) != 1 or t.stride(2) != 4 or t.stride(0) != t.stride(1) * H:
-        raise ValueError("images need dense RGBA rows and frames (row pitch may exceed 4*W)")
-    return Image(C.c_void_p(t.data_ptr()), int(W), int(H), int(t.stride(1)))
+    if t.stride(3) != 1 or t.stride(2) != ch or t.stride(0) != t.stride(1) * H:
+        raise ValueError("images need dense pixels, rows and frames (row pitch may exceed the row)")
+    return Image(C.c_void_p(t.data_ptr()), int(W), int(H), int(t.stride(1)) * t.element_size())
 
 
 class _Stitcher:
@@ -303,6 +312,10 @@ class _Stitcher:
         self._handle = C.c_void_p()
         self._status = CudaStatus()
         self._batch = int(batch_size)
+        # Stitchers for other pixel types (uchar3, float4, float3), made on first use: the
+        # reference's stitchers take their pixel type from the tensors they are given.
+        self._others: dict = {}
+        self._args = (control_masks, num_levels, batch_size, minimize_blend, fused, storage, filter)
         if not control_masks.is_valid():
             self._status = CudaStatus(301, "Stitching masks were not able to be loaded")
             return
@@ -315,13 +328,32 @@ class _Stitcher:
             print(f"Stitched canvas size: {self.canvas_width()} x {self.canvas_height()}")
 
     def __del__(self):
-        h = getattr(self, "_handle", None)
-        if h:
-            try:
-                _lib.lib().hmp_stitcher_destroy(h)
-            except Exception:
-                pass
-            self._handle = C.c_void_p()
+        for h in [getattr(self, "_handle", None), *getattr(self, "_others", {}).values()]:
+            if h:
+                try:
+                    _lib.lib().hmp_stitcher_destroy(h)
+                except Exception:
+                    pass
+        self._handle = C.c_void_p()
+        self._others = {}
+
+    def _handle_for(self, channels: int, float_pixels: bool):
+        if (channels, float_pixels) == (4, False):
+            return self._handle
+        h = self._others.get((channels, float_pixels))
+        if h is None:
+            masks, levels, batch, minimize, fused, storage, filt = self._args
+            cfg, keep = build_config(self._kind, masks, levels, batch, minimize, fused, storage, filt, channels,
+                                     float_pixels)
+            h = C.c_void_p()
+            st = _status(_lib.lib().hmp_stitcher_create(C.byref(cfg), C.byref(h)))
+            del keep
+            if not st.ok():
+                if h:
+                    _lib.lib().hmp_stitcher_destroy(h)
+                raise CudaStatusError(st)
+            self._others[(channels, float_pixels)] = h
+        return h
 
     @property
     def status(self) -> CudaStatus:
@@ -387,21 +419,27 @@ class _Stitcher:
             raise ValueError("Input batch size does not match stitcher batch size")
         if any(t.shape[-1] not in (3, 4) for t in batched):
             raise ValueError("Only 3- and 4-channel inputs are supported")
+        ptype = _pixel_type(batched[0])
+        if any(_pixel_type(t) != ptype for t in batched):
+            raise ValueError("inputs must share one pixel type")
+        handle = self._handle_for(*ptype)
         device = batched[0].device
         if canvas is None:
-            canvas = torch.empty((self._batch, self.canvas_height(), self.canvas_width(), 4), dtype=torch.uint8,
-                                 device=device)
+            canvas = torch.empty((self._batch, self.canvas_height(), self.canvas_width(), ptype[0]),
+                                 dtype=torch.float32 if ptype[1] else torch.uint8, device=device)
         else:
             canvas = _ensure_batched(canvas)
             if canvas.shape[0] != self._batch:
                 raise ValueError("Canvas batch size does not match stitcher batch size")
+            if _pixel_type(canvas) != ptype:
+                raise ValueError("canvas pixel type must match the inputs'")
         imgs = (Image * len(batched))(*[_image(t) for t in batched])
         cv = _image(canvas)
         if stream is None:
             stream = torch.cuda.current_stream(device).cuda_stream
         elif hasattr(stream, "cuda_stream"):
             stream = stream.cuda_stream
-        s = _lib.lib().hmp_stitcher_process(self._handle, imgs, len(batched), C.byref(cv), C.c_void_p(stream))
+        s = _lib.lib().hmp_stitcher_process(handle, imgs, len(batched), C.byref(cv), C.c_void_p(stream))
         status = _status(s)
         if not status.ok():
             raise CudaStatusError(status)

@@ -126,7 +126,7 @@ class CudaMat {
   int width() const { return cols_; }
   int height() const { return rows_; }
   int batch_size() const { return batch_size_; }
-  int channels() const { return int(sizeof(T) / sizeof(unsigned char)); }
+  int channels() const { return sizeof(T) % 3 == 0 ? 3 : 4; }  // uchar3 / float3 vs uchar4 / float4
   int pitch() const { return pitch_ ? pitch_ : int(sizeof(T)) * cols_; }
   size_t size() const { return size_t(pitch()) * rows_ * batch_size_; }
   cudaError_t upload(const void* host, int batch_item = 0, cudaStream_t stream = 0) {
@@ -273,6 +273,28 @@ struct ControlMasksN {
 };
 
 namespace cuda {
+
+// Pixel types of the reference's pipelines (CudaStitchPano*<T_pipeline, T_compute>): uchar4 is
+// the fused per-frame path; uchar3, float4 and float3 run the level-by-level kernels.
+template <typename T>
+struct PixelTraits;
+template <>
+struct PixelTraits<uchar4> {
+  static constexpr int kChannels = 4, kFormat = HMP_PIXEL_U8;
+};
+template <>
+struct PixelTraits<uchar3> {
+  static constexpr int kChannels = 3, kFormat = HMP_PIXEL_U8;
+};
+template <>
+struct PixelTraits<float4> {
+  static constexpr int kChannels = 4, kFormat = HMP_PIXEL_F32;
+};
+template <>
+struct PixelTraits<float3> {
+  static constexpr int kChannels = 3, kFormat = HMP_PIXEL_F32;
+};
+
 namespace detail {
 
 // Owns an hmp_stitcher and implements the shared part of the three classes.
@@ -293,7 +315,8 @@ class StitcherBase {
  protected:
   void create(int kind, int batch, int levels, const std::vector<const HostImage<uint16_t>*>& cols,
               const std::vector<const HostImage<uint16_t>*>& rows, const HostImage<uint8_t>& seam,
-              const std::vector<SpatialTiff>& positions, bool minimize, bool fused, int storage) {
+              const std::vector<SpatialTiff>& positions, bool minimize, bool fused, int storage, int channels,
+              int pixel_format) {
     batch_ = batch;
     std::vector<hmp_remap> remaps(cols.size());
     for (size_t i = 0; i < cols.size(); ++i)
@@ -304,7 +327,8 @@ class StitcherBase {
     cfg.n_images = int(cols.size());
     cfg.num_levels = levels;
     cfg.batch_size = batch;
-    cfg.channels = 4;
+    cfg.channels = channels;
+    cfg.pixel_format = pixel_format;
     cfg.minimize_blend = minimize ? 1 : 0;
     cfg.fused = fused ? 1 : 0;
     cfg.storage = storage;
@@ -355,7 +379,8 @@ class CudaStitchPano : public detail::StitcherBase {
     }
     create(HMP_KIND_PANO2, batch_size, num_levels, {&control_masks.img1_col, &control_masks.img2_col},
            {&control_masks.img1_row, &control_masks.img2_row}, control_masks.whole_seam_mask_image,
-           control_masks.positions, minimize_blend, true, storage);
+           control_masks.positions, minimize_blend, true, storage, PixelTraits<T_pipeline>::kChannels,
+           PixelTraits<T_pipeline>::kFormat);
   }
   CudaStatusOr<std::unique_ptr<CudaMat<T_pipeline>>> process(const CudaMat<T_pipeline>& inputImage1,
                                                              const CudaMat<T_pipeline>& inputImage2,
@@ -385,7 +410,8 @@ class CudaStitchPano3 : public detail::StitcherBase {
     create(HMP_KIND_PANO3, batch_size, num_levels,
            {&control_masks.img0_col, &control_masks.img1_col, &control_masks.img2_col},
            {&control_masks.img0_row, &control_masks.img1_row, &control_masks.img2_row},
-           control_masks.whole_seam_mask_image, control_masks.positions, true, fused, storage);
+           control_masks.whole_seam_mask_image, control_masks.positions, true, fused, storage,
+           PixelTraits<T_pipeline>::kChannels, PixelTraits<T_pipeline>::kFormat);
   }
   CudaStatusOr<std::unique_ptr<CudaMat<T_pipeline>>> process(const CudaMat<T_pipeline>& inputImage0,
                                                              const CudaMat<T_pipeline>& inputImage1,
@@ -413,7 +439,8 @@ class CudaStitchPanoN : public detail::StitcherBase {
       rows.push_back(&control_masks.img_row[i]);
     }
     create(HMP_KIND_PANON, batch_size, num_levels, cols, rows, control_masks.whole_seam_mask_indexed,
-           control_masks.positions, minimize_blend, true, storage);
+           control_masks.positions, minimize_blend, true, storage, PixelTraits<T_pipeline>::kChannels,
+           PixelTraits<T_pipeline>::kFormat);
   }
   CudaStatusOr<std::unique_ptr<CudaMat<T_pipeline>>> process(const std::vector<const CudaMat<T_pipeline>*>& inputs,
                                                              cudaStream_t stream,

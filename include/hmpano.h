@@ -92,7 +92,7 @@ typedef struct hmp_config {
   int n_images;       /* 2 (PANO2), 3 (PANO3), 2..8 (PANON) */
   int num_levels;     /* 0 = hard seam; pyramid levels otherwise */
   int batch_size;     /* frames per process() call */
-  int channels;       /* 4 (RGBA) */
+  int channels;       /* 4 (RGBA) or 3 (RGB) */
   int minimize_blend; /* PANO2 / PANON: blend only the seam region (reference default: 1) */
   int fused;          /* PANO3: 1 = fused remap (reference default), 0 = legacy remap+copy */
   int storage;        /* HMP_STORAGE_* */
@@ -101,13 +101,22 @@ typedef struct hmp_config {
   const uint8_t* seam;     /* host, seam_height x seam_width */
   int seam_width;
   int seam_height;
+  int pixel_format;   /* HMP_PIXEL_U8 (default) or HMP_PIXEL_F32: the frames' and canvas's sample type */
 } hmp_config;
 
+/* Pixel sample types (the reference's CudaStitchPano<T_pipeline, T_compute> pipelines): uchar4 /
+ * uchar3 (HMP_PIXEL_U8, canvas packed by truncation) and float4 / float3 (HMP_PIXEL_F32, canvas
+ * stores the reconstruction as is). uchar4 runs the fused per-frame kernels; the other three run
+ * level-by-level kernels with the same arithmetic (3-channel pixels have no alpha: plain means,
+ * plain bilinear upsampling, blends without alpha tests). */
+#define HMP_PIXEL_U8 0
+#define HMP_PIXEL_F32 1
+
 typedef struct hmp_image {
-  void* data; /* device pointer, RGBA8 */
+  void* data; /* device pointer to pixels of the stitcher's type (RGBA8 unless configured otherwise) */
   int width;
   int height;
-  size_t pitch; /* bytes per row (>= 4*width); frame stride = pitch*height */
+  size_t pitch; /* bytes per row (>= pixel size * width); frame stride = pitch*height */
 } hmp_image;
 
 typedef struct hmp_stitcher hmp_stitcher;

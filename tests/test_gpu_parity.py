@@ -52,7 +52,7 @@ def test_golden_cases_bit_exact(golden, oracle_lib):
 def test_golden_cases_f16_storage(golden, oracle_lib):
     for name in _golden_names(golden):
         c = oracle_lib.load_golden_case(golden, name)
-        if c["levels"] < 2:
+        if c["levels"] < 2 or c["frames"][0].shape[-1] != 4:  # FP16 storage is an RGBA8 option
             continue
         st = make_stitcher(c["kind"], masks_for_case(c), c["levels"], c["batch"], c["minimize"], storage="f16")
         out = gpu_stitch(st, c["frames"])
