@@ -488,8 +488,19 @@ class CudaStitchPano3(_Stitcher):
                  fused: bool = True, *, storage: str = "f32", filter: str = "refbox"):
         super().__init__(control_masks, num_levels, batch_size, quiet, True, fused, storage, filter)
 
-    def process(self, input_image_0, input_image_1, input_image_2, canvas=None, stream=None):
-        return self._run([input_image_0, input_image_1, input_image_2], canvas, stream)
+    def process(self, input_image_0, input_image_1, input_image_2, canvas=None, stream=None, fused=None):
+        """``fused`` (default: the constructor's) picks the remap per call, as the reference's
+        process(..., fused) does (src/pano/cudaPano3.h:101-107); the other mode runs on a second
+        stitcher made on first use."""
+        inputs = [input_image_0, input_image_1, input_image_2]
+        masks, levels, batch, _, ctor_fused, storage, filt = self._args
+        if fused is None or bool(fused) == bool(ctor_fused):
+            return self._run(inputs, canvas, stream)
+        other = getattr(self, "_other_mode", None)
+        if other is None:
+            other = self._other_mode = CudaStitchPano3(batch, levels, masks, True, bool(fused), storage=storage,
+                                                       filter=filt)
+        return other._run(inputs, canvas, stream)
 
 
 class CudaStitchPanoN(_Stitcher):

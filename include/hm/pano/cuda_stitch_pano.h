@@ -401,7 +401,8 @@ template <typename T_pipeline, typename T_compute>
 class CudaStitchPano3 : public detail::StitcherBase {
  public:
   CudaStitchPano3(int batch_size, int num_levels, const ControlMasks3& control_masks, bool quiet = false,
-                  bool fused = true, int storage = HMP_STORAGE_F32) {
+                  bool fused = true, int storage = HMP_STORAGE_F32)
+      : masks_(control_masks), levels_(num_levels), fused_(fused), storage_(storage) {
     (void)quiet;
     if (!control_masks.is_valid()) {
       status_ = CudaStatus(cudaErrorFileNotFound, "Stitching masks (3-image) were not able to be loaded");
@@ -413,13 +414,27 @@ class CudaStitchPano3 : public detail::StitcherBase {
            control_masks.whole_seam_mask_image, control_masks.positions, true, fused, storage,
            PixelTraits<T_pipeline>::kChannels, PixelTraits<T_pipeline>::kFormat);
   }
+  // `fused` picks the remap per call, as in the reference (cudaPano3.h:101-107): the fused remap
+  // (invalid entries leave pixels transparent) or the legacy remap + copy. The mode other than the
+  // constructor's runs on a second stitcher, made on its first use.
   CudaStatusOr<std::unique_ptr<CudaMat<T_pipeline>>> process(const CudaMat<T_pipeline>& inputImage0,
                                                              const CudaMat<T_pipeline>& inputImage1,
                                                              const CudaMat<T_pipeline>& inputImage2,
                                                              cudaStream_t stream,
-                                                             std::unique_ptr<CudaMat<T_pipeline>>&& canvas) {
-    return run<T_pipeline>({&inputImage0, &inputImage1, &inputImage2}, stream, std::move(canvas));
+                                                             std::unique_ptr<CudaMat<T_pipeline>>&& canvas,
+                                                             bool fused = true) {
+    if (fused == fused_ || !st_)
+      return run<T_pipeline>({&inputImage0, &inputImage1, &inputImage2}, stream, std::move(canvas));
+    if (!other_) other_.reset(new CudaStitchPano3(batch_, levels_, masks_, true, fused, storage_));
+    return other_->process(inputImage0, inputImage1, inputImage2, stream, std::move(canvas), fused);
   }
+
+ private:
+  ControlMasks3 masks_;
+  int levels_ = 0;
+  bool fused_ = true;
+  int storage_ = HMP_STORAGE_F32;
+  std::unique_ptr<CudaStitchPano3> other_;
 };
 
 // N-image stitcher, N in [2, 8] (src/pano/cudaPanoN.h:80-146).

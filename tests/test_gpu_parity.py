@@ -110,6 +110,14 @@ def test_three_image_legacy_remap(oracle_lib):
         out = gpu_stitch(st, frames)
         ref = oracle_lib.Stitch.from_rig(rig, 4, fused3=fused).run(frames)
         assert np.array_equal(out, ref), fused
+    # The reference picks the mode per call: process(..., fused) (src/pano/cudaPano3.h:101-107).
+    import torch
+
+    st = hmpano.CudaStitchPano3(1, 4, masks_for_rig(rig), quiet=True)
+    ins = [torch.from_numpy(f).cuda() for f in frames]
+    for fused in (False, True, False):
+        out = st.process(*ins, fused=fused).cpu().numpy()
+        assert np.array_equal(out, oracle_lib.Stitch.from_rig(rig, 4, fused3=fused).run(frames)), fused
 
 
 def test_full_scale_two_image_l6():
