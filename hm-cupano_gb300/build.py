@@ -35,6 +35,7 @@ UNITS = {
     "hmp_server.cpp": [],
     "hmp_control_dir.cpp": [],
     "hmp_generic.cu": ["-fmad=false"],
+    "hmp_batch.cpp": [],
 }
 HEADERS = ["hmp_plan.h", "hmp_device.cuh", "hmp_kernels.h", "hmp_blend.cuh", "hmp_admission.h"]
 

@@ -5,6 +5,7 @@ this package mirrors the reference's Python/C++ stitcher API on top of it.
 """
 from .pano import (
     UNMAPPED_POSITION_VALUE,
+    Batch,
     ControlMasks,
     ControlMasks3,
     ControlMasksN,
@@ -22,6 +23,7 @@ from .pano import (
 )
 
 __all__ = [
+    "Batch",
     "ControlMasks",
     "ControlMasks3",
     "ControlMasksN",

@@ -154,6 +154,11 @@ SIGNATURES = {
     "hmp_read_seam_png": ([C.c_char_p, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int), C.c_void_p,
                            C.c_size_t], Status),
     "hmp_read_tiff_u16": ([C.c_char_p, C.POINTER(C.c_int), C.POINTER(C.c_int), C.c_void_p, C.c_size_t], Status),
+    "hmp_batch_create": ([C.POINTER(C.c_void_p)], Status),
+    "hmp_batch_destroy": ([C.c_void_p], None),
+    "hmp_batch_add": ([C.c_void_p, C.c_void_p, C.POINTER(Image), C.c_int, C.POINTER(Image), C.c_int], Status),
+    "hmp_batch_capture": ([C.c_void_p, C.c_void_p], Status),
+    "hmp_batch_launch": ([C.c_void_p, C.c_void_p], Status),
 }
 
 NOALLOC_SCRATCH_BYTES = 48 * 1024 * 1024  # HMP_NOALLOC_SCRATCH_BYTES

@@ -1,6 +1,6 @@
 """Batched streaming form: many frames of several independent streams with uneven canvas sizes,
-the whole job replayed from one CUDA graph, frames per call and pyramid tiles chosen by an
-autotuner whose choice is cached in JSON.
+the whole job replayed from one CUDA graph (the library's hmp_batch_* job), frames per call and
+pyramid tiles chosen by an autotuner whose choice is cached in JSON.
 
 The job: 4 two-image streams (2 x 5120x2880 -> 8500x3300) and 4 three-image streams
 (3 x 2704x1520 -> 6000x1800), 32 consecutive frames each, 6 levels, FP16 pyramid storage with
@@ -68,7 +68,8 @@ class Job:
 
 
 class Plan:
-    """Stitchers (one per stream, `batch` frames per call) and the job's CUDA graph."""
+    """Stitchers (one per stream, `batch` frames per call) and the job as one native batch
+    (hmp_batch_*: every stream's calls captured into one CUDA graph)."""
 
     def __init__(self, job: Job, batch: int, tile_down: int):
         import torch
@@ -76,7 +77,7 @@ class Plan:
         if job.frames % batch:
             raise ValueError("frames per stream must be a multiple of the batch")
         self.job, self.batch, self.tile_down = job, batch, tile_down
-        self.sts, self.canvases, self.torch_streams = [], [], []
+        self.sts, self.canvases = [], []
         for s in job.streams:
             cls = pano.CudaStitchPano if s["kind"] == 2 else pano.CudaStitchPano3
             st = cls(batch, job.levels, s["masks"], quiet=True, storage=job.storage)
@@ -86,60 +87,38 @@ class Plan:
             self.sts.append(st)
             h, w = s["rig"].canvas_h, s["rig"].canvas_w
             self.canvases.append([torch.empty((batch, h, w, 4), dtype=torch.uint8, device=job.device) for _ in range(2)])
-            self.torch_streams.append(torch.cuda.Stream(job.device))
-        # Pre-marshalled calls: (stitcher, inputs, canvas) per stream and step.
-        self.calls = []
-        for i, s in enumerate(job.streams):
-            steps = []
-            for k in range(job.frames // batch):
-                ins = [t[k * batch:(k + 1) * batch] for t in s["inputs"]]
-                imgs = (_lib.Image * len(ins))(*[pano._image(t) for t in ins])
-                steps.append((imgs, len(ins), pano._image(self.canvases[i][k % 2])))
-            self.calls.append(steps)
         self.root = torch.cuda.Stream(job.device)
         self.graph = None
+        self.rebuild()
 
-    def _enqueue(self) -> None:
-        import torch
-
-        fn = _lib.lib().hmp_stitcher_process
-        fork = torch.cuda.Event()
-        fork.record(self.root)
-        for i, steps in enumerate(self.calls):
-            ts = self.torch_streams[i]
-            ts.wait_event(fork)
-            for imgs, n, cv in steps:
-                s = fn(self.sts[i]._handle, imgs, n, C.byref(cv), C.c_void_p(ts.cuda_stream))
-                if s.code:
-                    raise RuntimeError(s.message.decode())
-            done = torch.cuda.Event()
-            done.record(ts)
-            self.root.wait_event(done)
+    def rebuild(self) -> None:
+        """A new batch of every stream's calls (after the stitchers' tiles change)."""
+        self.graph = pano.Batch()
+        for i, s in enumerate(self.job.streams):
+            for k in range(self.job.frames // self.batch):
+                ins = [t[k * self.batch:(k + 1) * self.batch] for t in s["inputs"]]
+                self.graph.add(self.sts[i], ins, self.canvases[i][k % 2], stream_index=i)
+        self.captured = False
 
     def capture(self) -> None:
         import torch
 
-        self._enqueue()  # untimed run outside the graph (first-call work)
+        self.graph.capture(self.root)  # one eager run (first-call work), then the capture
         torch.cuda.synchronize(self.job.device)
-        self.graph = torch.cuda.CUDAGraph()
-        with torch.cuda.graph(self.graph, stream=self.root):
-            self._enqueue()
-        torch.cuda.synchronize(self.job.device)
+        self.captured = True
 
     def time(self, reps: int = 3) -> float:
         """Seconds per job (graph replay, CUDA events on the root stream)."""
         import torch
 
-        if self.graph is None:
+        if not self.captured:
             self.capture()
-        with torch.cuda.stream(self.root):
-            self.graph.replay()
+        self.graph.launch(self.root)
         torch.cuda.synchronize(self.job.device)
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(self.root)
-        with torch.cuda.stream(self.root):
-            for _ in range(reps):
-                self.graph.replay()
+        for _ in range(reps):
+            self.graph.launch(self.root)
         e1.record(self.root)
         torch.cuda.synchronize(self.job.device)
         return e0.elapsed_time(e1) / 1e3 / reps
@@ -171,7 +150,7 @@ def autotune(job: Job, batches=(1, 2, 4, 8), tiles=(32, 64), reps: int = 3, use_
             else:
                 for st in plan.sts:
                     st.set_tiles(tile)
-                plan.graph = None
+                plan.rebuild()
             sec = plan.time(reps)
             trials.append({"batch": b, "tile_down": tile, "fps": round(len(job.streams) * job.frames / sec, 1)})
         del plan

@@ -57,6 +57,59 @@ def _normalize_positions(positions: Sequence[SpatialTiff]) -> list[tuple[int, in
     return [(int(p.xpos), int(p.ypos)) for p in positions]
 
 
+class Batch:
+    """A batched job through hmp_batch_*: process() calls of several stitchers, captured once into
+    a CUDA graph (calls under one stream index in order, indices concurrently) and replayed with one
+    launch. Inputs and canvases are fixed at add(); refill the inputs between launches."""
+
+    def __init__(self):
+        self._h = C.c_void_p()
+        s = _status(_lib.lib().hmp_batch_create(C.byref(self._h)))
+        if not s.ok():
+            raise CudaStatusError(s)
+        self._keep = []
+
+    def add(self, stitcher, inputs: Sequence, canvas, stream_index: int = 0) -> None:
+        batched = [_ensure_batched(t) for t in inputs]
+        canvas = _ensure_batched(canvas)
+        imgs = (Image * len(batched))(*[_image(t) for t in batched])
+        cv = _image(canvas)
+        handle = stitcher._handle_for(*_pixel_type(batched[0]))
+        self._keep += [batched, canvas, imgs, cv, stitcher]
+        s = _status(_lib.lib().hmp_batch_add(self._h, handle, imgs, len(batched), C.byref(cv), int(stream_index)))
+        if not s.ok():
+            raise CudaStatusError(s)
+
+    def _stream(self, stream):
+        import torch
+
+        if stream is None:
+            return torch.cuda.current_stream().cuda_stream
+        return stream.cuda_stream if hasattr(stream, "cuda_stream") else stream
+
+    def capture(self, stream=None) -> None:
+        s = _status(_lib.lib().hmp_batch_capture(self._h, C.c_void_p(self._stream(stream))))
+        if not s.ok():
+            raise CudaStatusError(s)
+
+    def launch(self, stream=None) -> None:
+        s = _status(_lib.lib().hmp_batch_launch(self._h, C.c_void_p(self._stream(stream))))
+        if not s.ok():
+            raise CudaStatusError(s)
+
+    def close(self) -> None:
+        if self._h:
+            _lib.lib().hmp_batch_destroy(self._h)
+            self._h = C.c_void_p()
+        self._keep = []
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 def load_control_dir(directory, kind: int, n_images: int = 0) -> dict:
     """Read a control directory through hmp_control_dir_load (src/pano/controlMasks.cpp:133-326 and
     its three- and N-image forms): {"map_x": [...], "map_y": [...], "positions": [SpatialTiff],

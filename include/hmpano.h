@@ -306,6 +306,21 @@ HMP_API void hmp_server_reset_stats(hmp_server* server);
  * rect and effective levels, out9 = {bx, by, bw, bh, wx, wy, ww, wh, levels}; also the canvas
  * size. Mirrors CanvasManager::updateMinimizeBlend / convertMaskMat (src/pano/canvasManager.cpp:
  * 16-101) and the N-image ROI logic (src/pano/cudaPanoN.inl:156-190). */
+/* ---- Batched job (config 4's native form) ----
+ * Many process() calls of several stitchers captured once into a CUDA graph and replayed with one
+ * launch; no counterpart in the reference (its batched use runs process() per frame). Calls added
+ * under one stream index run in order; different indices run concurrently, so a stitcher's calls
+ * must all use one index (HMP_ERR_INVALID_VALUE otherwise). The first capture
+ * (hmp_batch_capture, or the first hmp_batch_launch) runs the job once eagerly, then captures it;
+ * replays use the device buffers given at add time. Stitchers must outlive the batch. */
+typedef struct hmp_batch hmp_batch;
+HMP_API hmp_status hmp_batch_create(hmp_batch** out);
+HMP_API void hmp_batch_destroy(hmp_batch* batch);
+HMP_API hmp_status hmp_batch_add(hmp_batch* batch, hmp_stitcher* st, const hmp_image* inputs, int n_inputs,
+                                 const hmp_image* canvas, int stream_index);
+HMP_API hmp_status hmp_batch_capture(hmp_batch* batch, void* stream);
+HMP_API hmp_status hmp_batch_launch(hmp_batch* batch, void* stream);
+
 HMP_API hmp_status hmp_plan_geometry(const hmp_config* cfg, int* canvas_w, int* canvas_h, int* out9);
 
 #ifdef __cplusplus

@@ -43,7 +43,7 @@ def test_cpp_drop_in_compiles_and_links():
 
 
 def _write_rig(d: Path, rig, frames, levels: int, batch: int, minimize: bool) -> None:
-    lines = [f"{rig.kind} {rig.n} {levels} {batch} {int(minimize)}"]
+    lines = [f"{rig.kind} {rig.n} {levels} {batch} {int(minimize)} {frames[0].shape[-1]}"]
     for i in range(rig.n):
         h, w = rig.map_x[i].shape
         lines.append(f"{w} {h} {rig.pos_x[i]} {rig.pos_y[i]}")
@@ -58,22 +58,27 @@ def _write_rig(d: Path, rig, frames, levels: int, batch: int, minimize: bool) ->
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("channels", [4, 3])
 @pytest.mark.parametrize("workload,kind,levels,batch", [
     ("pano2_1280x720_to_2200x800", 2, 6, 1),
     ("pano3_2704x1520_to_6000x1800", 3, 3, 2),
     ("panon8_2000x1500_to_9000x2400", 1, 4, 1),
 ])
-def test_cpp_drop_in_matches_oracle(tmp_path, oracle_lib, workload, kind, levels, batch):
+def test_cpp_drop_in_matches_oracle(tmp_path, oracle_lib, workload, kind, levels, batch, channels):
+    """CudaStitchPano*<uchar4, float4> and <uchar3, float3>; the three-image stitcher also runs its
+    legacy remap per call (process(..., fused=false))."""
     from hmpano import synth
 
     exe = _compile()
-    rig = synth.workload_rig(workload, seed=77, kind=kind, scale=0.25)
-    frames = synth.rig_frames(rig, seed=5, batch=batch)
+    rig = synth.workload_rig(workload, seed=77, kind=kind, scale=0.25, oob_fraction=0.02)
+    frames = [f[..., :channels].copy() for f in synth.rig_frames(rig, seed=5, batch=batch)]
     _write_rig(tmp_path, rig, frames, levels, batch, True)
     r = subprocess.run([str(exe), str(tmp_path)], capture_output=True, text=True, timeout=120)
     assert r.returncode == 0, (r.returncode, r.stdout, r.stderr)
     _, cw, ch = r.stdout.split()
-    got = np.fromfile(tmp_path / "canvas.bin", dtype=np.uint8).reshape(batch, int(ch), int(cw), 4)
-    want = oracle_lib.Stitch.from_rig(rig, levels, batch=batch).run(frames)
-    assert got.shape == want.shape
-    assert np.array_equal(got, want), int(np.abs(got.astype(int) - want.astype(int)).max())
+    outputs = [("canvas.bin", True)] + ([("canvas_legacy.bin", False)] if kind == 3 else [])
+    for name, fused in outputs:
+        got = np.fromfile(tmp_path / name, dtype=np.uint8).reshape(batch, int(ch), int(cw), channels)
+        want = oracle_lib.Stitch.from_rig(rig, levels, batch=batch, fused3=fused).run(frames)
+        assert got.shape == want.shape
+        assert np.array_equal(got, want), (name, int(np.abs(got.astype(int) - want.astype(int)).max()))

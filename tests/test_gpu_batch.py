@@ -26,3 +26,36 @@ def test_batched_graph_job_equals_plain_path():
             assert torch.equal(g, w), (b, tile, i)
     tune = batch.autotune(job, batches=(1, 2), tiles=(32, 64), reps=1, use_cache=False)
     assert tune["batch"] in (1, 2) and tune["tile_down"] in (32, 64) and len(tune["trials"]) == 4
+
+
+def test_native_batch_replays_with_refilled_inputs():
+    """hmp_batch_*: the captured job reads its inputs at launch, so refilled inputs give new canvases
+    equal to process() on them; calls on two stream indices both run."""
+    import torch
+
+    import hmpano
+    from hmpano import synth
+
+    from helpers import make_stitcher, masks_for_rig
+
+    rig = synth.workload_rig("pano2_1280x720_to_2200x800", seed=12, kind=2, scale=0.5)
+    st = make_stitcher(2, masks_for_rig(rig), 4, 1)
+    st2 = make_stitcher(2, masks_for_rig(rig), 4, 1)  # one process() in flight per stitcher
+    frames = [torch.from_numpy(f).cuda() for f in synth.rig_frames(rig, seed=2)]
+    other = [torch.from_numpy(f).cuda() for f in synth.rig_frames(rig, seed=3)]
+    h, w = st.canvas_height(), st.canvas_width()
+    cv = [torch.empty((1, h, w, 4), dtype=torch.uint8, device="cuda") for _ in range(2)]
+    job = hmpano.Batch()
+    job.add(st, frames, cv[0], stream_index=0)
+    job.add(st2, other, cv[1], stream_index=1)
+    with pytest.raises(hmpano.CudaStatusError, match="stream index"):
+        job.add(st, other, cv[1], stream_index=1)
+    job.launch()
+    torch.cuda.synchronize()
+    assert torch.equal(cv[0], st.process(*frames)) and torch.equal(cv[1], st.process(*other))
+    for f in frames:
+        f.copy_(torch.roll(f, shifts=5, dims=2))
+    job.launch()
+    torch.cuda.synchronize()
+    assert torch.equal(cv[0], st.process(*frames))
+    job.close()
