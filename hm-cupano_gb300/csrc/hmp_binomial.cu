@@ -1,6 +1,6 @@
 // hmp_binomial.cu -- the Binomial5 pyramid: 5-tap [1,4,6,4,1]/16 separable filter with reflect-101
-// borders in place of the reference's 2x2 box / bilinear pair (no reference implementation; the
-// oracle's FP64 build is the judge, its FP32 build the bit-level twin).
+// borders in place of the reference's 2x2 box / bilinear pair (no reference implementation; parity
+// is checked against the oracle: its FP64 build for accuracy, its FP32 build bit for bit).
 //
 //   down:  G^{l+1}(x, y) = sum over taps (2x+i, 2y+j), i, j in -2..2 with alpha != 0, of
 //          w_i w_j / 256 * G^l, divided by the sum of those weights (0 if none); alpha is the

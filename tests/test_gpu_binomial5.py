@@ -1,5 +1,5 @@
 """GPU parity of the Binomial5 pyramid (5-tap [1,4,6,4,1]/16, reflect-101; no reference
-implementation, so the oracle is the judge).
+implementation, so parity is against the oracle alone).
 
 FP32 storage follows the oracle's operation order term by term, so it must equal the FP32 oracle
 bit for bit; FP16 storage is checked against the FP64 oracle with the FP16 tolerance of the
