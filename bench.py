@@ -217,18 +217,14 @@ def main() -> None:
 
     import __graft_entry__
 
-    rank = int(os.environ.get("RANK", "0"))
-    world = int(os.environ.get("WORLD_SIZE", "1"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(local)
-    dist = None
-    if world > 1:
-        import torch.distributed as dist
-
-        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     __graft_entry__.build()
     import hmpano
-    from hmpano import _lib, synth
+    from hmpano import _lib, replicas, synth
+
+    reps = replicas.init("nccl")
+    rank, world = reps.rank, reps.world
 
     rig = synth.workload_rig(WORKLOAD, seed=1234)
     B = args.batch
@@ -267,8 +263,7 @@ def main() -> None:
             step(i)
     torch.cuda.synchronize()
     pano.set_timing(True)
-    if dist:
-        dist.barrier()
+    reps.barrier()
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     sampler = ClockSampler(local) if rank == 0 else None
@@ -280,15 +275,11 @@ def main() -> None:
         step(i)
     e1.record(stream)
     torch.cuda.synchronize()
-    if dist:
-        dist.barrier()
+    reps.barrier()
     ms = e0.elapsed_time(e1) / args.steps
     ktimes = pano.kernel_times()
     pano.set_timing(False)
-    if dist:
-        t = torch.tensor([ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = reps.max_over_ranks(ms)
     mpix = W * H / 1e6
 
     # The headline pass: the same steps without per-kernel event records (instrumentation),
@@ -320,14 +311,10 @@ def main() -> None:
     if sampler:
         sampler.__exit__(None, None, None)
         sampler.mark(t_region0, t_region1)
-    ms_plain = e0.elapsed_time(e1) / args.steps
-    if dist:
-        t = torch.tensor([ms_plain], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms_plain = float(t.item())
+    ms_plain = reps.max_over_ranks(e0.elapsed_time(e1) / args.steps)
     ms_instrumented = ms
     ms = ms_plain
-    value = world * args.steps * B * mpix / (ms * args.steps / 1e3)
+    value = reps.job_rate(args.steps * B * mpix, ms * args.steps / 1e3)
 
     # Kernel attribution: a pass with the kernels serialised on one stream, so that each
     # kernel's event-timed duration is its own (feeds the roofline of the dominant kernel).
@@ -453,15 +440,14 @@ def main() -> None:
         from hmpano import batch
 
         line["batched"] = batch.run(dev)
-    if not args.no_serve:
+    if not args.no_serve and world == 1:
         # Serving mix on this GPU: 12 configurations, Poisson arrivals, 150 GB admission budget.
         from hmpano import serve_bench
 
         line["serve"] = serve_bench.sweep(dev, seconds=args.serve_seconds)
     if rank == 0:
         print(json.dumps(line), flush=True)
-    if dist:
-        dist.destroy_process_group()
+    reps.close()
 
 
 if __name__ == "__main__":
