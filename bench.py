@@ -428,7 +428,10 @@ def main() -> None:
                      "timing": f"CUDA events, {k_serial} steps with the kernels serialised on one stream"},
         "kernel_ms": {k: round(v[0] / max(v[1], 1), 5) for k, v in ktimes.items()},
         "kernel_ms_serialized": {k: round(v[0] / max(v[1], 1), 5) for k, v in ktimes_serial.items()},
-        "gpu_launches": int(sum(v[1] for v in ktimes.values())),
+        # Kernels launched in the headline timed region (every rank): each process() launches
+        # exactly launches_per_process of this library's kernels (4 here: pyr_down, pyr_coarse,
+        # pyr_fine, canvas_gather), counted per kernel by the instrumented pass.
+        "gpu_launches": world * args.steps * int(info["launches_per_process"]),
         "e2e": e2e,
         "clocks": sampler.summary() if sampler else None,
     }
