@@ -15,6 +15,7 @@ no graph) on one stream.
 from __future__ import annotations
 
 import ctypes as C
+import itertools
 import json
 import os
 import time
@@ -71,7 +72,9 @@ class Plan:
     """Stitchers (one per stream, `batch` frames per call) and the job as one native batch
     (hmp_batch_*: every stream's calls captured into one CUDA graph)."""
 
-    def __init__(self, job: Job, batch: int, tile_down: int):
+    def __init__(self, job: Job, batch: int, tile_down):
+        """tile_down: one pyramid down-tile edge for every stream, or {kind: edge} per stream kind
+        (2 = two-image, 3 = three-image)."""
         import torch
 
         if job.frames % batch:
@@ -83,12 +86,23 @@ class Plan:
             st = cls(batch, job.levels, s["masks"], quiet=True, storage=job.storage)
             if not st.status.ok():
                 raise pano.CudaStatusError(st.status)
-            st.set_tiles(tile_down)
+            st.set_tiles(self.tile_for(s["kind"]))
             self.sts.append(st)
             h, w = s["rig"].canvas_h, s["rig"].canvas_w
             self.canvases.append([torch.empty((batch, h, w, 4), dtype=torch.uint8, device=job.device) for _ in range(2)])
         self.root = torch.cuda.Stream(job.device)
         self.graph = None
+        self.rebuild()
+
+    def tile_for(self, kind: int) -> int:
+        t = self.tile_down
+        return int(t[kind] if isinstance(t, dict) else t)
+
+    def set_tiles(self, tile_down) -> None:
+        """New tiles (one edge, or {kind: edge}); the graph is rebuilt."""
+        self.tile_down = tile_down
+        for st, s in zip(self.sts, self.job.streams):
+            st.set_tiles(self.tile_for(s["kind"]))
         self.rebuild()
 
     def rebuild(self) -> None:
@@ -130,7 +144,8 @@ class Plan:
 
 
 def autotune(job: Job, batches=(1, 2, 4, 8), tiles=(32, 64), reps: int = 3, use_cache: bool = True) -> dict:
-    """Time every (frames per call, tile_down) candidate; keep and cache the fastest."""
+    """Time every frames-per-call candidate with every pyramid down-tile edge per stream kind
+    (two-image and three-image streams choose theirs separately); keep and cache the fastest."""
     key = job.signature()
     cache = {}
     if use_cache and CACHE.exists():
@@ -140,19 +155,20 @@ def autotune(job: Job, batches=(1, 2, 4, 8), tiles=(32, 64), reps: int = 3, use_
             cache = {}
     if use_cache and key in cache:
         return dict(cache[key], cached=True)
+    kinds = sorted({s["kind"] for s in job.streams})
+    combos = [dict(zip(kinds, c)) for c in itertools.product(tiles, repeat=len(kinds))]
     trials = []
     t0 = time.perf_counter()
     for b in batches:
         plan = None
-        for tile in tiles:
+        for combo in combos:
             if plan is None:
-                plan = Plan(job, b, tile)
+                plan = Plan(job, b, combo)
             else:
-                for st in plan.sts:
-                    st.set_tiles(tile)
-                plan.rebuild()
+                plan.set_tiles(combo)
             sec = plan.time(reps)
-            trials.append({"batch": b, "tile_down": tile, "fps": round(len(job.streams) * job.frames / sec, 1)})
+            trials.append({"batch": b, "tile_down": {str(k): v for k, v in combo.items()},
+                           "fps": round(len(job.streams) * job.frames / sec, 1)})
         del plan
     best = max(trials, key=lambda t: t["fps"])
     result = {"batch": best["batch"], "tile_down": best["tile_down"], "fps": best["fps"], "trials": trials,
@@ -209,7 +225,8 @@ def run(device, use_cache: bool = False) -> dict:
     """Autotune, then the batched job and the plain per-frame path on the same frames."""
     job = Job(device)
     tune = autotune(job, use_cache=use_cache)
-    plan = Plan(job, tune["batch"], tune["tile_down"])
+    t = tune["tile_down"]
+    plan = Plan(job, tune["batch"], {int(k): v for k, v in t.items()} if isinstance(t, dict) else t)
     sec = plan.time(5)
     plain_sec = plain_path(job)
     frames = len(job.streams) * job.frames
