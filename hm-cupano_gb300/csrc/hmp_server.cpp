@@ -80,6 +80,7 @@ struct hmp_server {
   long long next_id = 1;
   long long submitted = 0, completed = 0, failed = 0, created = 0, evicted = 0, outstanding = 0;
   int max_in_flight = 0;
+  double resident_bytes = 0, resident_peak = 0;  // the policy's figures, published under `mu`
   std::vector<double> lat_ms;
   double mpix_done = 0;
   Clock::time_point t_first{}, t_last{};
@@ -146,6 +147,14 @@ struct hmp_server {
         }
       if (slot < 0) break;
       ConfigEntry& c = configs[it->config];
+      if (c.bytes > policy.budget()) {
+        // An instance of this configuration was measured larger than the whole budget: the
+        // request can never be admitted, so it fails instead of waiting.
+        finish(*it, mk(HMP_ERR_MEMORY_ALLOCATION, "configuration exceeds the server's HBM budget"), Clock::now());
+        it = queue.erase(it);
+        worked = true;
+        continue;
+      }
       const double est = c.bytes > 0 ? c.bytes : 0.0;
       const hmp::AdmissionPolicy::Decision d = policy.decide(it->config, est);
       int inst = -1;
@@ -219,6 +228,11 @@ struct hmp_server {
       worked = true;
       std::lock_guard<std::mutex> lk(mu);
       max_in_flight = std::max(max_in_flight, int(inflight.size()));
+    }
+    if (worked) {
+      std::lock_guard<std::mutex> lk(mu);
+      resident_bytes = policy.resident();
+      resident_peak = policy.peak();
     }
     return worked;
   }
@@ -377,8 +391,8 @@ HMP_API hmp_status hmp_server_get_stats(hmp_server* s, hmp_server_stats* out) {
   out->instances_evicted = s->evicted;
   out->max_in_flight = s->max_in_flight;
   out->canvas_mpix = s->mpix_done;
-  out->resident_bytes = s->policy.resident();
-  out->resident_bytes_peak = s->policy.peak();
+  out->resident_bytes = s->resident_bytes;
+  out->resident_bytes_peak = s->resident_peak;
   if (!s->lat_ms.empty()) {
     std::vector<double> v = s->lat_ms;
     std::sort(v.begin(), v.end());

@@ -789,6 +789,15 @@ struct hmp_stitcher {
       if (e != cudaSuccess) return cuda_status(e, "stream fork");
       ps = aux;
     }
+    // A failed launch after the fork still joins the pyramid stream back, so that the caller's
+    // stream waits for whatever was already queued there.
+    const auto failed = [&](cudaError_t err, const char* what) {
+      if (fork) {
+        cudaEventRecord(ev_join, aux);
+        cudaStreamWaitEvent(s, ev_join, 0);
+      }
+      return cuda_status(err, what);
+    };
     hmp::PyrArgs a{};
     a.S = S;
     for (int k = 0; k < p.n; ++k) a.slot[k] = slot_planes[k];
@@ -822,7 +831,7 @@ struct hmp_stitcher {
       tbegin(1, ps);
       e = hmp::launch_b5_pyramid(a, p.rule, p.storage, p.batch, ps);
       tend(1, ps);
-      if (e != cudaSuccess) return cuda_status(e, "Binomial5 pyramid launch");
+      if (e != cudaSuccess) return failed(e, "Binomial5 pyramid launch");
     }
     if (p.levels > 1 && !b5) {
       a.tile = tile_down;
@@ -831,7 +840,7 @@ struct hmp_stitcher {
       tbegin(1, ps);
       e = hmp::launch_pyr_down(a, p.storage, grid, ps);
       tend(1, ps);
-      if (e != cudaSuccess) return cuda_status(e, "pyr_down launch");
+      if (e != cudaSuccess) return failed(e, "pyr_down launch");
     }
     a.R1 = R1;
     if (p.levels > 1 && !b5) {
@@ -847,7 +856,7 @@ struct hmp_stitcher {
       tbegin(2, ps);
       e = hmp::launch_pyr_coarse(a, p.rule, p.storage, cgrid, coarse_smem, ps);
       tend(2, ps);
-      if (e != cudaSuccess) return cuda_status(e, "pyr_coarse launch");
+      if (e != cudaSuccess) return failed(e, "pyr_coarse launch");
     }
     if (!b5) {
       const int fx0 = a.wx0 & ~1, fy0 = a.wy0 & ~1;
@@ -855,13 +864,13 @@ struct hmp_stitcher {
       tbegin(3, ps);
       e = hmp::launch_pyr_fine(a, p.rule, p.storage, fgrid, ps);
       tend(3, ps);
-      if (e != cudaSuccess) return cuda_status(e, "pyr_fine launch");
+      if (e != cudaSuccess) return failed(e, "pyr_fine launch");
     }
     if (p.canvas_plane_used) {
       tbegin(0, s);
       e = hmp::launch_canvas_gather(ga, s);
       tend(0, s);
-      if (e != cudaSuccess) return cuda_status(e, "canvas_gather launch");
+      if (e != cudaSuccess) return failed(e, "canvas_gather launch");
     }
     if (fork) {
       e = cudaEventRecord(ev_join, aux);

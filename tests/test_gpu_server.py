@@ -111,5 +111,9 @@ def test_server_bounded_waits_and_errors(prepared):
     rid = srv.submit(ids[0], p["sets"][0][0], torch.empty((1, h, w, 4), dtype=torch.uint8, device="cuda"))
     st = srv.wait(rid, timeout_ms=60000)  # larger than the whole budget: fails, does not hang
     assert st.code == 2, st
+    # Its size is now known: a second request of the configuration fails at once as well.
+    rid = srv.submit(ids[0], p["sets"][0][0], torch.empty((1, h, w, 4), dtype=torch.uint8, device="cuda"))
+    st = srv.wait(rid, timeout_ms=60000)
+    assert st.code == 2, st
     assert srv.drain(10000).ok()
     srv.close()
