@@ -58,6 +58,36 @@ def _peaks() -> tuple[float, str]:
     return 6800.0, "fallback"
 
 
+def m1_bytes(info: dict, n_images: int, batch: int, storage: str) -> float:
+    """Bytes per process() of a level-materialised two-pass pyramid (the reference's structure):
+    the compulsory bytes M0, plus level 0 gathered again for the reconstruction, plus, at every
+    level >= 1, each image's Gaussian written and read once, the reconstruction written and read
+    once (4 channels of `storage`) and the mask level read once (K floats: 1 for two images, else
+    one per image). RGBA8 frames and canvas."""
+    m0 = float(info["m0_bytes"])
+    levels = int(info["levels"])
+    if levels == 0:
+        return m0
+    cw, ch = info["canvas"]
+    wr, br = info["write_rect"], info["blend_rect"]
+    a0 = wr[2] * wr[3]
+    # m0 = outside the write rect (5 + 8B per pixel) + mapped slot pixels (4 + 4B) + a0 (1 + 4B).
+    level0 = m0 - (cw * ch - a0) * (5 + 8 * batch) - a0 * (1 + 4 * batch)
+    s = 16 if storage == "f32" else 8
+    k = 1 if n_images == 2 else n_images
+    w, h, levels_bytes = br[2], br[3], 0.0
+    for _ in range(1, levels):
+        w, h = (w + 1) // 2, (h + 1) // 2
+        levels_bytes += w * h * (batch * (2 * n_images * s + 2 * s) + 4 * k)
+    return m0 + level0 + levels_bytes
+
+
+def ncu_frame_bytes(traffic: dict, prefix: str, kernels) -> int | None:
+    """DRAM bytes of one frame summed over its kernels' ncu captures (None unless all present)."""
+    vals = [traffic.get(f"{prefix}/{k}") for k in kernels]
+    return int(sum(vals)) if vals and all(v is not None for v in vals) else None
+
+
 class ClockSampler:
     """nvidia-smi clocks and throttle reasons sampled during the timed region."""
 
@@ -391,13 +421,17 @@ def main() -> None:
     gather_bytes = gather_px * (4.0 + 8.0 * B)
     dom_bytes = {"canvas_gather": gather_bytes}.get(dom)
     achieved = dom_bytes / (per_launch_ms / 1e3) / 1e9 if dom_bytes else None
-    traffic = None
+    traffic = frame_dram = None
     tp = REPO / "profiles" / "traffic.json"
     if tp.exists():
         try:
-            traffic = json.loads(tp.read_text()).get(f"{WORKLOAD}/L{args.levels}/{args.storage}/{dom}")
+            prefix = f"{WORKLOAD}/L{args.levels}/{args.storage}"
+            captured = json.loads(tp.read_text())
+            traffic = captured.get(f"{prefix}/{dom}")
+            if B == 1 and args.filter == "refbox" and info["levels"] > 1:
+                frame_dram = ncu_frame_bytes(captured, prefix, names)
         except Exception:
-            traffic = None
+            traffic = frame_dram = None
     line = {
         "metric": METRIC,
         "value": round(value, 2),
@@ -414,6 +448,10 @@ def main() -> None:
         "fps": round(world * B * 1e3 / ms, 1),
         "hbm_frac_frame": round(info["m0_bytes"] / (ms / 1e3) / (peak * 1e9), 4),
         "m0_bytes_per_step": int(info["m0_bytes"]),
+        # The level-materialised model (every pyramid level through HBM) for comparison, and the
+        # frame's DRAM bytes summed over its kernels' ncu captures (profiles/, each kernel alone).
+        "m1_bytes_per_step": int(m1_bytes(info, 2, B, args.storage)),
+        "ncu_dram_bytes_per_step": frame_dram,
         "ms_per_step_instrumented": round(ms_instrumented, 5),
         "config": {"workload": WORKLOAD, "levels": args.levels, "storage": args.storage, "batch": B,
                    "graph": bool(args.graph), "filter": args.filter,

@@ -312,7 +312,9 @@ HMP_API void hmp_server_reset_stats(hmp_server* server);
  * under one stream index run in order; different indices run concurrently, so a stitcher's calls
  * must all use one index (HMP_ERR_INVALID_VALUE otherwise). The first capture
  * (hmp_batch_capture, or the first hmp_batch_launch) runs the job once eagerly, then captures it;
- * replays use the device buffers given at add time. Stitchers must outlive the batch. */
+ * replays use the device buffers given at add time. Stitchers must outlive the batch, and a
+ * stitcher called directly between replays must be given frames of the sizes and pitches it was
+ * captured with (a call with other frames re-resolves its canvas table, which the graph reads). */
 typedef struct hmp_batch hmp_batch;
 HMP_API hmp_status hmp_batch_create(hmp_batch** out);
 HMP_API void hmp_batch_destroy(hmp_batch* batch);
