@@ -45,6 +45,17 @@ struct LoadError : std::runtime_error {
 
 [[noreturn]] void fail(const std::string& m, int code = HMP_ERR_INVALID_VALUE) { throw LoadError(code, m); }
 
+// Largest image side and pixel count either decoder accepts; larger headers are rejected before
+// anything is sized from them (and keep every byte count below 2^40).
+constexpr int64_t kMaxSide = int64_t(1) << 20;
+constexpr int64_t kMaxPixels = int64_t(1) << 31;
+
+void check_size(int64_t w, int64_t h, const std::string& path) {
+  if (w <= 0 || h <= 0) fail("image without pixels: " + path);
+  if (w > kMaxSide || h > kMaxSide || w * h > kMaxPixels)
+    fail("image larger than 2^20 pixels per side or 2^31 pixels: " + path, HMP_ERR_NOT_SUPPORTED);
+}
+
 Bytes read_file(const std::string& path) {
   FILE* f = std::fopen(path.c_str(), "rb");
   if (!f) fail("Cannot open file: " + path, HMP_ERR_FILE_NOT_FOUND);
@@ -60,7 +71,8 @@ Bytes read_file(const std::string& path) {
 
 class Inflate {
  public:
-  Inflate(const uint8_t* p, size_t n, Bytes& out) : p_(p), n_(n), out_(out) {}
+  // `limit`: the most output bytes the caller uses; decoding stops once they are out.
+  Inflate(const uint8_t* p, size_t n, Bytes& out, size_t limit) : p_(p), n_(n), out_(out), limit_(limit) {}
 
   void run() {
     int last;
@@ -75,7 +87,7 @@ class Inflate {
         dynamic();
       else
         fail("corrupt deflate stream (block type 3)");
-    } while (!last);
+    } while (!last && out_.size() < limit_);
   }
 
  private:
@@ -104,7 +116,7 @@ class Inflate {
     pos_ += 4;
     if ((len ^ 0xFFFFu) != nlen) fail("corrupt deflate stream (stored length)");
     if (pos_ + len > n_) fail("truncated deflate stream");
-    out_.insert(out_.end(), p_ + pos_, p_ + pos_ + len);
+    out_.insert(out_.end(), p_ + pos_, p_ + pos_ + std::min<size_t>(len, limit_ - out_.size()));
     pos_ += len;
   }
 
@@ -144,6 +156,7 @@ class Inflate {
     static const uint8_t dext[30] = {0, 0, 0, 0, 1, 1, 2, 2, 3, 3, 4, 4, 5, 5, 6, 6, 7, 7, 8, 8, 9, 9, 10, 10, 11, 11, 12, 12, 13, 13};
     for (;;) {
       int sym = decode(lit);
+      if (out_.size() >= limit_) return;
       if (sym < 256) {
         out_.push_back(uint8_t(sym));
       } else if (sym == 256) {
@@ -156,8 +169,8 @@ class Inflate {
         if (ds >= 30) fail("corrupt deflate stream (distance code)");
         const size_t d = dbase[ds] + bits(dext[ds]);
         if (d > out_.size()) fail("corrupt deflate stream (distance too far)");
-        const size_t from = out_.size() - d;
-        for (size_t k = 0; k < len; ++k) {
+        const size_t from = out_.size() - d, copy = std::min<size_t>(len, limit_ - out_.size());
+        for (size_t k = 0; k < copy; ++k) {
           const uint8_t v = out_[from + k];
           out_.push_back(v);
         }
@@ -220,14 +233,16 @@ class Inflate {
   uint32_t buf_ = 0;
   int cnt_ = 0;
   Bytes& out_;
+  size_t limit_;
 };
 
-// zlib stream (RFC 1950): a 2-byte header, deflate data, Adler-32 (not checked).
-Bytes zlib_inflate(const uint8_t* p, size_t n) {
+// zlib stream (RFC 1950): a 2-byte header, deflate data, Adler-32 (not checked). At most `limit`
+// output bytes.
+Bytes zlib_inflate(const uint8_t* p, size_t n, size_t limit) {
   if (n < 2 || (p[0] & 0x0F) != 8 || ((p[0] << 8) | p[1]) % 31 != 0 || (p[1] & 0x20))
     fail("not a zlib stream");
   Bytes out;
-  Inflate(p + 2, n - 2, out).run();
+  Inflate(p + 2, n - 2, out, limit).run();
   return out;
 }
 
@@ -259,8 +274,8 @@ Png decode_png(const std::string& path) {
     const uint8_t* d = &b[pos + 8];
     if (type == "IHDR") {
       if (len < 13) fail("bad PNG header: " + path);
-      png.w = int(be32(d));
-      png.h = int(be32(d + 4));
+      png.w = int(std::min<uint32_t>(be32(d), uint32_t(INT32_MAX)));
+      png.h = int(std::min<uint32_t>(be32(d + 4), uint32_t(INT32_MAX)));
       png.depth = d[8];
       png.color = d[9];
       interlace = d[12];
@@ -274,15 +289,16 @@ Png decode_png(const std::string& path) {
     }
     pos += 12 + size_t(len);
   }
-  if (!have_header || png.w <= 0 || png.h <= 0) fail("PNG without a valid header: " + path);
+  if (!have_header) fail("PNG without a valid header: " + path);
+  check_size(int64_t(png.w), int64_t(png.h), path);
   if (interlace) fail("interlaced PNG is not supported: " + path, HMP_ERR_NOT_SUPPORTED);
   const std::set<int> depths = png.color == 0 ? std::set<int>{1, 2, 4, 8, 16}
                                : png.color == 3 ? std::set<int>{1, 2, 4, 8}
                                                 : std::set<int>{8, 16};
   if (!(png.color == 0 || png.color == 2 || png.color == 3 || png.color == 4 || png.color == 6) || !depths.count(png.depth))
     fail("unsupported PNG colour type / bit depth: " + path, HMP_ERR_NOT_SUPPORTED);
-  const Bytes raw = zlib_inflate(idat.data(), idat.size());
   const size_t rb = png.row_bytes(), bpp = std::max<size_t>(1, size_t(png.channels()) * png.depth / 8);
+  const Bytes raw = zlib_inflate(idat.data(), idat.size(), (rb + 1) * size_t(png.h));
   if (raw.size() < (rb + 1) * size_t(png.h)) fail("truncated PNG image data: " + path);
   png.pix.assign(rb * size_t(png.h), 0);
   for (int y = 0; y < png.h; ++y) {
@@ -392,16 +408,21 @@ struct Tiff {
   bool has(uint16_t tag) const { return tags.count(tag) != 0; }
   // Integer value i of a BYTE / SHORT / LONG tag.
   uint32_t uint_at(uint16_t tag, uint32_t i = 0) const {
+    if (!has(tag)) fail("TIFF tag " + std::to_string(tag) + " is missing");
     const Entry& e = tags.at(tag);
     if (i >= e.count) fail("TIFF tag " + std::to_string(tag) + " has too few values");
     if (e.type == 3) return u16(e.at + 2 * i);
     if (e.type == 4) return u32(e.at + 4 * i);
-    if (e.type == 1) return b.at(e.at + i);
+    if (e.type == 1) {
+      if (size_t(e.at) + i >= b.size()) fail("truncated TIFF");
+      return b[size_t(e.at) + i];
+    }
     fail("TIFF tag " + std::to_string(tag) + " is not an integer");
   }
   uint32_t uint_or(uint16_t tag, uint32_t dflt) const { return has(tag) ? uint_at(tag) : dflt; }
   // A RATIONAL / FLOAT / DOUBLE / integer tag as float (libtiff hands these tags out as float).
   float real(uint16_t tag) const {
+    if (!has(tag)) fail("TIFF tag " + std::to_string(tag) + " is missing");
     const Entry& e = tags.at(tag);
     if (e.type == 5) {
       const uint32_t num = u32(e.at), den = u32(e.at + 4);
@@ -474,7 +495,7 @@ Bytes lzw_decode(const uint8_t* p, size_t n, size_t expect) {
   size_t bitpos = 0;
   int width = 9, prev = -1;
   for (;;) {
-    if (bitpos + width > n * 8) break;
+    if (out.size() >= expect || bitpos + width > n * 8) break;  // nothing past the strip is used
     int code = 0;
     for (int k = 0; k < width; ++k, ++bitpos) code = (code << 1) | ((p[bitpos >> 3] >> (7 - (bitpos & 7))) & 1);
     if (code == 257) break;  // end of information
@@ -528,27 +549,31 @@ Bytes packbits_decode(const uint8_t* p, size_t n, size_t expect) {
 // horizontal predictor).
 std::vector<uint16_t> read_tiff_u16(const std::string& path, int& w, int& h) {
   const Tiff t = parse_tiff(path);
-  w = int(t.uint_at(256));
-  h = int(t.uint_at(257));
+  const uint32_t w32 = t.uint_at(256), h32 = t.uint_at(257);
+  check_size(int64_t(w32), int64_t(h32), path);
+  w = int(w32);
+  h = int(h32);
   const uint32_t spp = t.uint_or(277, 1), bits = t.uint_or(258, 1), fmt = t.uint_or(339, 1);
   const uint32_t comp = t.uint_or(259, 1), pred = t.uint_or(317, 1);
-  if (w <= 0 || h <= 0) fail("TIFF without an image: " + path);
   if (spp != 1 || bits != 16 || fmt != 1)
     fail("mapping tables must be single-channel 16-bit unsigned TIFF images: " + path, HMP_ERR_NOT_SUPPORTED);
   if (!(comp == 1 || comp == 5 || comp == 8 || comp == 32946 || comp == 32773))
     fail("unsupported TIFF compression " + std::to_string(comp) + ": " + path, HMP_ERR_NOT_SUPPORTED);
   if (pred != 1 && pred != 2) fail("unsupported TIFF predictor " + std::to_string(pred) + ": " + path, HMP_ERR_NOT_SUPPORTED);
   const bool tiled = t.has(322);
-  const int bw = tiled ? int(t.uint_at(322)) : w;
-  const int bh = tiled ? int(t.uint_at(323)) : int(std::min<uint32_t>(t.uint_or(278, uint32_t(h)), uint32_t(h)));
-  if (bw <= 0 || bh <= 0) fail("bad TIFF strip or tile size: " + path);
+  const uint32_t bw32 = tiled ? t.uint_at(322) : uint32_t(w);
+  const uint32_t bh32 = tiled ? t.uint_at(323) : std::min<uint32_t>(t.uint_or(278, uint32_t(h)), uint32_t(h));
+  if (bw32 == 0 || bh32 == 0 || bw32 > uint32_t(kMaxSide) || bh32 > uint32_t(kMaxSide) ||
+      uint64_t(bw32) * bh32 > uint64_t(kMaxPixels))
+    fail("bad TIFF strip or tile size: " + path);
+  const int bw = int(bw32), bh = int(bh32);
   const uint16_t off_tag = tiled ? 324 : 273, cnt_tag = tiled ? 325 : 279;
   const int across = (w + bw - 1) / bw, down = (h + bh - 1) / bh;
-  const uint32_t nblocks = uint32_t(across) * uint32_t(down);
+  const uint64_t nblocks = uint64_t(across) * uint64_t(down);
   if (!t.has(off_tag) || !t.has(cnt_tag) || t.tags.at(off_tag).count < nblocks || t.tags.at(cnt_tag).count < nblocks)
     fail("TIFF strip or tile table missing: " + path);
   std::vector<uint16_t> img(size_t(w) * h);
-  for (uint32_t blk = 0; blk < nblocks; ++blk) {
+  for (uint32_t blk = 0; blk < uint32_t(nblocks); ++blk) {
     const int bx = int(blk % uint32_t(across)) * bw, by = int(blk / uint32_t(across)) * bh;
     const int rows = tiled ? bh : std::min(bh, h - by);  // a tile is stored whole; a strip is clipped
     const size_t expect = size_t(bw) * rows * 2;
@@ -563,7 +588,7 @@ std::vector<uint16_t> read_tiff_u16(const std::string& path, int& w, int& h) {
     else if (comp == 32773)
       data = packbits_decode(src, cnt, expect);
     else
-      data = zlib_inflate(src, cnt);
+      data = zlib_inflate(src, cnt, expect);
     if (data.size() < expect) fail("TIFF strip or tile too short: " + path);
     for (int r = 0; r < rows; ++r) {
       uint16_t acc = 0;
@@ -670,6 +695,9 @@ HMP_API hmp_status hmp_control_dir_load(const char* directory, int kind, int n_i
   } catch (const std::bad_alloc&) {
     delete d;
     return make(HMP_ERR_MEMORY_ALLOCATION, "out of host memory");
+  } catch (const std::exception& e) {
+    delete d;
+    return make(HMP_ERR_INVALID_VALUE, std::string("control directory: ") + e.what());
   }
   d->pub.internal = d;
   *out = &d->pub;
@@ -699,6 +727,12 @@ HMP_API hmp_status hmp_read_seam_png(const char* path, int* width, int* height, 
   } catch (const LoadError& e) {
     s.code = e.code;
     std::snprintf(s.message, sizeof(s.message), "%s", e.what());
+  } catch (const std::bad_alloc&) {
+    s.code = HMP_ERR_MEMORY_ALLOCATION;
+    std::snprintf(s.message, sizeof(s.message), "out of host memory");
+  } catch (const std::exception& e) {
+    s.code = HMP_ERR_INVALID_VALUE;
+    std::snprintf(s.message, sizeof(s.message), "%s", e.what());
   }
   return s;
 }
@@ -718,6 +752,12 @@ HMP_API hmp_status hmp_read_tiff_u16(const char* path, int* width, int* height, 
     s.code = HMP_OK;
   } catch (const LoadError& e) {
     s.code = e.code;
+    std::snprintf(s.message, sizeof(s.message), "%s", e.what());
+  } catch (const std::bad_alloc&) {
+    s.code = HMP_ERR_MEMORY_ALLOCATION;
+    std::snprintf(s.message, sizeof(s.message), "out of host memory");
+  } catch (const std::exception& e) {
+    s.code = HMP_ERR_INVALID_VALUE;
     std::snprintf(s.message, sizeof(s.message), "%s", e.what());
   }
   return s;

@@ -5,6 +5,7 @@ rig's control directory round trip. Host code only: no GPU.
 """
 from __future__ import annotations
 
+import struct
 from pathlib import Path
 
 import numpy as np
@@ -152,6 +153,86 @@ def test_tiff_rejects_float_tables(hp, tmp_path):
     p.write_bytes(bytes(b))
     with pytest.raises(hp.CudaStatusError, match="16-bit unsigned"):
         hp.read_tiff_u16(p)
+
+
+# ---- malformed and oversized files: errors or bounded work, never a crash ----
+
+def _patch_tiff_tag(path: Path, tag: int, ttype: int, new_tag: int | None = None, new_value: int | None = None):
+    b = bytearray(path.read_bytes())
+    at = bytes(b).index(tag.to_bytes(2, "little") + ttype.to_bytes(2, "little"))
+    if new_tag is not None:
+        b[at:at + 2] = new_tag.to_bytes(2, "little")
+    if new_value is not None:
+        b[at + 8:at + 12] = new_value.to_bytes(4, "little")
+    path.write_bytes(bytes(b))
+
+
+def test_tiff_missing_width_is_an_error(hp, tmp_path):
+    p = tmp_path / "m.tif"
+    cf.write_tiff(p, np.zeros((4, 4), np.uint16))
+    _patch_tiff_tag(p, 256, 4, new_tag=0x8123)  # ImageWidth renamed to an unknown private tag
+    with pytest.raises(hp.CudaStatusError, match="256"):
+        hp.read_tiff_u16(p)
+
+
+def test_tiff_and_png_reject_huge_headers(hp, tmp_path):
+    p = tmp_path / "m.tif"
+    cf.write_tiff(p, np.zeros((4, 4), np.uint16))
+    _patch_tiff_tag(p, 256, 4, new_value=1 << 30)
+    with pytest.raises(hp.CudaStatusError, match="larger than") as e:
+        hp.read_tiff_u16(p)
+    assert e.value.status.code == 801
+    q = tmp_path / "s.png"
+    cf.write_png(q, np.zeros((4, 4), np.uint8), color_type=0)
+    b = bytearray(q.read_bytes())
+    b[16:24] = (0x7FFF0000).to_bytes(4, "big") + (0x7FFF0000).to_bytes(4, "big")  # IHDR width, height
+    q.write_bytes(bytes(b))
+    with pytest.raises(hp.CudaStatusError, match="larger than"):
+        hp.read_seam_png(q)
+
+
+@pytest.mark.parametrize("compression", [5, 8])
+def test_tiff_strip_that_decodes_past_the_image_is_cut(hp, tmp_path, compression):
+    """A strip whose stream holds far more than the image: the decoder stops at the strip's size
+    (a 100 MB stream of zeros after the pixels costs nothing)."""
+    import zlib
+
+    img = np.arange(48, dtype=np.uint16).reshape(6, 8) * 997
+    p = tmp_path / "m.tif"
+    cf.write_tiff(p, img, compression=compression)
+    raw = img.astype("<u2").tobytes() + bytes(100 << 20 if compression == 8 else 1 << 16)
+    stream = zlib.compress(raw, 9) if compression == 8 else cf.lzw_encode(raw)
+    b = p.read_bytes()
+    old = zlib.compress(img.astype("<u2").tobytes()) if compression == 8 else cf.lzw_encode(img.astype("<u2").tobytes())
+    assert b.endswith(old)
+    p.write_bytes(b[: len(b) - len(old)] + stream)
+    _patch_tiff_tag(p, 279, 4, new_value=len(stream))  # StripByteCounts
+    np.testing.assert_array_equal(hp.read_tiff_u16(p), img)
+
+
+def test_png_idat_that_decodes_past_the_image_is_cut(hp, tmp_path):
+    import zlib
+
+    rows = b"".join(b"\x00" + bytes([y * 10 + x for x in range(5)]) for y in range(3))
+    ihdr = struct.pack(">IIBBBBB", 5, 3, 8, 0, 0, 0, 0)
+    idat = zlib.compress(rows + bytes(100 << 20), 9)
+    data = cf._png_chunk(b"IHDR", ihdr) + cf._png_chunk(b"IDAT", idat) + cf._png_chunk(b"IEND", b"")
+    q = tmp_path / "s.png"
+    q.write_bytes(b"\x89PNG\r\n\x1a\n" + data)
+    out, _ = hp.read_seam_png(q)
+    np.testing.assert_array_equal(out, np.array([[y * 10 + x for x in range(5)] for y in range(3)], np.uint8))
+
+
+def test_loader_reports_a_bad_table_without_crashing(hp, tmp_path):
+    rng = np.random.default_rng(5)
+    mx, my = _rig_tables(rng, 2)
+    seam = np.zeros((24, 60), np.uint8)
+    seam[:, 30:] = 255
+    cf.write_control_dir(tmp_path, mx, my, [(0, 0), (20, 0)], seam, paletted=False)
+    _patch_tiff_tag(tmp_path / "mapping_0001_y.tif", 257, 4, new_tag=0x8124)  # ImageLength missing
+    with pytest.raises(hp.CudaStatusError, match="257"):
+        hp.load_control_dir(tmp_path, hp.pano._lib.KIND_PANO2)
+    assert not hp.ControlMasks().load(tmp_path)
 
 
 # ---- the loader's rules ----
