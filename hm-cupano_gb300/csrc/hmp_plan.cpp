@@ -116,6 +116,9 @@ int validate(const hmp_config& c, std::string& m) {
       return fail(m, HMP_ERR_FILE_NOT_FOUND, "Stitching masks were not able to be loaded");
     if (r.xpos < 0 || r.ypos < 0)
       return fail(m, HMP_ERR_INVALID_VALUE, "canvas positions must be normalised (>= 0)");
+    // Keeps position + size (the canvas extent) and every pixel count far from int overflow.
+    if (int64_t(r.xpos) + r.width > (int64_t(1) << 20) || int64_t(r.ypos) + r.height > (int64_t(1) << 20))
+      return fail(m, HMP_ERR_NOT_SUPPORTED, "canvas larger than 2^20 pixels per side");
   }
   return HMP_OK;
 }

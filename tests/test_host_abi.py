@@ -142,6 +142,11 @@ def test_create_rejects_invalid_configurations(lib):
     mN = hmpano.ControlMasksN([mx, mx], [my, my], np.zeros((h, w), np.uint8), [hmpano.SpatialTiff(0, 0)] * 2)
     code, msg = _create(lib, mN, _lib.KIND_PANON, 9, minimize_blend=False)
     assert code == 801 and "levels" in msg
+    # a position that puts the canvas beyond 2^20 pixels per side (rejected before any sizing)
+    m = _two_image_masks()
+    m.positions = [hmpano.SpatialTiff(0, 0), hmpano.SpatialTiff(float(1 << 21), 0)]
+    code, msg = _create(lib, m, _lib.KIND_PANO2, 0)
+    assert code == 801 and "2^20" in msg
 
 
 def test_python_mirror_keeps_invalid_masks_as_status():
