@@ -467,6 +467,7 @@ class _Stitcher:
         st = self.status
         if not st.ok():
             raise CudaStatusError(st)
+        _check_backend(getattr(self, "_backend", "auto"))
         batched = [_ensure_batched(t) for t in inputs]
         if any(t.shape[0] != self._batch for t in batched):
             raise ValueError("Input batch size does not match stitcher batch size")
@@ -499,15 +500,29 @@ class _Stitcher:
         return canvas
 
 
+def _check_backend(backend) -> None:
+    """The reference's backend names (cupano/ops.py:24, 60-69): "auto" and "triton" select its GPU
+    kernels; here both run this library's CUDA kernels, the only backend. Anything else is the
+    reference's ValueError, raised by process() as there."""
+    if backend not in ("auto", "triton"):
+        raise ValueError(f"Unsupported backend: {backend}")
+
+
 class CudaStitchPano(_Stitcher):
-    """Two-image stitcher (src/pano/cudaPano.h:68-115, cupano/pano.py:127-551)."""
+    """Two-image stitcher (src/pano/cudaPano.h:68-115, cupano/pano.py:127-551).
+
+    ``backend`` and ``enable_cuda_graphs`` are the reference Python class's arguments: every
+    backend name it accepts runs this library's kernels, and process() launches at most four
+    kernels with no allocation, so callers capture it in a CUDA graph themselves if they want one
+    (it is capturable from the first call)."""
 
     _kind = _lib.KIND_PANO2
 
     def __init__(self, batch_size: int, num_levels: int, control_masks: ControlMasks, quiet: bool = False,
-                 minimize_blend: bool = True, max_output_width: int = 0, *, storage: str = "f32",
-                 filter: str = "refbox"):
-        del max_output_width
+                 minimize_blend: bool = True, max_output_width: int = 0, backend: str = "auto",
+                 enable_cuda_graphs: bool = True, *, storage: str = "f32", filter: str = "refbox"):
+        del max_output_width, enable_cuda_graphs
+        self._backend = backend
         super().__init__(control_masks, num_levels, batch_size, quiet, minimize_blend, True, storage, filter)
 
     def process(self, input_image_1, input_image_2, canvas=None, stream=None):
@@ -562,7 +577,10 @@ class CudaStitchPanoN(_Stitcher):
     _kind = _lib.KIND_PANON
 
     def __init__(self, batch_size: int, num_levels: int, control_masks: ControlMasksN, quiet: bool = False,
-                 minimize_blend: bool = True, *, storage: str = "f32", filter: str = "refbox"):
+                 minimize_blend: bool = True, backend: str = "auto", enable_cuda_graphs: bool = True, *,
+                 storage: str = "f32", filter: str = "refbox"):
+        del enable_cuda_graphs  # as for CudaStitchPano
+        self._backend = backend
         self._n = len(control_masks.img_col)
         if control_masks.is_valid() and not 2 <= self._n <= 8:
             self._handle = C.c_void_p()

@@ -198,6 +198,26 @@ def test_process_errors_are_sticky():
         st.process(frames[0], frames[1])
 
 
+def test_reference_backend_names(oracle_lib):
+    """The reference's backend names run these kernels (same bits); an unknown one is its
+    ValueError from process() (cupano/ops.py:60-69)."""
+    import torch
+    from hmpano import synth
+
+    import hmpano
+
+    rig = synth.workload_rig("pano2_1280x720_to_2200x800", seed=8)
+    frames = [torch.from_numpy(f).cuda() for f in synth.rig_frames(rig, seed=2)]
+    outs = []
+    for backend in ("auto", "triton"):
+        st = hmpano.CudaStitchPano(1, 3, masks_for_rig(rig), True, True, 0, backend, False)
+        outs.append(st.process(frames[0], frames[1]).cpu())
+    assert torch.equal(outs[0], outs[1])
+    st = hmpano.CudaStitchPano(1, 3, masks_for_rig(rig), quiet=True, backend="torch")
+    with pytest.raises(ValueError, match="Unsupported backend"):
+        st.process(frames[0], frames[1])
+
+
 def test_graph_capture_replays_identically(oracle_lib):
     """process() allocates nothing, so it can be captured in a CUDA graph and replayed."""
     import torch

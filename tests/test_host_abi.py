@@ -158,3 +158,19 @@ def test_python_mirror_keeps_invalid_masks_as_status():
         pano.process(None, None)
     panoN = hmpano.CudaStitchPanoN(1, 0, hmpano.ControlMasksN(), quiet=True)
     assert not panoN.status.ok()
+
+
+def test_python_mirror_takes_the_reference_constructor_arguments():
+    """cupano's CudaStitchPano(batch, levels, masks, quiet, minimize_blend, max_output_width,
+    backend, enable_cuda_graphs) and CudaStitchPanoN(batch, levels, masks, quiet, minimize_blend,
+    backend, enable_cuda_graphs) (cupano/pano.py:127-138, 553-563), positionally and by name."""
+    import hmpano
+
+    p = hmpano.CudaStitchPano(1, 0, hmpano.ControlMasks(), True, True, 0, "triton", False)
+    assert p.status.code == 301  # the masks' status, not a TypeError
+    p = hmpano.CudaStitchPano(1, 0, hmpano.ControlMasks(), quiet=True, backend="auto", enable_cuda_graphs=True)
+    assert p.status.code == 301
+    n = hmpano.CudaStitchPanoN(1, 0, hmpano.ControlMasksN(), True, True, "auto", False)
+    assert not n.status.ok()
+    with pytest.raises(ValueError, match="Unsupported backend"):
+        hmpano.pano._check_backend("torch")
