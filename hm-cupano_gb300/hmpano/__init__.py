@@ -6,6 +6,7 @@ this package mirrors the reference's Python/C++ stitcher API on top of it.
 from .pano import (
     UNMAPPED_POSITION_VALUE,
     Batch,
+    CanvasInfo,
     ControlMasks,
     ControlMasks3,
     ControlMasksN,
@@ -14,6 +15,7 @@ from .pano import (
     CudaStitchPano,
     CudaStitchPano3,
     CudaStitchPanoN,
+    Rect,
     SpatialTiff,
     StitchServer,
     load_control_dir,
@@ -24,6 +26,7 @@ from .pano import (
 
 __all__ = [
     "Batch",
+    "CanvasInfo",
     "ControlMasks",
     "ControlMasks3",
     "ControlMasksN",
@@ -32,6 +35,7 @@ __all__ = [
     "CudaStitchPano",
     "CudaStitchPano3",
     "CudaStitchPanoN",
+    "Rect",
     "SpatialTiff",
     "StitchServer",
     "UNMAPPED_POSITION_VALUE",

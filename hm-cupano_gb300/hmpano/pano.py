@@ -17,6 +17,7 @@ current stream.
 from __future__ import annotations
 
 import ctypes as C
+import os
 from dataclasses import dataclass, field
 from typing import Iterable, Sequence
 
@@ -32,6 +33,43 @@ UNMAPPED_POSITION_VALUE = np.uint16(65535)
 class SpatialTiff:
     xpos: float
     ypos: float
+
+
+@dataclass
+class Rect:
+    """Integer rectangle of the reference's geometry module (cupano/geometry.py), exported for
+    code written against it."""
+
+    x: int = 0
+    y: int = 0
+    width: int = 0
+    height: int = 0
+
+    @property
+    def empty(self) -> bool:
+        return self.width <= 0 or self.height <= 0
+
+    @property
+    def right(self) -> int:
+        return self.x + self.width
+
+    @property
+    def bottom(self) -> int:
+        return self.y + self.height
+
+    def intersect(self, other: "Rect") -> "Rect":
+        x0, y0 = max(self.x, other.x), max(self.y, other.y)
+        w, h = min(self.right, other.right) - x0, min(self.bottom, other.bottom) - y0
+        return Rect(x0, y0, max(0, w), max(0, h))
+
+
+@dataclass
+class CanvasInfo:
+    """Canvas size and the tables' integer positions on it (cupano/geometry.py)."""
+
+    width: int
+    height: int
+    positions: list = field(default_factory=list)
 
 
 @dataclass(frozen=True)
@@ -166,9 +204,15 @@ def read_tiff_u16(path) -> np.ndarray:
     return out
 
 
+def _is_dir_arg(v) -> bool:
+    return isinstance(v, (str, os.PathLike))
+
+
 @dataclass
 class ControlMasks:
-    """Two-image control data (src/pano/controlMasks.h:30-66)."""
+    """Two-image control data (src/pano/controlMasks.h:30-66). ``ControlMasks(game_dir)`` loads a
+    control directory, as the reference's constructor does (cupano/masks.py:82-90); the fields can
+    also be given directly."""
 
     img1_col: np.ndarray = field(default_factory=lambda: np.empty((0, 0), np.uint16))
     img1_row: np.ndarray = field(default_factory=lambda: np.empty((0, 0), np.uint16))
@@ -176,6 +220,11 @@ class ControlMasks:
     img2_row: np.ndarray = field(default_factory=lambda: np.empty((0, 0), np.uint16))
     whole_seam_mask_image: np.ndarray = field(default_factory=lambda: np.empty((0, 0), np.uint8))
     positions: list = field(default_factory=list)
+
+    def __post_init__(self):
+        if _is_dir_arg(self.img1_col):
+            game_dir, self.img1_col = self.img1_col, np.empty((0, 0), np.uint16)
+            self.load(game_dir)
 
     def is_valid(self) -> bool:
         return bool(self.img1_col.size and self.img1_row.size and self.img2_col.size and self.img2_row.size
@@ -212,7 +261,8 @@ class ControlMasks:
 
 @dataclass
 class ControlMasks3:
-    """Three-image control data (src/pano/controlMasks3.h); the seam holds labels 0, 1, 2."""
+    """Three-image control data (src/pano/controlMasks3.h); the seam holds labels 0, 1, 2.
+    ``ControlMasks3(game_dir)`` loads a control directory, like the C++ constructor."""
 
     img0_col: np.ndarray = field(default_factory=lambda: np.empty((0, 0), np.uint16))
     img0_row: np.ndarray = field(default_factory=lambda: np.empty((0, 0), np.uint16))
@@ -222,6 +272,11 @@ class ControlMasks3:
     img2_row: np.ndarray = field(default_factory=lambda: np.empty((0, 0), np.uint16))
     whole_seam_mask_image: np.ndarray = field(default_factory=lambda: np.empty((0, 0), np.uint8))
     positions: list = field(default_factory=list)
+
+    def __post_init__(self):
+        if _is_dir_arg(self.img0_col):
+            game_dir, self.img0_col = self.img0_col, np.empty((0, 0), np.uint16)
+            self.load(game_dir)
 
     def is_valid(self) -> bool:
         return bool(all(a.size for a in (self.img0_col, self.img0_row, self.img1_col, self.img1_row, self.img2_col,
@@ -253,12 +308,21 @@ class ControlMasks3:
 
 @dataclass
 class ControlMasksN:
-    """N-image control data (src/pano/controlMasksN.h); the seam holds labels 0..N-1."""
+    """N-image control data (src/pano/controlMasksN.h); the seam holds labels 0..N-1.
+    ``ControlMasksN(directory, n_images)`` loads a control directory, as the reference's
+    constructor does when both are given (cupano/masks.py:133-139)."""
 
     img_col: list = field(default_factory=list)
     img_row: list = field(default_factory=list)
     whole_seam_mask_indexed: np.ndarray = field(default_factory=lambda: np.empty((0, 0), np.uint8))
     positions: list = field(default_factory=list)
+
+    def __post_init__(self):
+        if _is_dir_arg(self.img_col):
+            directory, n_images = self.img_col, self.img_row
+            self.img_col, self.img_row = [], []
+            if isinstance(n_images, int):
+                self.load(directory, n_images)
 
     def is_valid(self) -> bool:
         return bool(self.img_col and len(self.img_col) == len(self.img_row) and len(self.positions) == len(self.img_col)

@@ -259,6 +259,13 @@ def test_two_image_directory(hp, tmp_path):
     # inverted: the smallest value is image 1 (1), the largest 0
     np.testing.assert_array_equal(m.whole_seam_mask_image, (seam_file == 0).astype(np.uint8))
     assert m.canvas_width() == 65 and m.canvas_height() == 36
+    # the reference's constructor form, with a str or a path
+    for arg in (str(tmp_path), tmp_path):
+        m2 = hp.ControlMasks(arg)
+        assert m2.is_valid()
+        np.testing.assert_array_equal(m2.img1_col, mx[0])
+        np.testing.assert_array_equal(m2.whole_seam_mask_image, m.whole_seam_mask_image)
+    assert not hp.ControlMasks(str(tmp_path / "missing")).is_valid()
 
 
 def test_n_image_labels_remapped_and_counted(hp, tmp_path):
@@ -271,6 +278,10 @@ def test_n_image_labels_remapped_and_counted(hp, tmp_path):
     assert m.load(tmp_path, 3)
     np.testing.assert_array_equal(m.whole_seam_mask_indexed, labels)
     assert not hp.ControlMasksN().load(tmp_path, 4)  # three classes for four images
+    m2 = hp.ControlMasksN(str(tmp_path), 3)  # the reference's constructor form
+    assert m2.is_valid()
+    np.testing.assert_array_equal(m2.whole_seam_mask_indexed, labels)
+    assert not hp.ControlMasksN(str(tmp_path)).is_valid()  # without n_images nothing is loaded
 
 
 def test_three_image_seam_rules(hp, tmp_path):
@@ -281,6 +292,7 @@ def test_three_image_seam_rules(hp, tmp_path):
     m = hp.ControlMasks3()
     assert m.load(tmp_path / "ok")
     np.testing.assert_array_equal(m.whole_seam_mask_image, labels)
+    assert hp.ControlMasks3(tmp_path / "ok").is_valid()
     cf.write_control_dir(tmp_path / "grey", mx, my, [(0, 0), (10, 0), (20, 0)], labels, paletted=False)
     assert not hp.ControlMasks3().load(tmp_path / "grey")  # the three-image seam must be paletted
 

@@ -174,3 +174,15 @@ def test_python_mirror_takes_the_reference_constructor_arguments():
     assert not n.status.ok()
     with pytest.raises(ValueError, match="Unsupported backend"):
         hmpano.pano._check_backend("torch")
+
+
+def test_python_mirror_exports_the_reference_names():
+    """Every name cupano exports (cupano/__init__.py) is importable from the mirror."""
+    import hmpano
+
+    for name in ("CanvasInfo", "ControlMasks", "ControlMasksN", "CudaStatus", "CudaStatusError", "CudaStitchPano",
+                 "CudaStitchPanoN", "Rect", "SpatialTiff", "UNMAPPED_POSITION_VALUE"):
+        assert hasattr(hmpano, name), name
+    r = hmpano.Rect(2, 3, 10, 4).intersect(hmpano.Rect(8, 0, 10, 5))
+    assert (r.x, r.y, r.width, r.height, r.right, r.bottom, r.empty) == (8, 3, 4, 2, 12, 5, False)
+    assert hmpano.Rect(0, 0, 5, 5).intersect(hmpano.Rect(6, 0, 5, 5)).empty
