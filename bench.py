@@ -428,8 +428,9 @@ def main() -> None:
             prefix = f"{WORKLOAD}/L{args.levels}/{args.storage}"
             captured = json.loads(tp.read_text())
             traffic = captured.get(f"{prefix}/{dom}")
-            if B == 1 and args.filter == "refbox" and info["levels"] > 1:
-                frame_dram = ncu_frame_bytes(captured, prefix, names)
+            if B == 1 and args.filter == "refbox":
+                # The hard seam is the gather alone; a pyramid frame is all four kernels.
+                frame_dram = ncu_frame_bytes(captured, prefix, names if info["levels"] > 1 else ["canvas_gather"])
         except Exception:
             traffic = frame_dram = None
     line = {
