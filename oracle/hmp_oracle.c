@@ -36,7 +36,7 @@ typedef struct {
 static int g_threads = 0;
 /* Pixel channels of the stitch in progress: 4 (RGBA) or 3 (RGB, no alpha: plain means, plain
  * bilinear upsampling, blends without alpha tests, zero fill for out-of-range entries). The
- * op-level entry points below always run with 4. */
+ * op-level entry points below run with 4, except hmpo_laplacian_blend_ch_f32. */
 static int g_ch = 4;
 
 void hmpo_set_threads(int n) {
@@ -406,4 +406,14 @@ int hmpo_laplacian_blend_f32(const float* const* inputs, int n, const float* mas
     return HMPO_EINVAL;
   return laplacian_blend_f32(inputs, n, mask, k, w, h, effective_levels(w, h, levels), rule, HMPO_FILTER_REFBOX, 1,
                              out);
+}
+
+int hmpo_laplacian_blend_ch_f32(const float* const* inputs, int n, const float* mask, int k, int w, int h,
+                                int levels, int rule, int channels, float* out) {
+  if (channels != 3 && channels != 4)
+    return HMPO_EINVAL;
+  g_ch = channels;
+  const int rc = hmpo_laplacian_blend_f32(inputs, n, mask, k, w, h, levels, rule, out);
+  g_ch = 4;
+  return rc;
 }

@@ -101,6 +101,10 @@ void hmpo_blend_two_f32(const float* l1, const float* l2, const float* mask, int
 /* Full Laplacian blend of n full buffers (rule: 2 = two-image, 3 = three-image, 1 = N-way). */
 int hmpo_laplacian_blend_f32(const float* const* inputs, int n, const float* mask, int k, int w, int h, int levels,
                              int rule, float* out);
+/* The same with the arithmetic of 3 (RGB, no alpha) or 4 (RGBA) channels; buffers hold 4 floats
+ * per pixel either way (the fourth is ignored for 3). */
+int hmpo_laplacian_blend_ch_f32(const float* const* inputs, int n, const float* mask, int k, int w, int h,
+                                int levels, int rule, int channels, float* out);
 
 /* Threads used by the OpenMP loops (0 = library default). */
 void hmpo_set_threads(int n);

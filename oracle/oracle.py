@@ -76,6 +76,10 @@ def lib() -> C.CDLL:
         L.hmpo_reconstruct_rgba_f32.argtypes = [P(C.c_float), P(C.c_float), C.c_int, C.c_int, P(C.c_float)]
         L.hmpo_blend_two_f32.argtypes = [P(C.c_float), P(C.c_float), P(C.c_float), C.c_int, C.c_int, P(C.c_float)]
         L.hmpo_downsample_mask_f32.argtypes = [P(C.c_float), C.c_int, C.c_int, C.c_int, P(C.c_float)]
+        L.hmpo_blend_nway_f32.argtypes = [P(P(C.c_float)), C.c_int, P(C.c_float), C.c_int, C.c_int, P(C.c_float)]
+        L.hmpo_laplacian_blend_ch_f32.argtypes = [P(P(C.c_float)), C.c_int, P(C.c_float), C.c_int, C.c_int, C.c_int,
+                                                  C.c_int, C.c_int, C.c_int, P(C.c_float)]
+        L.hmpo_laplacian_blend_ch_f32.restype = C.c_int
         L.hmpo_set_threads.argtypes = [C.c_int]
         L.hmpo_get_threads.restype = C.c_int
         _lib = L
@@ -204,6 +208,45 @@ def blend_two_rgba(l1: np.ndarray, l2: np.ndarray, mask: np.ndarray) -> np.ndarr
     lib().hmpo_blend_two_f32(_ptr(l1, C.c_float), _ptr(l2, C.c_float), _ptr(mask, C.c_float), w, h,
                              _ptr(out, C.c_float))
     return out
+
+
+def blend_nway_rgba(laps, mask: np.ndarray) -> np.ndarray:
+    """One level of the N-way blend (cudaBlendN.cu:199-288): laps n x [h, w, 4], mask [h, w, n]."""
+    laps = [np.ascontiguousarray(a, dtype=np.float32) for a in laps]
+    mask = np.ascontiguousarray(mask, dtype=np.float32)
+    h, w = laps[0].shape[-3], laps[0].shape[-2]
+    ptrs = (C.POINTER(C.c_float) * len(laps))(*[_ptr(a, C.c_float) for a in laps])
+    out = np.zeros((h, w, 4), dtype=np.float32)
+    lib().hmpo_blend_nway_f32(ptrs, len(laps), _ptr(mask, C.c_float), w, h, _ptr(out, C.c_float))
+    return out
+
+
+RULE_NWAY, RULE_TWO, RULE_THREE = 1, 2, 3
+
+
+def laplacian_blend(images, mask: np.ndarray, levels: int, rule: int) -> np.ndarray:
+    """The whole Laplacian blend of full float buffers (cudaBlend.cu:847-1049, cudaBlend3.cu:881-1206,
+    cudaBlendN.cu:649-828): images n x [h, w, C] (C = 3 or 4), mask [h, w, k] (k = 1 for the
+    two-image rule, else one weight per image); returns [h, w, C]."""
+    h, w, ch = np.shape(images[0])
+    if ch not in (3, 4):
+        raise ValueError("images must have 3 or 4 channels")
+    # The oracle's float buffers hold 4 values per pixel in both modes (the 3-channel mode
+    # ignores the fourth).
+    padded = []
+    for a in images:
+        b = np.zeros((h, w, 4), dtype=np.float32)
+        b[..., :ch] = a
+        padded.append(b)
+    mask = np.ascontiguousarray(mask, dtype=np.float32)
+    k = mask.shape[-1] if mask.ndim == 3 else 1
+    ptrs = (C.POINTER(C.c_float) * len(padded))(*[_ptr(a, C.c_float) for a in padded])
+    out = np.zeros((h, w, 4), dtype=np.float32)
+    rc = lib().hmpo_laplacian_blend_ch_f32(ptrs, len(padded), _ptr(mask, C.c_float), k, w, h, int(levels), int(rule),
+                                           ch, _ptr(out, C.c_float))
+    if rc != 0:
+        raise ValueError(f"laplacian_blend: oracle error {rc}")
+    return out[..., :ch]
 
 
 def downsample_mask(mask: np.ndarray) -> np.ndarray:

@@ -81,3 +81,87 @@ def test_oracle_known_answers(golden, oracle_lib):
     for a, b in [("kat_pano2_pattern_l4_min", "kat_pano2_pattern_l4_full"),
                  ("kat_panon2_pattern_l4_min", "kat_panon2_pattern_l4_full")]:
         assert np.array_equal(golden[f"{a}/canvas"], golden[f"{b}/canvas"])
+
+
+def _px(*v):
+    return np.array(v, np.float32).reshape(1, 1, -1)
+
+
+def test_oracle_nway_blend_known_answers(oracle_lib):
+    """The reference's N-way blend tests (src/cuda/cudaBlendN_test.cpp:27-183), through the
+    oracle's whole Laplacian blend with a float mask (one weight per image), tolerance 1e-5 as there."""
+    o = oracle_lib
+    # An alpha-0 image drops out and the weights renormalise: 0.1/0.8/0.1 -> 0.5/0/0.5 (:27-70).
+    out = o.laplacian_blend([_px(10, 20, 30, 255), _px(100, 110, 120, 0), _px(90, 100, 110, 255)],
+                            _px(0.1, 0.8, 0.1), 1, o.RULE_NWAY)
+    np.testing.assert_allclose(out[0, 0], [50, 60, 70, 255], atol=1e-5)
+    # Four levels of constant images with weights 0.25 / 0.75 give the weighted mean everywhere (:73-139).
+    i0 = np.tile(np.array([10, 20, 30, 255], np.float32), (8, 8, 1))
+    i1 = np.tile(np.array([110, 120, 130, 255], np.float32), (8, 8, 1))
+    m = np.tile(np.array([0.25, 0.75], np.float32), (8, 8, 1))
+    out = o.laplacian_blend([i0, i1], m, 4, o.RULE_NWAY)
+    np.testing.assert_allclose(out.reshape(-1, 4), np.tile([85, 95, 105, 255], (64, 1)), atol=1e-5)
+    # The mask selects only a transparent image: the highest-alpha image is copied (:142-183).
+    out = o.laplacian_blend([_px(255, 0, 0, 255), _px(0, 255, 0, 0), _px(0, 0, 255, 128)], _px(0, 1, 0), 1,
+                            o.RULE_NWAY)
+    np.testing.assert_allclose(out[0, 0], [255, 0, 0, 255], atol=1e-5)
+
+
+def test_oracle_three_image_blend_known_answers(oracle_lib):
+    """The reference's three-image blend tests (src/cuda/cudaBlend3_test.cpp:62-387), through the
+    oracle's three-image rule, tolerance 1e-5 as there."""
+    o = oracle_lib
+    rgb = [_px(10, 20, 30), _px(40, 50, 60), _px(70, 80, 90)]
+    # One-hot masks pick one RGB image (:62-150).
+    for k in range(3):
+        w = [0.0, 0.0, 0.0]
+        w[k] = 1.0
+        np.testing.assert_allclose(o.laplacian_blend(rgb, _px(*w), 1, o.RULE_THREE)[0, 0], rgb[k][0, 0], atol=1e-5)
+    # Equal weights of 1, 2, 3 give 2 (:152-196).
+    out = o.laplacian_blend([np.full((2, 2, 3), v, np.float32) for v in (1, 2, 3)],
+                            np.full((2, 2, 3), 1 / 3, np.float32), 1, o.RULE_THREE)
+    np.testing.assert_allclose(out, 2.0, atol=1e-5)
+    # RGBA: colour weighted 0.2 / 0.3 / 0.5, alpha the largest (:198-248).
+    out = o.laplacian_blend([_px(10, 20, 30, 40), _px(50, 60, 70, 80), _px(90, 100, 110, 120)], _px(0.2, 0.3, 0.5), 1,
+                            o.RULE_THREE)
+    np.testing.assert_allclose(out[0, 0], [62, 72, 82, 120], atol=1e-5)
+    # An alpha-0 image drops out (:255-289) and a mask on a transparent image falls back (:291-328).
+    out = o.laplacian_blend([_px(10, 20, 30, 255), _px(100, 110, 120, 0), _px(90, 100, 110, 255)],
+                            _px(0.1, 0.8, 0.1), 1, o.RULE_THREE)
+    np.testing.assert_allclose(out[0, 0], [50, 60, 70, 255], atol=1e-5)
+    out = o.laplacian_blend([_px(255, 0, 0, 255), _px(0, 255, 0, 0), _px(0, 0, 255, 128)], _px(0, 1, 0), 1,
+                            o.RULE_THREE)
+    np.testing.assert_allclose(out[0, 0], [255, 0, 0, 255], atol=1e-5)
+    # Two levels across a top/bottom seam leave no alpha holes and no vanished colour (:330-387).
+    imgs = []
+    for c, v in ((0, 100), (1, 150), (2, 200)):
+        a = np.zeros((4, 4, 4), np.float32)
+        a[..., c] = v
+        a[..., 3] = 255
+        imgs.append(a)
+    m = np.zeros((4, 4, 3), np.float32)
+    m[:2, :, 0] = 1
+    m[2:, :, 1] = 1
+    out = o.laplacian_blend(imgs, m, 2, o.RULE_THREE)
+    for y in (1, 2):
+        assert (out[y, :, 3] >= 250).all() and (out[y, :, :3].sum(axis=-1) > 50).all()
+
+
+@pytest.mark.parametrize("name", ["two_way_overlap", "no_overlap", "gap", "multi_seam_intersection"])
+def test_oracle_reference_pano_layouts(oracle_lib, name):
+    """The reference's N-image stitcher tests (src/pano/cudaPanoN_test.cpp:192-298) on the oracle:
+    the minimised blend equals the full-canvas blend (there within 1e-4 on float pixels; here the
+    uint8 canvases are equal), and an uncovered gap stays transparent."""
+    import pano_layouts as pl
+
+    lay = pl.layouts()[name]
+    mx, my = pl.tables(lay)
+    px, py = zip(*lay["positions"])
+    fr = pl.frames(lay)
+    outs = [oracle_lib.Stitch(pl.KIND_PANON, mx, my, px, py, lay["seam"], lay["levels"], 1, minimize).run(fr)
+            for minimize in (False, True)]
+    assert np.array_equal(outs[0], outs[1]), name
+    if lay["gap"]:
+        x0, x1 = lay["gap"]
+        assert (outs[1][0, :, x0:x1, 3] == 0).all()
+        assert (outs[1][0, :, :x0, 3] == 255).all() and (outs[1][0, :, x1:, 3] == 255).all()
