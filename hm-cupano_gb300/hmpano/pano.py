@@ -411,14 +411,17 @@ def _pixel_type(t) -> tuple[int, bool]:
 
 def _image(t) -> Image:
     """hmp_image over a [B, H, W, C] CUDA tensor (C = 4 or 3; uint8 or float32) with dense pixels
-    and frames (the row pitch may exceed the row)."""
+    and frames (the row pitch may exceed the row). The stride of a dimension of size 1 is not
+    used (numpy's `a[None]` gives such an axis stride 0)."""
     ch, _ = _pixel_type(t)
     if not t.is_cuda:
         raise ValueError("images must live on a CUDA device")
     B, H, W, _ = t.shape
-    if t.stride(3) != 1 or t.stride(2) != ch or t.stride(0) != t.stride(1) * H:
+    pitch = t.stride(1) if H > 1 else W * ch
+    if (t.stride(3) != 1 or (W > 1 and t.stride(2) != ch) or pitch < W * ch
+            or (B > 1 and t.stride(0) != pitch * H)):
         raise ValueError("images need dense pixels, rows and frames (row pitch may exceed the row)")
-    return Image(C.c_void_p(t.data_ptr()), int(W), int(H), int(t.stride(1)) * t.element_size())
+    return Image(C.c_void_p(t.data_ptr()), int(W), int(H), int(pitch) * t.element_size())
 
 
 class _Stitcher:
