@@ -165,3 +165,20 @@ def test_oracle_reference_pano_layouts(oracle_lib, name):
         x0, x1 = lay["gap"]
         assert (outs[1][0, :, x0:x1, 3] == 0).all()
         assert (outs[1][0, :, :x0, 3] == 255).all() and (outs[1][0, :, x1:, 3] == 255).all()
+
+
+def test_oracle_three_image_trivial_stitches(oracle_lib):
+    """The reference's three-image stitcher tests (src/pano/cudaPano3_test.cpp:56-196) on a 1x1
+    canvas with all three tables at (0, 0): label 2 under the hard seam takes the third (RGB)
+    image; label 1 with one level takes the middle image, alpha kept."""
+    z = [np.zeros((1, 1), np.uint16)] * 3
+    st = oracle_lib.Stitch(3, z, z, [0, 0, 0], [0, 0, 0], np.array([[2]], np.uint8), 0)
+    out = st.run([np.full((1, 1, 1, 3), v, np.uint8) for v in (10, 50, 200)])
+    assert (st.canvas_w, st.canvas_h) == (1, 1) and out[0, 0, 0].tolist() == [200, 200, 200]
+    frames = []
+    for v in (30, 60, 90):
+        f = np.full((1, 1, 1, 4), v, np.uint8)
+        f[..., 3] = 255
+        frames.append(f)
+    out = oracle_lib.Stitch(3, z, z, [0, 0, 0], [0, 0, 0], np.array([[1]], np.uint8), 1).run(frames)
+    assert out[0, 0, 0].tolist() == [60, 60, 60, 255]
