@@ -556,6 +556,11 @@ class _Stitcher:
                 raise ValueError("canvas pixel type must match the inputs'")
         imgs = (Image * len(batched))(*[_image(t) for t in batched])
         cv = _image(canvas)
+        # The library checks that the current device is the stitcher's; the tensors must live there
+        # too (a pointer into another GPU's memory would be read by this GPU's kernels).
+        current = torch.cuda.current_device()
+        if any(t.device.index != current for t in [*batched, canvas]):
+            raise ValueError(f"inputs and canvas must be on the current CUDA device (cuda:{current})")
         if stream is None:
             stream = torch.cuda.current_stream(device).cuda_stream
         elif hasattr(stream, "cuda_stream"):
