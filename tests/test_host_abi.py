@@ -186,3 +186,44 @@ def test_python_mirror_exports_the_reference_names():
     r = hmpano.Rect(2, 3, 10, 4).intersect(hmpano.Rect(8, 0, 10, 5))
     assert (r.x, r.y, r.width, r.height, r.right, r.bottom, r.empty) == (8, 3, 4, 2, 12, 5, False)
     assert hmpano.Rect(0, 0, 5, 5).intersect(hmpano.Rect(6, 0, 5, 5)).empty
+
+
+def test_c_abi_rejects_bad_arguments_before_any_device_work(lib):
+    """Argument errors come back as statuses with the reference's cudaError_t values, without a
+    GPU: null handles, server options, batch-job rules (stitcher handles are only compared, never
+    used, by hmp_batch_add)."""
+    from hmpano import _lib
+
+    info = _lib.StitcherInfo()
+    assert lib.hmp_stitcher_get_info(None, C.byref(info)).code == 1
+    assert lib.hmp_stitcher_process(None, None, 0, None, None).code == 1
+    assert lib.hmp_stitcher_set_tiles(None, 64, 32).code == 1
+    assert lib.hmp_stitcher_status(None).code == 1
+    assert lib.hmp_stitcher_canvas_width(None) == 0
+    lib.hmp_stitcher_destroy(None)  # no-op
+
+    srv = C.c_void_p()
+    for budget, slots in ((0, 4), (1 << 30, 0), (1 << 30, 65)):
+        opt = _lib.ServerOptions(budget, slots, 2)
+        assert lib.hmp_server_create(C.byref(opt), C.byref(srv)).code == 1 and not srv
+
+    b = C.c_void_p()
+    assert lib.hmp_batch_create(C.byref(b)).code == 0 and b
+    try:
+        img = (_lib.Image * 2)()
+        canvas = _lib.Image()
+        st1, st2 = C.c_void_p(0x1000), C.c_void_p(0x2000)
+        assert lib.hmp_batch_add(b, st1, img, 2, C.byref(canvas), 0).code == 0
+        assert lib.hmp_batch_add(b, st1, img, 2, C.byref(canvas), 0).code == 0  # in order, same index
+        s = lib.hmp_batch_add(b, st1, img, 2, C.byref(canvas), 1)  # one stitcher, two stream indices
+        assert s.code == 1 and b"one stream index" in s.message
+        assert lib.hmp_batch_add(b, st2, img, 2, C.byref(canvas), 1).code == 0
+        assert lib.hmp_batch_add(b, st2, img, 2, C.byref(canvas), 256).code == 1
+        assert lib.hmp_batch_add(b, st2, img, 0, C.byref(canvas), 1).code == 1
+        assert lib.hmp_batch_add(b, None, img, 2, C.byref(canvas), 1).code == 1
+    finally:
+        lib.hmp_batch_destroy(b)  # nothing was captured: no CUDA objects to release
+    assert lib.hmp_batch_capture(None, None).code == 1 and lib.hmp_batch_launch(None, None).code == 1
+
+    d = C.POINTER(_lib.ControlDir)()
+    assert lib.hmp_control_dir_load(b"/nonexistent", 99, 2, C.byref(d)).code == 1 and not d
