@@ -20,13 +20,21 @@
  *   hmp_stitcher_dump_pyramid <- CudaStitchPano::dump_soft_blend_pyramid(directory, stream)
  *                                                                    src/pano/cudaPano.h:101
  *   hmp_stitcher_destroy  <- ~CudaStitchPano*()
+ *   hmp_control_dir_load  <- ControlMasks::load / ControlMasks3::load / ControlMasksN::load
+ *                            src/pano/controlMasks.cpp:133-326, controlMasks3.cpp:186-300,
+ *                            controlMasksN.cpp:22-193
+ *   hmp_blend2_noalloc    <- cudaBatchedLaplacianBlend (two-image blend without a stitcher)
+ *                            src/cuda/cudaBlend.cu:678-843, without its allocations
+ *   hmp_batch_*, hmp_server_*: no counterpart (the reference stitches one configuration per
+ *                            process, one call at a time)
  *
  * Error convention (src/cuda/cudaStatus.h:12-75): every call returns an hmp_status whose code is
  * a cudaError_t value (0 = success) with a message. Construction errors are also kept as the
  * stitcher's sticky status; process() first returns the sticky status, then the per-call error,
  * and a per-call error becomes sticky (src/pano/cudaPano.inl:460-472).
  *
- * Data: images are RGBA8 (uchar4), device memory, frame b of a batch at data + b*pitch*height.
+ * Data: images are RGBA8 (uchar4) unless hmp_config.channels / pixel_format select uchar3, float4
+ * or float3; device memory, frame b of a batch at data + b*pitch*height.
  * Remap tables, positions and the seam are host data consumed at create time (the ControlMasks
  * of the reference, already loaded: the two-image seam is in its inverted form, 1 = image 1;
  * the three/N-image seam holds labels 0..n-1). Positions are normalised (minimum 0).
