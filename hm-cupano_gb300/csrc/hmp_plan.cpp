@@ -402,13 +402,13 @@ int build_plan(const hmp_config& c, Plan& p, std::string& m) {
   // The N-way kernels pick from the class alone unless the weights are fractional.
   p.mask_hot.assign(p.levels, {});
   for (int l = 1; p.rule == kRuleNway && l < p.levels; ++l) {
-    const std::vector<float>& m = p.mask_levels[l];
+    const std::vector<float>& wts = p.mask_levels[l];
     std::vector<uint8_t>& h = p.mask_hot[l];
     h.resize(size_t(p.lw[l]) * p.lh[l]);
     for (size_t i = 0; i < h.size(); ++i) {
       int hot = kHotNone;
       for (int k = 0; k < K && hot != kHotFrac; ++k) {
-        const float w = m[i * K + k];
+        const float w = wts[i * K + k];
         if (w == 1.0f)
           hot = hot == kHotNone ? k : kHotFrac;
         else if (w != 0.0f)
