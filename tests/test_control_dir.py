@@ -352,3 +352,42 @@ def test_cpp_drop_in_loads_the_same_directory(hp, tmp_path):
               m.whole_seam_mask_image.shape[0], m.positions[0].xpos, m.positions[0].ypos, m.positions[1].xpos,
               m.positions[1].ypos, h(m.img1_col), h(m.img2_row), h(m.whole_seam_mask_image)]
     assert [float(x) for x in out] == [float(x) for x in expect]
+
+
+def test_decoders_survive_mutated_files_under_sanitizers(tmp_path):
+    """tests/cpp/decoder_fuzz.cpp, built with AddressSanitizer and UndefinedBehaviorSanitizer around
+    the decoders' own source, decodes thousands of randomly mutated TIFF and PNG files (written from
+    the format specifications by control_files.py): each is accepted or rejected, and no memory
+    error or undefined behaviour occurs."""
+    import shutil
+    import subprocess
+
+    if shutil.which("g++") is None:
+        pytest.skip("no g++")
+    repo = Path(__file__).resolve().parents[1]
+    exe = tmp_path / "decoder_fuzz"
+    r = subprocess.run(["g++", "-std=c++17", "-O1", "-g", "-fsanitize=address,undefined",
+                        "-fno-sanitize-recover=undefined", "-I", str(repo / "include"),
+                        str(repo / "tests" / "cpp" / "decoder_fuzz.cpp"),
+                        str(repo / "hm-cupano_gb300" / "csrc" / "hmp_control_dir.cpp"), "-o", str(exe)],
+                       capture_output=True, text=True)
+    if r.returncode != 0:
+        pytest.skip(f"no sanitizer runtime: {r.stderr.strip()[:200]}")
+    seeds = tmp_path / "seeds"
+    seeds.mkdir()
+    rng = np.random.default_rng(0)
+    img = rng.integers(0, 65535, (37, 53)).astype(np.uint16)
+    for i, (comp, pred, be, kw) in enumerate([(c, p, b, k) for c in (1, 5, 8, 32773) for p in (1, 2)
+                                               for b in (False, True) for k in ({"rows_per_strip": 7}, {"tile": 16})]):
+        cf.write_tiff(seeds / f"t{i}.tif", img, big_endian=be, compression=comp, predictor=pred, **kw)
+    cf.write_png(seeds / "p.png", rng.integers(0, 9, (37, 53)), color_type=3, palette=rng.integers(0, 256, (9, 3)))
+    for depth in (1, 4, 8, 16):
+        cf.write_png(seeds / f"g{depth}.png", rng.integers(0, 1 << depth, (19, 29)), color_type=0, bit_depth=depth)
+    cf.write_png(seeds / "c.png", rng.integers(0, 256, (11, 17, 3)), color_type=2)
+    files = sorted(str(p) for p in seeds.iterdir())
+    env = dict(__import__("os").environ, ASAN_OPTIONS="detect_leaks=1:abort_on_error=0")
+    out = subprocess.run([str(exe), "6000", "2024", str(tmp_path / "scratch"), *files], capture_output=True, text=True,
+                         env=env, timeout=600)
+    assert out.returncode == 0, out.stderr[-2000:]
+    decoded, rejected = (int(v) for v in out.stdout.split()[1::2])
+    assert decoded > 0 and rejected > 0 and decoded + rejected == 6000
