@@ -227,3 +227,46 @@ def test_c_abi_rejects_bad_arguments_before_any_device_work(lib):
 
     d = C.POINTER(_lib.ControlDir)()
     assert lib.hmp_control_dir_load(b"/nonexistent", 99, 2, C.byref(d)).code == 1 and not d
+
+
+def _sanitized_build(tmp_path, name, sources, compiler):
+    import shutil
+    import subprocess
+
+    if shutil.which(compiler) is None:
+        pytest.skip(f"no {compiler}")
+    exe = tmp_path / name
+    std = "-std=c++17" if compiler == "g++" else "-std=c11"
+    r = subprocess.run([compiler, std, "-O1", "-g", "-fsanitize=address,undefined", "-fno-sanitize-recover=undefined",
+                        "-I", str(REPO / "include"), "-I", str(REPO / "hm-cupano_gb300" / "csrc"),
+                        "-I", str(REPO / "oracle"), *[str(s) for s in sources], "-lm", "-o", str(exe)],
+                       capture_output=True, text=True)
+    if r.returncode != 0:
+        pytest.skip(f"no sanitizer runtime: {r.stderr.strip()[:200]}")
+    return exe
+
+
+def test_planner_under_sanitizers(tmp_path):
+    """tests/cpp/plan_fuzz.cpp: thousands of random configurations through the planner built with
+    AddressSanitizer and UndefinedBehaviorSanitizer; each is planned or rejected, none misbehaves."""
+    import subprocess
+
+    exe = _sanitized_build(tmp_path, "plan_fuzz", [REPO / "tests" / "cpp" / "plan_fuzz.cpp",
+                                                   REPO / "hm-cupano_gb300" / "csrc" / "hmp_plan.cpp"], "g++")
+    out = subprocess.run([str(exe), "3000", "5"], capture_output=True, text=True, timeout=600)
+    assert out.returncode == 0, out.stderr[-2000:]
+    planned, rejected = (int(v) for v in out.stdout.split()[1::2])
+    assert planned > 0 and rejected > 0
+
+
+def test_oracle_under_sanitizers(tmp_path):
+    """tests/cpp/oracle_fuzz.c: random stitches through the oracle (the parity checker) built with
+    AddressSanitizer and UndefinedBehaviorSanitizer; each runs or is rejected, none misbehaves."""
+    import subprocess
+
+    exe = _sanitized_build(tmp_path, "oracle_fuzz", [REPO / "tests" / "cpp" / "oracle_fuzz.c",
+                                                     REPO / "oracle" / "hmp_oracle.c"], "gcc")
+    out = subprocess.run([str(exe), "1500", "3"], capture_output=True, text=True, timeout=600)
+    assert out.returncode == 0, out.stderr[-2000:]
+    ran, rejected = (int(v) for v in out.stdout.split()[1::2])
+    assert ran > 0 and rejected > 0
