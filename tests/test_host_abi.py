@@ -270,3 +270,52 @@ def test_oracle_under_sanitizers(tmp_path):
     assert out.returncode == 0, out.stderr[-2000:]
     ran, rejected = (int(v) for v in out.stdout.split()[1::2])
     assert ran > 0 and rejected > 0
+
+
+def test_plan_geometry_matches_oracle_on_random_configurations(oracle_lib):
+    """The product's planner and the oracle agree on every random configuration: both reject it,
+    or both give the same canvas, blend region, write region and effective level count."""
+    import hmpano
+    from helpers import masks_for
+
+    rng = np.random.default_rng(2026)
+    agreed = rejected = 0
+    for _ in range(300):
+        kind = int(rng.choice([1, 2, 3]))
+        n = {2: 2, 3: 3}.get(kind, int(rng.integers(2, 9)))
+        mx, my, px, py = [], [], [], []
+        for _i in range(n):
+            w, h = int(rng.integers(8, 400)), int(rng.integers(8, 120))
+            mx.append(np.tile(np.arange(w, dtype=np.uint16), (h, 1)))
+            my.append(np.tile(np.arange(h, dtype=np.uint16)[:, None], (1, w)))
+            px.append(int(rng.integers(0, 300)))
+            py.append(int(rng.integers(0, 40)))
+        cw = max(x + m.shape[1] for x, m in zip(px, mx))
+        ch = max(y + m.shape[0] for y, m in zip(py, mx))
+        labels = 2 if kind == 2 else n
+        seam = rng.integers(0, labels, (ch, cw)).astype(np.uint8)
+        if rng.random() < 0.5:  # a few large regions instead of noise
+            cuts = np.sort(rng.integers(0, cw, labels - 1))
+            seam = np.searchsorted(cuts, np.arange(cw), side="right").astype(np.uint8)[None, :].repeat(ch, 0)
+        levels = int(rng.integers(0, 8))
+        minimize = bool(rng.integers(0, 2))
+        try:
+            g = hmpano.plan_geometry(kind, masks_for(kind, mx, my, px, py, seam), levels, minimize)
+        except hmpano.CudaStatusError:
+            g = None
+        try:  # the oracle checks a configuration when it plans the stitch (at every level count)
+            st = oracle_lib.Stitch(kind, mx, my, px, py, seam, levels, 1, minimize)
+            og = st.geometry()
+            canvas = (st.canvas_w, st.canvas_h)
+        except ValueError:
+            st = None
+        if g is None or st is None:
+            assert g is None and st is None, (kind, n, levels, minimize)
+            rejected += 1
+            continue
+        assert g["canvas"] == canvas
+        if levels:
+            assert (g["blend"], g["write"], g["levels"]) == (og["blend"], og["write"], og["levels"]), \
+                (kind, n, levels, minimize)
+        agreed += 1
+    assert agreed > 200
