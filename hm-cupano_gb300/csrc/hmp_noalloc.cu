@@ -115,7 +115,8 @@ extern "C" HMP_API hmp_status hmp_blend2_noalloc(const hmp_image* image1, const 
   if (!seam || seam_pitch < size_t(w) || seam_pitch > size_t(INT_MAX))
     return status_of(HMP_ERR_INVALID_VALUE, "seam must be a device pointer with pitch >= width");
   if (num_levels < 1 || num_levels > 30) return status_of(HMP_ERR_INVALID_VALUE, "num_levels must be in 1..30");
-  if (batch_size < 1) return status_of(HMP_ERR_INVALID_VALUE, "batch_size must be >= 1");
+  // Bounds every scratch size below (batch x level pixels x 16 bytes) far from overflow.
+  if (batch_size < 1 || batch_size > 65536) return status_of(HMP_ERR_INVALID_VALUE, "batch_size must be in 1..65536");
   const int L = hmp::effective_levels(w, h, num_levels);
   if (L > hmp::kMaxLevels)
     return status_of(HMP_ERR_NOT_SUPPORTED, "more than 7 effective pyramid levels are not supported");

@@ -96,7 +96,9 @@ int validate(const hmp_config& c, std::string& m) {
   if (c.n_images < 2 || c.n_images > kMaxImages)
     return fail(m, HMP_ERR_INVALID_VALUE, "Unsupported N for blend (supported 2..8)");
   if (c.num_levels < 0 || c.num_levels > 30) return fail(m, HMP_ERR_INVALID_VALUE, "num_levels out of range");
-  if (c.batch_size < 1) return fail(m, HMP_ERR_INVALID_VALUE, "batch_size must be >= 1");
+  // With canvases below 2^20 pixels per side, 2^16 frames keep every byte count below 2^60.
+  if (c.batch_size < 1 || c.batch_size > 65536)
+    return fail(m, HMP_ERR_INVALID_VALUE, "batch_size must be in 1..65536");
   if (c.channels != 4 && c.channels != 3) return fail(m, HMP_ERR_NOT_SUPPORTED, "only 3- and 4-channel pixels are supported");
   if (c.pixel_format != HMP_PIXEL_U8 && c.pixel_format != HMP_PIXEL_F32)
     return fail(m, HMP_ERR_INVALID_VALUE, "unknown pixel format");

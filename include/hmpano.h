@@ -99,7 +99,7 @@ typedef struct hmp_config {
   int kind;           /* HMP_KIND_* */
   int n_images;       /* 2 (PANO2), 3 (PANO3), 2..8 (PANON) */
   int num_levels;     /* 0 = hard seam; pyramid levels otherwise */
-  int batch_size;     /* frames per process() call */
+  int batch_size;     /* frames per process() call, 1..65536 */
   int channels;       /* 4 (RGBA) or 3 (RGB) */
   int minimize_blend; /* PANO2 / PANON: blend only the seam region (reference default: 1) */
   int fused;          /* PANO3: 1 = fused remap (reference default), 0 = legacy remap+copy */
@@ -261,8 +261,9 @@ HMP_API hmp_status hmp_stitcher_get_timing(hmp_stitcher* st, hmp_kernel_timing* 
  * equals hmp_stitcher_process of a two-image stitcher whose tables are the identity, with both
  * images at (0, 0) and minimize_blend = 0. Work is enqueued on `stream`.
  *
- * Sizes whose scratch exceeds HMP_NOALLOC_SCRATCH_BYTES are rejected with HMP_ERR_INVALID_VALUE
- * and a message giving the bytes needed. The first call on a device does the set-up (it looks up
+ * batch_size is 1..65536. Sizes whose scratch exceeds HMP_NOALLOC_SCRATCH_BYTES are rejected with
+ * HMP_ERR_INVALID_VALUE and a message giving the bytes needed. The first call on a device does the
+ * set-up (it looks up
  * the array's device address and sets kernel attributes), so make it before any stream capture.
  * Every call shares the one array, which keeps the last call's contents; calls whose work
  * overlaps on the GPU (other streams, other host threads) race on it and must be serialised. */

@@ -142,6 +142,9 @@ def test_create_rejects_invalid_configurations(lib):
     mN = hmpano.ControlMasksN([mx, mx], [my, my], np.zeros((h, w), np.uint8), [hmpano.SpatialTiff(0, 0)] * 2)
     code, msg = _create(lib, mN, _lib.KIND_PANON, 9, minimize_blend=False)
     assert code == 801 and "levels" in msg
+    # a batch whose level bytes would overflow (rejected before any sizing)
+    code, msg = _create(lib, _two_image_masks(), _lib.KIND_PANO2, 3, batch=1 << 30)
+    assert code == 1 and "65536" in msg
     # a position that puts the canvas beyond 2^20 pixels per side (rejected before any sizing)
     m = _two_image_masks()
     m.positions = [hmpano.SpatialTiff(0, 0), hmpano.SpatialTiff(float(1 << 21), 0)]
