@@ -263,8 +263,8 @@ HMP_API hmp_status hmp_stitcher_get_timing(hmp_stitcher* st, hmp_kernel_timing* 
  *
  * batch_size is 1..65536. Sizes whose scratch exceeds HMP_NOALLOC_SCRATCH_BYTES are rejected with
  * HMP_ERR_INVALID_VALUE and a message giving the bytes needed. The first call on a device does the
- * set-up (it looks up
- * the array's device address and sets kernel attributes), so make it before any stream capture.
+ * set-up (it looks up the array's device address and sets kernel attributes), so make it before
+ * any stream capture.
  * Every call shares the one array, which keeps the last call's contents; calls whose work
  * overlaps on the GPU (other streams, other host threads) race on it and must be serialised. */
 HMP_API hmp_status hmp_blend2_noalloc(const hmp_image* image1, const hmp_image* image2, const uint8_t* seam,
