@@ -710,12 +710,15 @@ struct hmp_stitcher {
     if (canvas->width != p.canvas_w || canvas->height != p.canvas_h || canvas->pitch < size_t(canvas->width) * pxb ||
         canvas->pitch % align != 0)
       return make_status(HMP_ERR_INVALID_VALUE, "canvas size does not match the stitcher");
+    // The kernels load and store whole 4-byte words of RGBA8 and float pixels.
+    if (reinterpret_cast<uintptr_t>(canvas->data) % align != 0)
+      return make_status(HMP_ERR_INVALID_VALUE, "canvas data must be aligned to 4 bytes");
     for (int i = 0; i < n_inputs; ++i) {
       const hmp_image& im = inputs[i];
       if (!im.data) return make_status(HMP_ERR_INVALID_DEVICE_POINTER, "input image is null");
       if (im.width <= 0 || im.height <= 0 || im.pitch < size_t(im.width) * pxb || im.pitch > size_t(INT_MAX) ||
-          im.pitch % align != 0)
-        return make_status(HMP_ERR_INVALID_VALUE, "input image has an invalid size or pitch");
+          im.pitch % align != 0 || reinterpret_cast<uintptr_t>(im.data) % align != 0)
+        return make_status(HMP_ERR_INVALID_VALUE, "input image has an invalid size, pitch or alignment");
       if (!generic && size_t(im.height) * (im.pitch / 4) >= size_t(hmp::kOffMask) - 1)
         return make_status(HMP_ERR_NOT_SUPPORTED, "input frames must hold fewer than 2^29 - 2 pixels");
       if (im.width >= 65535 || im.height >= 65535)
