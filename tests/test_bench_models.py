@@ -48,3 +48,24 @@ def test_frame_dram_needs_every_kernel():
     total = b.ncu_frame_bytes(captured, prefix, names)
     assert total == sum(captured[f"{prefix}/{k}"] for k in names)
     assert b.ncu_frame_bytes(captured, prefix, names + ["missing"]) is None
+
+
+def test_clock_summary_keeps_the_timed_window_and_reasons():
+    """nvidia-smi samples (index, sm, max sm, power, active, hw_slowdown, hw_thermal, sw_thermal,
+    sw_power_cap) are kept only inside the timed window; the median SM clock, the largest maximum
+    and every active throttle reason are reported."""
+    b = _bench()
+    s = b.ClockSampler(0)
+    rows = [
+        (0.5, "0, 1200, 2070, 500, 0x0, Not Active, Not Active, Not Active, Not Active"),
+        (1.0, "0, 2070, 2070, 900, 0x0, Not Active, Not Active, Not Active, Not Active"),
+        (1.1, "0, 2060, 2070, 950, 0x4, Not Active, Not Active, Not Active, Active"),
+        (1.2, "0, 2070, 2070, 960, 0x0, Not Active, Not Active, Not Active, Not Active"),
+        (1.3, "0, [N/A], 2070, 960, 0x0, Not Active"),  # a short or malformed line is skipped
+        (3.0, "0, 900, 2070, 300, 0x40, Active, Not Active, Not Active, Not Active"),
+    ]
+    s.stamped = [(t, [v.strip() for v in line.split(",")]) for t, line in rows]
+    s.mark(0.9, 2.0)
+    out = s.summary()
+    assert out["sm_mhz"] == 2070.0 and out["sm_max_mhz"] == 2070.0
+    assert out["reasons"] == ["sw_power_cap"] and out["samples"] == 4
