@@ -322,3 +322,22 @@ def test_plan_geometry_matches_oracle_on_random_configurations(oracle_lib):
                 (kind, n, levels, minimize)
         agreed += 1
     assert agreed > 200
+
+
+def test_c_abi_header_is_plain_c(tmp_path):
+    """include/hmpano.h compiles as strict C99 and C++11 with every warning an error: any FFI that
+    reads C headers (cgo, JNI, N-API, ctypes generators) can take it as is."""
+    import shutil
+    import subprocess
+
+    src_c = tmp_path / "abi.c"
+    src_c.write_text('#include "hmpano.h"\nint main(void) { hmp_config c = {0}; hmp_image i = {0}; (void)c; (void)i; '
+                     'return hmp_version() == 0; }\n')
+    src_cpp = tmp_path / "abi.cpp"
+    src_cpp.write_text('#include "hmpano.h"\nint main() { hmp_config c{}; (void)c; return hmp_version() == nullptr; }\n')
+    for cc, std, src in (("gcc", "-std=c99", src_c), ("g++", "-std=c++11", src_cpp)):
+        if shutil.which(cc) is None:
+            pytest.skip(f"no {cc}")
+        r = subprocess.run([cc, std, "-Wall", "-Wextra", "-pedantic", "-Werror", "-I", str(REPO / "include"),
+                            "-fsyntax-only", str(src)], capture_output=True, text=True)
+        assert r.returncode == 0, r.stderr
