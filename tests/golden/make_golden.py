@@ -56,6 +56,31 @@ def _install_stubs() -> None:
     sys.modules.setdefault("PIL.Image", pil.Image)
 
 
+def install_corrections(ref_ops) -> None:
+    """The port's workspace downsamples leave the 2x2 sum in their output buffer (module
+    docstring); write the mean there, as the CUDA kernels do."""
+    sum_only = ref_ops._downsample_mask_torch
+
+    def _downsample_mask_mean(mask, out=None):
+        result = sum_only(mask, out=out)
+        if out is not None:
+            out.copy_(result)
+            return out
+        return result
+
+    ref_ops._downsample_mask_torch = _downsample_mask_mean
+    image_sum_only = ref_ops._downsample_image_torch
+
+    def _downsample_image_mean(image, out=None):
+        result = image_sum_only(image, out=out)
+        if out is not None and result is not out:
+            out.copy_(result)
+            return out
+        return result
+
+    ref_ops._downsample_image_torch = _downsample_image_mean
+
+
 def _cases():
     """(name, rig parameters, levels, minimize, batch, oob_fraction, frame seed)."""
     p2 = dict(canvas_w=480, canvas_h=40, n=2, src_w=230, src_h=36, overlap=90, yaw_step_deg=50.0)
@@ -195,26 +220,7 @@ def main() -> None:
     from cupano import ops as ref_ops
     from cupano.ops import compute_laplacian
 
-    _sum_only = ref_ops._downsample_mask_torch
-
-    def _downsample_mask_mean(mask, out=None):
-        result = _sum_only(mask, out=out)
-        if out is not None:
-            out.copy_(result)
-            return out
-        return result
-
-    ref_ops._downsample_mask_torch = _downsample_mask_mean
-    _image_sum_only = ref_ops._downsample_image_torch
-
-    def _downsample_image_mean(image, out=None):
-        result = _image_sum_only(image, out=out)
-        if out is not None and result is not out:
-            out.copy_(result)
-            return out
-        return result
-
-    ref_ops._downsample_image_torch = _downsample_image_mean
+    install_corrections(ref_ops)
 
     store: dict[str, np.ndarray] = {}
     names = []
