@@ -9,7 +9,8 @@
 //   down      4 channels: the alpha-aware 2x2 mean (DownAcc); 3 channels: the plain mean of the
 //             in-bounds pixels (cudaBlend.cu:46-144)
 //   up        4 channels: the alpha-aware bilinear upsample (up_alpha); 3 channels: the separable
-//             bilinear one (cudaBlend.cu:389-455)
+//             bilinear one in the Laplacian (cudaBlend.cu:389-455) and the sequential four-tap sum
+//             in the reconstruction (up_taps; cudaBlend.cu:581-672, cudaBlendN.cu:372-447)
 //   blend     4 channels: blend_level / blend_level0 (the reference rules, alpha tests included);
 //             3 channels: two images m*a + (1-m)*b (cudaBlend.cu:520-576), three m1*v1 + m2*v2 +
 //             m3*v3 (cudaBlend3.cu:376-531), N the mask normalised by its sum (cudaBlendN.cu:199-288)
@@ -89,6 +90,33 @@ __device__ __forceinline__ float3 up_level(const float4* lo, int lw, int lh, int
     return up_alpha(lo, lw, 0, 0, lw, lh, x, y);
   else
     return up_plain(lo, lw, lh, x, y);
+}
+
+// The reconstruction's upsample of 3-channel pixels: the sequential four-tap sum
+// (((0 + v00 w00) + v10 w10) + v01 w01) + v11 w11 of the reference's reconstructions
+// (src/cuda/cudaBlend.cu:581-672 and src/cuda/cudaBlendN.cu:372-447, whose weight sum is exactly 1
+// here; cupano/ops.py:514-565). It rounds differently from the Laplacian's separable form at pixels
+// with odd x and odd y once a level holds blended (non-dyadic) values.
+__device__ __forceinline__ float3 up_taps(const float4* lo, int lw, int lh, int x, int y) {
+  const int gxi = x >> 1, gyi = y >> 1;
+  const float dx = (x & 1) ? 0.5f : 0.f, dy = (y & 1) ? 0.5f : 0.f;
+  const int gxi1 = min(gxi + 1, lw - 1), gyi1 = min(gyi + 1, lh - 1);
+  const float4 v00 = lo[(long long)gyi * lw + gxi], v10 = lo[(long long)gyi * lw + gxi1];
+  const float4 v01 = lo[(long long)gyi1 * lw + gxi], v11 = lo[(long long)gyi1 * lw + gxi1];
+  const float ex = 1.f - dx, ey = 1.f - dy;
+  const float w00 = ex * ey, w10 = dx * ey, w01 = ex * dy, w11 = dx * dy;
+  return make_float3((((0.f + v00.x * w00) + v10.x * w10) + v01.x * w01) + v11.x * w11,
+                     (((0.f + v00.y * w00) + v10.y * w10) + v01.y * w01) + v11.y * w11,
+                     (((0.f + v00.z * w00) + v10.z * w10) + v01.z * w01) + v11.z * w11);
+}
+
+// The reconstruction's upsample: alpha-aware for 4 channels, the four-tap sum for 3.
+template <int C>
+__device__ __forceinline__ float3 up_recon(const float4* lo, int lw, int lh, int x, int y) {
+  if constexpr (C == 4)
+    return up_alpha(lo, lw, 0, 0, lw, lh, x, y);
+  else
+    return up_taps(lo, lw, lh, x, y);
 }
 
 // 3-channel blends (no alpha): weights m[0..n) of the level's pixel.
@@ -221,7 +249,7 @@ __global__ void gen_up_kernel(const __grid_constant__ GenArgs a, int l, const fl
     r = blend_rgb<RULE, NMAX>(n, lap, m);
   }
   if (!last) {
-    const float3 up = up_level<C>(rnext + (long long)b * nw * nh, nw, nh, x, y);
+    const float3 up = up_recon<C>(rnext + (long long)b * nw * nh, nw, nh, x, y);
     r.x = up.x + r.x;
     r.y = up.y + r.y;
     r.z = up.z + r.z;

@@ -117,7 +117,8 @@ static inline void FN(up_alpha)(const REAL* low, int lw, int lh, int x, int y, R
   const REAL w[4] = {(one - dx) * (one - dy), dx * (one - dy), (one - dx) * dy, dx * dy};
   const REAL* p[4] = {low + ((size_t)gyi * lw + gxi) * 4, low + ((size_t)gyi * lw + gxi1) * 4,
                       low + ((size_t)gyi1 * lw + gxi) * 4, low + ((size_t)gyi1 * lw + gxi1) * 4};
-  if (g_ch == 3) { /* no alpha: separable bilinear, x then y (cudaBlend.cu:445-448) */
+  if (g_ch == 3) { /* no alpha: separable bilinear, x then y (cudaBlend.cu:445-448); the
+                     * reconstruction uses up_taps3 instead */
     for (int c = 0; c < 3; ++c) {
       const REAL v0 = p[0][c] * (one - dx) + p[1][c] * dx;
       const REAL v1 = p[2][c] * (one - dx) + p[3][c] * dx;
@@ -134,6 +135,31 @@ static inline void FN(up_alpha)(const REAL* low, int lw, int lh, int x, int y, R
       }
     }
     out3[c] = sw > 0 ? sv / sw : (REAL)0;
+  }
+}
+
+/* The reconstruction's upsample of 3-channel pixels: the sequential four-tap sum
+ * (((0 + v00 w00) + v10 w10) + v01 w01) + v11 w11 of the reference's reconstructions
+ * (cudaBlend.cu:581-672 and cudaBlendN.cu:372-447, whose weight sum is exactly 1 here;
+ * cupano/ops.py:514-565). It rounds differently from the separable form of the Laplacian at
+ * pixels with odd x and odd y once a level holds blended (non-dyadic) values. */
+static inline void FN(up_taps3)(const REAL* low, int lw, int lh, int x, int y, REAL out3[3]) {
+  int gxi = x >> 1, gyi = y >> 1;
+  if (gxi > lw - 1)
+    gxi = lw - 1;
+  if (gyi > lh - 1)
+    gyi = lh - 1;
+  const int gxi1 = gxi + 1 < lw - 1 ? gxi + 1 : lw - 1;
+  const int gyi1 = gyi + 1 < lh - 1 ? gyi + 1 : lh - 1;
+  const REAL dx = (REAL)x / (REAL)2 - (REAL)gxi, dy = (REAL)y / (REAL)2 - (REAL)gyi, one = 1;
+  const REAL w[4] = {(one - dx) * (one - dy), dx * (one - dy), (one - dx) * dy, dx * dy};
+  const REAL* p[4] = {low + ((size_t)gyi * lw + gxi) * 4, low + ((size_t)gyi * lw + gxi1) * 4,
+                      low + ((size_t)gyi1 * lw + gxi) * 4, low + ((size_t)gyi1 * lw + gxi1) * 4};
+  for (int c = 0; c < 3; ++c) {
+    REAL sv = 0;
+    for (int t = 0; t < 4; ++t)
+      sv += p[t][c] * w[t];
+    out3[c] = sv;
   }
 }
 
@@ -158,8 +184,8 @@ static void FN(laplacian)(const REAL* high, int hw, int hh, const REAL* low, int
   }
 }
 
-/* R_l = up_alpha(R_{l+1}) + blend_l (rgb), alpha = blend_l alpha (cudaBlend.cu:581-672,
- * cudaBlendN.cu:372-447). */
+/* R_l = up(R_{l+1}) + blend_l (rgb), alpha = blend_l alpha, up = up_alpha for 4 channels and
+ * up_taps3 for 3 (cudaBlend.cu:581-672, cudaBlendN.cu:372-447). */
 static void FN(reconstruct)(const REAL* low, int lw, int lh, const REAL* lap, int hw, int hh, REAL* out, int batch) {
   for (int b = 0; b < batch; ++b) {
     const REAL* L = low + (size_t)b * lw * lh * 4;
@@ -169,7 +195,10 @@ static void FN(reconstruct)(const REAL* low, int lw, int lh, const REAL* lap, in
     for (int y = 0; y < hh; ++y)
       for (int x = 0; x < hw; ++x) {
         REAL up[3];
-        FN(up_alpha)(L, lw, lh, x, y, up);
+        if (g_ch == 3)
+          FN(up_taps3)(L, lw, lh, x, y, up);
+        else
+          FN(up_alpha)(L, lw, lh, x, y, up);
         const REAL* p = P + ((size_t)y * hw + x) * 4;
         REAL* o = O + ((size_t)y * hw + x) * 4;
         o[0] = up[0] + p[0];
