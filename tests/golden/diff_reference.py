@@ -3,9 +3,9 @@ rigs (beyond the fixed golden cases).
 
 Like make_golden.py it imports hm-cupano's ``cupano`` package with stand-in cv2/tifffile/PIL
 modules and the workspace-downsample correction, so it needs the reference tree; the tests do not
-run it. Each rig draws 2 to 5 images, canvas and source sizes, overlap, levels 0..6, minimised or
-full blend, batch 1 or 2, out-of-range table entries and RGB or RGBA frames, runs the reference
-and the FP32 oracle, and compares the canvases bit for bit.
+run it. Each rig draws 2 to --max-images (default 5, at most 8) images, canvas and source sizes,
+overlap, levels 0..6, minimised or full blend, batch 1 or 2, out-of-range table entries and RGB
+or RGBA frames, runs the reference and the FP32 oracle, and compares the canvases bit for bit.
 
 Two kinds of rig are left out because the two implementations are known to differ there:
   * two images under the N-image stitcher at levels > 0 (the Python CudaStitchPanoN uses the
@@ -38,6 +38,7 @@ def main() -> int:
     ap = argparse.ArgumentParser()
     ap.add_argument("--seed", type=int, default=1)
     ap.add_argument("--rigs", type=int, default=100)
+    ap.add_argument("--max-images", type=int, default=5, help="images per rig: 2..max (at most 8)")
     ap.add_argument("--reference", default=os.environ.get("HM_CUPANO_REFERENCE", "/root/reference"))
     args = ap.parse_args()
     mg._install_stubs()
@@ -55,7 +56,7 @@ def main() -> int:
     rng = np.random.default_rng(args.seed)
     same = differ = rejected = 0
     for t in range(args.rigs):
-        n = int(rng.choice([2, 2, 3, 4, 5]))
+        n = int(rng.choice([2, 2] + list(range(3, min(args.max_images, 8) + 1))))
         kind = 2 if n == 2 else 1
         params = dict(canvas_w=int(rng.integers(300, 700)), canvas_h=int(rng.integers(16, 64)), n=n,
                       src_w=int(rng.integers(100, 260)), src_h=int(rng.integers(14, 60)),
