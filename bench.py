@@ -152,6 +152,48 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(self.samples)}
 
 
+CLOCK_PAD_S = 0.35
+
+
+def pad_steps(step, stream, seconds: float) -> int:
+    """Runs the bench step until `seconds` of wall time have passed (in chunks of 25 steps with a
+    synchronize after each, outside any timed region); returns the number of steps."""
+    import torch
+
+    n = 0
+    t0 = time.perf_counter()
+    while time.perf_counter() - t0 < seconds:
+        with torch.cuda.stream(stream):
+            for i in range(25):
+                step(n + i)
+        torch.cuda.synchronize()
+        n += 25
+    return n
+
+
+def host_link(dev, nbytes: int = 256 << 20) -> dict:
+    """Pinned host <-> device copy bandwidth (GB/s, best of 5, CUDA events), the bound of the
+    end-to-end number, whose every step copies its frames in and its canvas out."""
+    import torch
+
+    h = torch.empty(nbytes, dtype=torch.uint8).pin_memory()
+    d = torch.empty(nbytes, dtype=torch.uint8, device=dev)
+    s = torch.cuda.Stream(dev)
+    out = {}
+    for name, dst, src in (("h2d", d, h), ("d2h", h, d)):
+        best = float("inf")
+        for _ in range(5):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            with torch.cuda.stream(s):
+                e0.record(s)
+                dst.copy_(src, non_blocking=True)
+                e1.record(s)
+            torch.cuda.synchronize(dev)
+            best = min(best, e0.elapsed_time(e1) / 1e3)
+        out[name] = round(nbytes / best / 1e9, 1)
+    return out
+
+
 def _masks(rig):
     import hmpano
 
@@ -235,6 +277,7 @@ def main() -> None:
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-serve", action="store_true", help="skip the serving sweep (p50/p99 latency)")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched multi-stream graph job")
+    ap.add_argument("--no-variants", action="store_true", help="skip the other workloads' frame times")
     ap.add_argument("--serve-seconds", type=float, default=1.0, help="arrival window per offered rate")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
@@ -299,7 +342,6 @@ def main() -> None:
     sampler = ClockSampler(local) if rank == 0 else None
     if sampler:
         sampler.__enter__()
-    t_region0 = time.perf_counter()
     e0.record(stream)
     for i in range(args.steps):
         step(i)
@@ -325,6 +367,13 @@ def main() -> None:
             graph.replay()
         torch.cuda.synchronize()
     torch.cuda.synchronize()
+    # The clock record: nvidia-smi samples every 100 ms, and a short timed region (a few ms at
+    # the default step counts) holds none. The same steps therefore run for at least
+    # CLOCK_PAD_S before and after the timed region while the sampler runs, and the record
+    # covers that window (the timed region inside it is unchanged: exactly K steps).
+    t_region0 = time.perf_counter()
+    pad_before = pad_steps(step, stream, CLOCK_PAD_S)
+    torch.cuda.synchronize()
     e0.record(stream)
     if graph is not None:
         with torch.cuda.stream(stream):
@@ -337,6 +386,7 @@ def main() -> None:
             step(i)
     e1.record(stream)
     torch.cuda.synchronize()
+    pad_after = pad_steps(step, stream, CLOCK_PAD_S)
     t_region1 = time.perf_counter()
     if sampler:
         sampler.__exit__(None, None, None)
@@ -407,6 +457,14 @@ def main() -> None:
                "d2h_bytes_per_step": int(B * W * H * 4), "ms_per_step": round(ms_e2e, 4), "steps": k_e2e,
                "fps": round(world * B * 1e3 / ms_e2e, 1), "pipeline": "3 streams x 3 buffer sets",
                "output_check": ok}
+        # Its bound: the copies alone at the measured pinned copy bandwidth (the two directions
+        # overlap, so the floor is the slower of them).
+        link = host_link(dev)
+        floor_ms = max(e2e["h2d_bytes_per_step"] / (link["h2d"] * 1e9),
+                       e2e["d2h_bytes_per_step"] / (link["d2h"] * 1e9)) * 1e3
+        e2e["host_link_gbs"] = link
+        e2e["copy_floor_ms_per_step"] = round(floor_ms, 4)
+        e2e["frac_of_copy_floor"] = round(floor_ms / ms_e2e, 3)
 
     peak, peak_kind = _peaks()
     names = ["canvas_gather", "pyr_down", "pyr_coarse", "pyr_fine"]
@@ -472,10 +530,17 @@ def main() -> None:
         # pyr_fine, canvas_gather), counted per kernel by the instrumented pass.
         "gpu_launches": world * args.steps * int(info["launches_per_process"]),
         "e2e": e2e,
-        "clocks": sampler.summary() if sampler else None,
+        "clocks": dict(sampler.summary(), window_s=round(t_region1 - t_region0, 3),
+                       padding_steps=[pad_before, pad_after]) if sampler else None,
     }
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(rig, host_frames, args.levels)
+    if not args.no_variants and world == 1:
+        # The other named workloads alone: three-image 6000x1800 and eight-image 9000x2400 at 6
+        # levels (FP32 and FP16), and the headline frame with FP16 storage, Binomial5, 0 levels.
+        from hmpano import variants
+
+        line["variants"] = variants.run(dev, max(50, min(args.steps, 300)), peak)
     if not args.no_batched and world == 1:
         # Batched streaming job: 4 two-image + 4 three-image streams x 32 frames, FP16 storage, one
         # CUDA graph, frames per call and tiles autotuned.

@@ -23,10 +23,9 @@
  *   hmp_control_dir_load  <- ControlMasks::load / ControlMasks3::load / ControlMasksN::load
  *                            src/pano/controlMasks.cpp:133-326, controlMasks3.cpp:186-300,
  *                            controlMasksN.cpp:22-193
- *   hmp_blend2_noalloc    <- cudaBatchedLaplacianBlend (two-image blend without a stitcher)
- *                            src/cuda/cudaBlend.cu:678-843, without its allocations
- *   hmp_batch_*, hmp_server_*: no counterpart (the reference stitches one configuration per
- *                            process, one call at a time)
+ *   hmp_batch_*, hmp_server_*, hmp_blend2_noalloc: no counterpart (the reference stitches one
+ *                            configuration per process, one call at a time, and every blend it
+ *                            offers allocates its own device buffers)
  *
  * Error convention (src/cuda/cudaStatus.h:12-75): every call returns an hmp_status whose code is
  * a cudaError_t value (0 = success) with a message. Construction errors are also kept as the
@@ -257,7 +256,9 @@ HMP_API hmp_status hmp_stitcher_get_timing(hmp_stitcher* st, hmp_kernel_timing* 
  *
  * image1, image2: already-remapped RGBA8 frames of the same size (device, batch_size frames each
  * at data + b*pitch*height); seam: device, height rows of seam_pitch bytes, 1 = image 1, 0 =
- * image 2 (the two-image seam in its inverted form); out: same size as the images. The result
+ * image 2 (the two-image seam in its inverted form). Seam bytes must be exactly 0 or 1: the seam
+ * is device data, so it is not checked, and any other value (a 0/255 mask, say) gives an
+ * undefined blend, as it does in a stitcher. out: same size as the images. The result
  * equals hmp_stitcher_process of a two-image stitcher whose tables are the identity, with both
  * images at (0, 0) and minimize_blend = 0. Work is enqueued on `stream`.
  *

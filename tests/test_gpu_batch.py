@@ -8,6 +8,25 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 
+def _check_against_oracle(job, canvases):
+    """One stream of each kind (two- and three-image): its last frame's canvas against the FP64
+    oracle on the same frames, within the FP16-storage tolerance (1 LSB max, 0.05 LSB mean)."""
+    import numpy as np
+    from oracle import oracle
+
+    oracle.build()
+    seen = set()
+    for s, c in zip(job.streams, canvases):
+        if s["kind"] in seen:
+            continue
+        seen.add(s["kind"])
+        frames = [t[job.frames - 1:job.frames].cpu().numpy() for t in s["inputs"]]
+        ref = oracle.Stitch.from_rig(s["rig"], job.levels).run(frames, "f64")[0]
+        d = np.abs(c.cpu().numpy().astype(np.int32) - ref.astype(np.int32))
+        assert int(d.max()) <= 1 and float(d.mean()) <= 0.05, (s["workload"], int(d.max()), float(d.mean()))
+    assert seen == {2, 3}
+
+
 def test_batched_graph_job_equals_plain_path():
     import build as hmp_build
     import torch
@@ -18,6 +37,7 @@ def test_batched_graph_job_equals_plain_path():
     dev = torch.device("cuda", 0)
     job = batch.Job(dev, frames=4, scale=0.25)
     _, want = batch.plain_path(job, keep_last=True)
+    _check_against_oracle(job, want)
     for b, tile in [(1, 32), (2, 64), (4, 32)]:
         plan = batch.Plan(job, b, tile)
         plan.time(1)

@@ -28,8 +28,10 @@ def prepared():
     import torch
 
     from hmpano import synth
+    from oracle import oracle
 
     hmp_build.build()
+    oracle.build()
     assert torch.cuda.is_available(), "GPU tests need a CUDA device"
     out = []
     for ci, (workload, kind, levels, scale) in enumerate(CONFIGS):
@@ -38,8 +40,12 @@ def prepared():
         assert alone.status.ok(), alone.status
         sets = []
         for s in range(3):
-            frames = [torch.from_numpy(f).cuda() for f in synth.rig_frames(rig, seed=1000 * ci + s)]
+            host = synth.rig_frames(rig, seed=1000 * ci + s)
+            frames = [torch.from_numpy(f).cuda() for f in host]
             ref = alone._run(frames).clone()
+            if s == 0:  # the request alone is itself the oracle's result, bit for bit (FP32 storage)
+                want = oracle.Stitch.from_rig(rig, levels).run(host)
+                assert np.array_equal(ref.cpu().numpy(), want), workload
             sets.append((frames, ref))
         torch.cuda.synchronize()
         out.append({"rig": rig, "kind": kind, "levels": levels, "sets": sets,

@@ -232,6 +232,45 @@ def test_c_abi_rejects_bad_arguments_before_any_device_work(lib):
     assert lib.hmp_control_dir_load(b"/nonexistent", 99, 2, C.byref(d)).code == 1 and not d
 
 
+def test_noalloc_blend_rejects_bad_arguments_before_any_device_work(lib):
+    """hmp_blend2_noalloc checks every argument before its first CUDA call, so fake non-null
+    pointers are never dereferenced: each rejection is HMP_ERR_INVALID_VALUE with its message."""
+    from hmpano import _lib
+
+    def img(w, h, pitch=None, ptr=0x10000):
+        return _lib.Image(C.c_void_p(ptr), w, h, pitch if pitch is not None else 4 * w)
+
+    seam = C.c_void_p(0x20000)
+
+    def call(a, b, o, seam_ptr=seam, seam_pitch=64, levels=3, batch=1):
+        return lib.hmp_blend2_noalloc(C.byref(a) if a is not None else None, C.byref(b) if b is not None else None,
+                                      seam_ptr, seam_pitch, levels, batch, C.byref(o) if o is not None else None, None)
+
+    good = img(64, 32)
+    cases = [
+        (dict(a=None, b=good, o=good), b"non-null RGBA8"),
+        (dict(a=img(64, 32, ptr=0), b=good, o=good), b"non-null RGBA8"),
+        (dict(a=img(64, 32, pitch=4 * 64 - 4), b=good, o=good), b"non-null RGBA8"),  # pitch below a row
+        (dict(a=img(64, 32, pitch=4 * 64 + 2), b=good, o=good), b"non-null RGBA8"),  # pitch not a multiple of 4
+        (dict(a=img(64, 32, ptr=0x10002), b=good, o=good), b"non-null RGBA8"),  # data not 4-byte aligned
+        (dict(a=good, b=img(0, 32), o=good), b"non-null RGBA8"),
+        (dict(a=good, b=good, o=None), b"non-null RGBA8"),
+        (dict(a=img(65, 32), b=good, o=good), b"same size"),
+        (dict(a=good, b=img(64, 31), o=good), b"same size"),
+        (dict(a=img(70000, 2), b=img(70000, 2), o=img(70000, 2)), b"smaller than 65535"),
+        (dict(a=good, b=good, o=good, seam_ptr=None), b"seam"),
+        (dict(a=good, b=good, o=good, seam_pitch=63), b"seam"),
+        (dict(a=good, b=good, o=good, seam_pitch=1 << 40), b"seam"),
+        (dict(a=good, b=good, o=good, levels=0), b"num_levels"),
+        (dict(a=good, b=good, o=good, levels=31), b"num_levels"),
+        (dict(a=good, b=good, o=good, batch=0), b"batch_size"),
+        (dict(a=good, b=good, o=good, batch=65537), b"batch_size"),
+    ]
+    for kw, msg in cases:
+        s = call(**kw)
+        assert s.code == 1 and msg in s.message, (kw, s.code, s.message)
+
+
 def _sanitized_build(tmp_path, name, sources, compiler):
     import shutil
     import subprocess

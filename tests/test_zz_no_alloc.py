@@ -3,8 +3,9 @@ called through the C ABI, against hmp_stitcher_process of the equivalent two-ima
 identity tables, both images at (0, 0), minimize_blend off.
 
 Both paths run the same FP32 kernels on the same values, so the tolerance is the FP32 one of the
-parity tests: bit-exact. Two blends of different sizes and depths run back to back, so that the
-second one reads scratch the first one left behind. The file is named to be collected last and
+parity tests: bit-exact. Blends of different sizes and depths (one level up to the deepest
+supported, seven) run back to back, so that each one after the first reads scratch the one before
+it left behind. The file is named to be collected last and
 passes alone in a fresh process as well as after the other tests.
 """
 from __future__ import annotations
@@ -79,6 +80,8 @@ def test_noalloc_blend_matches_stitcher_twice_in_a_row():
         # (height, width, levels, batch, unmapped rectangle of image 2)
         (360, 640, 5, 1, (40, 120, 300, 420)),
         (301, 517, 4, 2, (150, 301, 0, 90)),
+        (123, 200, 1, 1, (10, 60, 20, 90)),  # one level: pyr_fine alone, no coarser levels
+        (360, 640, 7, 1, (200, 330, 500, 640)),  # the deepest pyramid supported (64-pixel alignment)
     ]
     prepared = []
     for h, w, levels, batch, hole in cases:
@@ -98,7 +101,7 @@ def test_noalloc_blend_matches_stitcher_twice_in_a_row():
         dev_in.append((torch.from_numpy(img1).cuda(), torch.from_numpy(img2).cuda(), seam_dev, out))
     torch.cuda.synchronize()
 
-    # Two calls in a row on one stream; the second reuses the scratch the first one wrote.
+    # Calls in a row on one stream; each reuses the scratch the one before it wrote.
     for (img1, img2, seam, levels, batch, _), (a, b, seam_dev, out) in zip(prepared, dev_in):
         s = _noalloc(lib, a, b, seam_dev, levels, batch, out)
         assert s.code == 0, s.message.decode()
