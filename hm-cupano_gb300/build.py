@@ -27,6 +27,7 @@ COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler",
           "-I", str(REPO / "include"), "-I", str(CSRC)]
 UNITS = {
     "hmp_plan.cpp": ["-Xcompiler", "-ffp-contract=off"],
+    "hmp_copyplan.cpp": [],
     "hmp_gather.cu": [],
     "hmp_pyramid.cu": ["-fmad=false"],
     "hmp_stitcher.cu": [],
@@ -37,7 +38,7 @@ UNITS = {
     "hmp_generic.cu": ["-fmad=false"],
     "hmp_batch.cpp": [],
 }
-HEADERS = ["hmp_plan.h", "hmp_device.cuh", "hmp_kernels.h", "hmp_blend.cuh", "hmp_admission.h"]
+HEADERS = ["hmp_plan.h", "hmp_copyplan.h", "hmp_device.cuh", "hmp_kernels.h", "hmp_blend.cuh", "hmp_admission.h"]
 
 
 def nvcc() -> str:

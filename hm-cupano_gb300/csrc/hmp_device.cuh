@@ -137,6 +137,10 @@ __device__ __forceinline__ uchar4 plane_pixel(const SrcSet& S, const PlaneDev& P
 // sentinel.
 constexpr uint32_t kOffZero = 0xFFFFFFFFu;    // (0, 0, 0, 0)
 constexpr uint32_t kOffOpaque = 0xFFFFFFFEu;  // (0, 0, 0, 255)
+// A canvas pixel the pyramid writes in copy-block mode (the gather leaves it alone). Frames hold
+// at most kOffMask - 2 pixels (process() rejects larger ones), so offsets stay below kOffMask - 2
+// and no resolved entry, owner 7 included, reaches this code.
+constexpr uint32_t kOffSkip = 0xFFFFFFFDu;
 constexpr int kOwnerShift = 29;
 constexpr uint32_t kOffMask = (1u << kOwnerShift) - 1u;  // frames hold fewer than kOffMask - 1 pixels
 

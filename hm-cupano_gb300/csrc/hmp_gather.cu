@@ -53,6 +53,9 @@ __device__ __forceinline__ void gather_one(uint32_t* dst, const uchar4* base, ui
 // Measured: loading the entries into registers instead of staging them in shared memory, and the
 // register path, each took about 4 % off the two-image 8500x3300 frame (fewer shared-memory
 // instructions in the queue that the pyramid kernels running beside the gather also use).
+// kCopy: the plane holds copy-block skips and the call may check source alpha (three or more
+// images); without it the kernel is compiled free of that code.
+template <bool kCopy>
 __global__ void __launch_bounds__(256, 6) canvas_gather_kernel(const __grid_constant__ GatherArgs a) {
   constexpr int PJ = 4;  // 64-pixel steps per segment
   static_assert(64 * PJ == kSegPixels, "a warp's segment is the resolve pass's segment");
@@ -79,8 +82,18 @@ __global__ void __launch_bounds__(256, 6) canvas_gather_kernel(const __grid_cons
   const unsigned so = __ldg(a.seg_owner + (long long)y * a.seg_pitch + blockIdx.x);
   const bool uniform = so != kSegMixed;
   const int uo = int(so & (kSegFills - 1));
+  // Copy-block mode: pixels the pyramid writes carry kOffSkip (only in mixed segments).
+  bool skips = false;
+  if (kCopy && so == kSegMixed) {
+#pragma unroll
+    for (int j = 0; j < PJ; ++j) skips = skips || er[j].x == kOffSkip || er[j].y == kOffSkip;
+    skips = __any_sync(0xFFFFFFFFu, skips);
+  }
   // Segments wholly inside the canvas and outside the skipped rect store without checks.
-  const bool plain = x0 + 64 * PJ <= W && !(row_skip && x0 < a.skip_x1 && x0 + 64 * PJ > a.skip_x0);
+  const bool plain = x0 + 64 * PJ <= W && !(row_skip && x0 < a.skip_x1 && x0 + 64 * PJ > a.skip_x0) && !skips;
+  // Copy-block mode: source pixels read inside the blend region must have alpha != 0.
+  const bool chk = kCopy && a.alpha_flag != nullptr && y >= a.chk_y0 && y < a.chk_y1 && x0 < a.chk_x1 && x0 + 64 * PJ > a.chk_x0;
+  bool bad = false;
   for (int b = 0; b < a.batch; ++b) {
     uint32_t* pxw = reinterpret_cast<uint32_t*>(px);
     uint32_t* crow = reinterpret_cast<uint32_t*>(reinterpret_cast<char*>(a.C.ptr) + b * a.C.bstride + y * a.C.pitch);
@@ -97,6 +110,13 @@ __global__ void __launch_bounds__(256, 6) canvas_gather_kernel(const __grid_cons
 #pragma unroll
       for (int j = 0; j < PJ; ++j)
         __stcs(reinterpret_cast<uint2*>(crow + x0 + 64 * j + 2 * lane), make_uint2(v[2 * j], v[2 * j + 1]));
+      if (chk) {
+#pragma unroll
+        for (int i = 0; i < 2 * PJ; ++i) {
+          const int x = x0 + 64 * (i >> 1) + 2 * lane + (i & 1);
+          bad = bad || ((v[i] >> 24) == 0u && x >= a.chk_x0 && x < a.chk_x1);
+        }
+      }
       continue;
     }
     if (uniform) {
@@ -126,7 +146,7 @@ __global__ void __launch_bounds__(256, 6) canvas_gather_kernel(const __grid_cons
         for (int h = 0; h < 2; ++h) {
           const uint32_t e = h ? e2.y : e2.x;
           uint32_t* d = pxw + 2 * (32 * j + lane) + h;
-          if (e < kOffOpaque) {
+          if (e < kOffSkip) {
             const int o = int(e >> kOwnerShift);
             cp_async4(d, reinterpret_cast<const uchar4*>(reinterpret_cast<const char*>(a.S.ptr[o]) + b * a.S.bstride[o]) +
                              (e & kOffMask));
@@ -138,6 +158,19 @@ __global__ void __launch_bounds__(256, 6) canvas_gather_kernel(const __grid_cons
     }
     cp_async_commit();
     cp_async_wait<0>();
+    if (chk) {
+      // Source reads only: offsets and owner-tagged entries lie below every fill and skip code.
+#pragma unroll
+      for (int j = 0; j < PJ; ++j) {
+        const uint2 v = px[32 * j + lane];
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+          const int x = x0 + 64 * j + 2 * lane + h;
+          const uint32_t e = h ? er[j].y : er[j].x;
+          bad = bad || (e < kOffSkip && ((h ? v.y : v.x) >> 24) == 0u && x >= a.chk_x0 && x < a.chk_x1);
+        }
+      }
+    }
     if (plain && (reinterpret_cast<uintptr_t>(crow) & 7) == 0) {
 #pragma unroll
       for (int j = 0; j < PJ; ++j)
@@ -149,10 +182,15 @@ __global__ void __launch_bounds__(256, 6) canvas_gather_kernel(const __grid_cons
 #pragma unroll
         for (int h = 0; h < 2; ++h) {
           const int x = x0 + 64 * j + 2 * lane + h;
-          if (x < W && !(row_skip && x >= a.skip_x0 && x < a.skip_x1)) __stcs(crow + x, h ? v.y : v.x);
+          const uint32_t e = h ? er[j].y : er[j].x;
+          if (x < W && !(row_skip && x >= a.skip_x0 && x < a.skip_x1) && (!kCopy || e != kOffSkip))
+            __stcs(crow + x, h ? v.y : v.x);
         }
       }
     }
+  }
+  if constexpr (kCopy) {
+    if (chk && __any_sync(0xFFFFFFFFu, bad) && lane == 0) atomicOr(a.alpha_flag, 1);
   }
 }
 
@@ -162,7 +200,8 @@ __global__ void __launch_bounds__(256, 6) canvas_gather_kernel(const __grid_cons
 // 65535 sentinel. (Frames hold fewer than kOffMask - 1 pixels, so no offset meets a fill code.)
 __global__ void __launch_bounds__(kSegPixels) resolve_plane_kernel(const __grid_constant__ PlaneDev raw, uint32_t* res,
                                                                    uint8_t* seg_owner, int seg_pitch,
-                                                                   const __grid_constant__ SrcSet S, int n, int opaque) {
+                                                                   const __grid_constant__ SrcSet S, int n, int opaque,
+                                                                   const __grid_constant__ SkipMap skip) {
   // One CTA per 256-pixel row segment, the gather's unit.
   const int x = blockIdx.x * kSegPixels + threadIdx.x, y = blockIdx.y;
   uint32_t r = kOffZero;  // pixels past the plane's width read as fills
@@ -177,14 +216,22 @@ __global__ void __launch_bounds__(kSegPixels) resolve_plane_kernel(const __grid_
       else if (opaque && sx != 0xFFFF)
         r = kOffOpaque;
     }
+    // Copy-block mode: a pixel of a block the pyramid writes.
+    if (skip.map && x >= skip.wr_x0 && x < skip.wr_x1 && y >= skip.wr_y0 && y < skip.wr_y1) {
+      const int bx = (x - skip.x0) >> 6, by = (y - skip.y0) >> 4;
+      if (bx >= 0 && by >= 0 && bx < skip.nx && by < skip.ny && skip.map[(long long)by * skip.pitch + bx]) r = kOffSkip;
+    }
   }
   // The segment's range of owners and whether it holds fills.
+  // A segment holding a skip is mixed: its entries keep their owners and the gather stores pixel
+  // by pixel.
   __shared__ unsigned s_lo[kSegPixels / 32], s_hi[kSegPixels / 32], s_fill[kSegPixels / 32];
   __shared__ unsigned s_code;
-  unsigned lo = r < kOffOpaque ? r >> kOwnerShift : 8u, hi = r < kOffOpaque ? r >> kOwnerShift : 0u;
+  unsigned lo = r < kOffSkip ? r >> kOwnerShift : 8u, hi = r < kOffSkip ? r >> kOwnerShift : 0u;
+  if (r == kOffSkip) lo = 1u, hi = 2u;
   lo = __reduce_min_sync(0xFFFFFFFFu, lo);
   hi = __reduce_max_sync(0xFFFFFFFFu, hi);
-  const unsigned fill = __reduce_or_sync(0xFFFFFFFFu, r >= kOffOpaque ? 1u : 0u);
+  const unsigned fill = __reduce_or_sync(0xFFFFFFFFu, r >= kOffSkip ? 1u : 0u);
   if ((threadIdx.x & 31) == 0) {
     s_lo[threadIdx.x >> 5] = lo;
     s_hi[threadIdx.x >> 5] = hi;
@@ -203,22 +250,25 @@ __global__ void __launch_bounds__(kSegPixels) resolve_plane_kernel(const __grid_
   }
   __syncthreads();
   // Entries of a one-owner segment are stored without their owner (the segment has it).
-  if (in) res[(long long)y * raw.map_pitch + x] = (s_code != kSegMixed && r < kOffOpaque) ? (r & kOffMask) : r;
+  if (in) res[(long long)y * raw.map_pitch + x] = (s_code != kSegMixed && r < kOffSkip) ? (r & kOffMask) : r;
 }
 
 }  // namespace
 
 cudaError_t launch_resolve_plane(const PlaneDev& raw, uint32_t* res, uint8_t* seg_owner, int seg_pitch, const SrcSet& S,
-                                 int n, bool opaque, cudaStream_t stream) {
+                                 int n, bool opaque, const SkipMap& skip, cudaStream_t stream) {
   if (raw.w <= 0 || raw.h <= 0) return cudaSuccess;
   resolve_plane_kernel<<<dim3((raw.w + kSegPixels - 1) / kSegPixels, raw.h), kSegPixels, 0, stream>>>(
-      raw, res, seg_owner, seg_pitch, S, n, opaque ? 1 : 0);
+      raw, res, seg_owner, seg_pitch, S, n, opaque ? 1 : 0, skip);
   return cudaGetLastError();
 }
 
-cudaError_t launch_canvas_gather(const GatherArgs& a, cudaStream_t stream) {
+cudaError_t launch_canvas_gather(const GatherArgs& a, bool copy_blocks, cudaStream_t stream) {
   const dim3 grid((a.C.w + 255) / 256, (a.C.h + 7) / 8);
-  canvas_gather_kernel<<<grid, 256, 0, stream>>>(a);
+  if (copy_blocks)
+    canvas_gather_kernel<true><<<grid, 256, 0, stream>>>(a);
+  else
+    canvas_gather_kernel<false><<<grid, 256, 0, stream>>>(a);
   return cudaGetLastError();
 }
 

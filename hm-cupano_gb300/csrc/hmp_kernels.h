@@ -20,6 +20,11 @@ struct GatherArgs {
   // entry is a fill. A one-owner segment's entries are stored without the owner bits.
   const uint8_t* seg_owner;
   int seg_pitch;
+  // Copy-block mode: every source pixel the gather reads inside [chk_x0, chk_x1) x [chk_y0, chk_y1)
+  // (the blend region) must have alpha != 0 for the copy blocks to equal the pyramid; one with
+  // alpha 0 sets *alpha_flag (nullptr: no check).
+  int* alpha_flag;
+  int chk_x0, chk_y0, chk_x1, chk_y1;
 };
 constexpr int kSegPixels = 256;
 constexpr unsigned kSegFills = 8u, kSegMixed = 0xFFu;
@@ -50,6 +55,14 @@ struct PyrArgs {
   int coarse_cap; // N-way pyr_coarse: likewise, per coarse tile
   int fine_cap;   // N-way pyr_fine: likewise, per 64 x 16 level-0 block (with its upsample halo)
   int pdl;        // launch pyr_coarse / pyr_fine as programmatic dependents of the kernel before them
+  // Work list of the launch (copy-block mode): entry blockIdx.x is the CTA's tile, tx | ty << 16,
+  // with bit 31 set on pyr_down tiles whose source pixels feed a copy block's reconstruction
+  // (checked for alpha 0, which sets *alpha_flag). nullptr: the dense grid.
+  const uint32_t* tiles;
+  int* alpha_flag;
+  // Fallback launches: every CTA returns at once unless *gate != 0 (a copy block's source pixels
+  // held alpha 0, so the whole write rect is recomputed). nullptr: always run.
+  const int* gate;
   CanvasDev C;
   int wx0, wy0, wx1, wy1;  // write rect, blend coordinates, end exclusive
   int cx_off, cy_off;      // canvas = blend + offset
@@ -98,10 +111,18 @@ cudaError_t kernels_init();
 // Resolves a plane's packed entries (raw.map) into offsets for the frames S (res: raw's layout).
 // opaque: the soft-seam rule for entries outside their source.
 // Also writes seg_owner (see GatherArgs) for the plane's 256-pixel row segments.
+// Copy-block mode: canvas pixels inside `wr` whose 64 x 16 block (grid origin x0, y0, nx x ny
+// blocks, one byte each at map[by * pitch + bx]) is marked resolve to kOffSkip. map nullptr: none.
+struct SkipMap {
+  const uint8_t* map;
+  int pitch, x0, y0, nx, ny;
+  int wr_x0, wr_y0, wr_x1, wr_y1;  // canvas coordinates, end exclusive
+};
 cudaError_t launch_resolve_plane(const PlaneDev& raw, uint32_t* res, uint8_t* seg_owner, int seg_pitch, const SrcSet& S,
-                                 int n, bool opaque, cudaStream_t stream);
+                                 int n, bool opaque, const SkipMap& skip, cudaStream_t stream);
 
-cudaError_t launch_canvas_gather(const GatherArgs& a, cudaStream_t stream);
+// copy_blocks: the plane holds copy-block skips (kOffSkip) or the call checks source alpha.
+cudaError_t launch_canvas_gather(const GatherArgs& a, bool copy_blocks, cudaStream_t stream);
 
 // Gaussian levels 1..L-1 of every slot; grid = tiles over the blend region x batch.
 cudaError_t launch_pyr_down(const PyrArgs& a, int storage, dim3 grid, cudaStream_t stream);

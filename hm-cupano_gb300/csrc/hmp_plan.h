@@ -65,7 +65,8 @@ struct Plan {
   Rect blend;  // pyramid domain, canvas coordinates
   Rect write;  // pyramid write-back region, canvas coordinates (inside blend)
   bool canvas_plane_used = false;
-  GatherPlane canvas;               // canvas coordinates; pixels in `write` are skipped
+  GatherPlane canvas;               // canvas coordinates; pixels in `write` are skipped (all of
+                                    // them, or those of pyramid blocks in copy-block mode)
   std::vector<GatherPlane> slots;   // n, blend coordinates
   std::vector<uint8_t> mask0;       // blend.w * blend.h: two-image weight value or label
   std::vector<std::vector<float>> mask_levels;  // levels >= 1: lw*lh*mask_k floats

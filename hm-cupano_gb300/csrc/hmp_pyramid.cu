@@ -99,6 +99,28 @@ __device__ __forceinline__ Store* level_of(const PyrArgs& a, int k, int l, int b
 // kernel has completed and its writes are visible (at once after a normal launch).
 __device__ __forceinline__ void grid_dep_wait() { asm volatile("griddepcontrol.wait;\n" ::: "memory"); }
 
+// The tile of this CTA: blockIdx.x / y of the dense grid, or entry blockIdx.x of the launch's work
+// list (copy-block mode: tx | ty << 16, bit 31 = check the tile's source alpha). Returns false
+// when the launch is a gated-off fallback (the gate is written before the launch's stream reaches
+// it, so every thread of every CTA reads the same value and returns together). Copy blocks apply
+// to three or more images only; the two-image kernels are compiled without this code (kLists
+// false), since extra code in them measured slower beside the canvas gather.
+template <bool kLists>
+__device__ __forceinline__ bool cta_tile(const PyrArgs& a, int& tx, int& ty, bool& check) {
+  tx = int(blockIdx.x);
+  ty = int(blockIdx.y);
+  check = false;
+  if constexpr (!kLists) return true;
+  if (a.gate != nullptr && *a.gate == 0) return false;
+  if (a.tiles != nullptr) {
+    const uint32_t t = __ldg(a.tiles + blockIdx.x);
+    tx = int(t & 0xFFFFu);
+    ty = int((t >> 16) & 0x7FFFu);
+    check = (t >> 31) != 0u && a.alpha_flag != nullptr;
+  }
+  return true;
+}
+
 template <int NMAX, typename Store, int TD>
 __global__ void __launch_bounds__(256) pyr_down_kernel(const __grid_constant__ PyrArgs a) {
   // Only the three- and N-image kernels keep level 0 for pyr_fine; the two-image kernel is
@@ -112,7 +134,13 @@ __global__ void __launch_bounds__(256) pyr_down_kernel(const __grid_constant__ P
   float4* bufB = sm + n * T1 * T1;                  // levels 2, 4, 6: [n][T2*T2]
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int b = blockIdx.z;
-  const int X0 = blockIdx.x * TD, Y0 = blockIdx.y * TD;
+  int tx, ty;
+  bool check;
+  if (!cta_tile<kKeepLevel0>(a, tx, ty, check)) return;
+  const int X0 = tx * TD, Y0 = ty * TD;
+  // Copy-block mode: which level-0 pixels are source reads, one ballot word per warp row and 32
+  // pixels, [slot][row][TD / 32] over the level-2 buffer (written only after the check).
+  uint32_t* src_bits = reinterpret_cast<uint32_t*>(bufB);
   const bool opaque = a.opaque != 0;
   const int L = a.levels;
   const int lw0 = a.lw[0], lh0 = a.lh[0], lw1 = a.lw[1], lh1 = a.lh[1];
@@ -168,11 +196,37 @@ __global__ void __launch_bounds__(256) pyr_down_kernel(const __grid_constant__ P
           cp_async<4>(d, sp);
         else
           *d = fill;
+        if constexpr (kKeepLevel0) {
+          if (check) {
+            const unsigned m = __ballot_sync(0xFFFFFFFFu, sp != nullptr);
+            if (lane == 0) src_bits[(k * TD + r) * (TD / 32) + j] = m;
+          }
+        }
       }
     }
   }
   cp_async_commit_wait_all();
   __syncthreads();
+  if constexpr (kKeepLevel0) {
+    // Copy-block mode: a source pixel with alpha 0 breaks the exactness a copy block relies on,
+    // so it sends the frame to the fallback (the whole write rect through the pyramid).
+    if (check) {
+      bool bad = false;
+#pragma unroll
+      for (int k = 0; k < NMAX; ++k) {
+        if (!active[k]) continue;
+        for (int r = warp; r < TD; r += 8)
+#pragma unroll
+          for (int j = 0; j < TD / 32; ++j) {
+            const unsigned m = src_bits[(k * TD + r) * (TD / 32) + j];
+            const uint32_t v = pix[k * TD * TD + r * TD + 32 * j + lane];
+            bad = bad || (((m >> lane) & 1u) != 0u && (v >> 24) == 0u);
+          }
+      }
+      if (__any_sync(0xFFFFFFFFu, bad) && lane == 0) atomicOr(a.alpha_flag, 1);
+      __syncthreads();  // the bits overlay the level-2 buffer written below
+    }
+  }
   // Level 0 for pyr_fine: each slot's gathered pixels inside its plane rect, so that the level-0
   // pass reads them back directly instead of repeating the table lookups and gathers.
   if constexpr (kKeepLevel0) {
@@ -299,7 +353,11 @@ __global__ void __launch_bounds__(256) pyr_down_n_kernel(const __grid_constant__
   float4* bufB = sm + cap * T1 * T1;                // levels 2, 4, 6: [cap][T2*T2]
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int b = blockIdx.z;
-  const int X0 = blockIdx.x * TD, Y0 = blockIdx.y * TD;
+  int tx, ty;
+  bool check;
+  if (!cta_tile<true>(a, tx, ty, check)) return;
+  const int X0 = tx * TD, Y0 = ty * TD;
+  uint32_t* src_bits = reinterpret_cast<uint32_t*>(bufB);  // as in pyr_down_kernel, per list entry
   const bool opaque = a.opaque != 0;
   const int L = a.levels;
   const int lw0 = a.lw[0], lh0 = a.lh[0], lw1 = a.lw[1], lh1 = a.lh[1];
@@ -351,11 +409,29 @@ __global__ void __launch_bounds__(256) pyr_down_n_kernel(const __grid_constant__
           cp_async<4>(d, sp);
         else
           *d = fill;
+        if (check) {
+          const unsigned m = __ballot_sync(0xFFFFFFFFu, sp != nullptr);
+          if (lane == 0) src_bits[(c * TD + r) * (TD / 32) + j] = m;
+        }
       }
     }
   }
   cp_async_commit_wait_all();
   __syncthreads();
+  if (check) {  // as in pyr_down_kernel
+    bool bad = false;
+#pragma unroll 1
+    for (int c = 0; c < na; ++c)
+      for (int r = warp; r < TD; r += 8)
+#pragma unroll
+        for (int j = 0; j < TD / 32; ++j) {
+          const unsigned m = src_bits[(c * TD + r) * (TD / 32) + j];
+          const uint32_t v = pix[c * TD * TD + r * TD + 32 * j + lane];
+          bad = bad || (((m >> lane) & 1u) != 0u && (v >> 24) == 0u);
+        }
+    if (__any_sync(0xFFFFFFFFu, bad) && lane == 0) atomicOr(a.alpha_flag, 1);
+    __syncthreads();
+  }
   if (a.use_p0) {
 #pragma unroll 1
     for (int c = 0; c < na; ++c) {
@@ -487,11 +563,15 @@ template <int RULE, int NMAX, typename Store, int T1>
 __global__ void __launch_bounds__(256) pyr_coarse_kernel(const __grid_constant__ PyrArgs a) {
   extern __shared__ float4 sm[];
   char* smb = reinterpret_cast<char*>(sm);
+  int tx, ty;
+  bool check;
+  if (!cta_tile<RULE != kRuleTwo>(a, tx, ty, check)) return;
+  if (RULE == kRuleTwo || a.tiles == nullptr) tx += a.tx0, ty += a.ty0;
   grid_dep_wait();  // G^l of pyr_down
   const int n = RULE == kRuleNway ? a.n : NMAX;
   const int K = RULE == kRuleTwo ? 1 : (RULE == kRuleThree ? 3 : a.K);
   const int b = blockIdx.z;
-  const int X1 = (a.tx0 + blockIdx.x) * T1, Y1 = (a.ty0 + blockIdx.y) * T1;
+  const int X1 = tx * T1, Y1 = ty * T1;
   const int L = a.levels, c = L - 1;
   const int tid = threadIdx.x;
   const CoarseLayout lo = coarse_layout(n, K, T1, L, int(sizeof(Store)));
@@ -704,10 +784,14 @@ template <typename Store, int T1>
 __global__ void __launch_bounds__(256) pyr_coarse_n_kernel(const __grid_constant__ PyrArgs a) {
   extern __shared__ float4 sm[];
   char* smb = reinterpret_cast<char*>(sm);
+  int tx, ty;
+  bool check;
+  if (!cta_tile<true>(a, tx, ty, check)) return;
+  if (a.tiles == nullptr) tx += a.tx0, ty += a.ty0;
   grid_dep_wait();  // G^l of pyr_down
   const int n = a.n, K = a.K, cap = a.coarse_cap;
   const int b = blockIdx.z;
-  const int X1 = (a.tx0 + blockIdx.x) * T1, Y1 = (a.ty0 + blockIdx.y) * T1;
+  const int X1 = tx * T1, Y1 = ty * T1;
   const int L = a.levels, c = L - 1;
   const int tid = threadIdx.x;
   const CoarseLayout lo = coarse_layout(cap, 0, T1, L, int(sizeof(Store)));
@@ -905,10 +989,13 @@ __device__ __forceinline__ float3 up_tile(const T* t, int i, bool ox, bool oy) {
 template <int RULE, int NMAX, typename Store, bool P0M>
 __global__ void __launch_bounds__(256) pyr_fine_kernel(const __grid_constant__ PyrArgs a) {
   extern __shared__ float4 fsm[];  // R^1 tile, then G^1 tiles of slots 0..n-1 (Store)
+  int tx, ty;
+  bool check;
+  if (!cta_tile<RULE != kRuleTwo>(a, tx, ty, check)) return;
   const int n = RULE == kRuleNway ? a.n : NMAX;
   const int b = blockIdx.z;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int bx0 = (a.wx0 & ~1) + blockIdx.x * 64, by0 = (a.wy0 & ~1) + blockIdx.y * 16;
+  const int bx0 = (a.wx0 & ~1) + tx * 64, by0 = (a.wy0 & ~1) + ty * 16;
   const int X = bx0 + 2 * lane, Y = by0 + 2 * warp;
   const bool opaque = a.opaque != 0;
   const bool has1 = a.levels > 1;
@@ -1052,11 +1139,14 @@ __global__ void __launch_bounds__(256) pyr_fine_kernel(const __grid_constant__ P
 template <typename Store>
 __global__ void __launch_bounds__(256) pyr_fine_n_kernel(const __grid_constant__ PyrArgs a) {
   extern __shared__ float4 fsm[];
+  int tx, ty;
+  bool check;
+  if (!cta_tile<true>(a, tx, ty, check)) return;
   grid_dep_wait();  // R^1 of pyr_coarse; G^1 and level 0 of pyr_down
   const int n = a.n, cap = a.fine_cap;
   const int b = blockIdx.z;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int bx0 = (a.wx0 & ~1) + blockIdx.x * 64, by0 = (a.wy0 & ~1) + blockIdx.y * 16;
+  const int bx0 = (a.wx0 & ~1) + tx * 64, by0 = (a.wy0 & ~1) + ty * 16;
   const int X = bx0 + 2 * lane, Y = by0 + 2 * warp;
   const int lw0 = a.lw[0], lh0 = a.lh[0], lw1 = a.lw[1], lh1 = a.lh[1];
   float4* rs = fsm;

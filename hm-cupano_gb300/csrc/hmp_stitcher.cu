@@ -22,6 +22,7 @@
 #include <string>
 #include <vector>
 
+#include "hmp_copyplan.h"
 #include "hmp_kernels.h"
 #include "hmp_plan.h"
 #include "hmpano.h"
@@ -127,6 +128,19 @@ struct hmp_stitcher {
   float4* Rl[hmp::kDevMaxLevels]{};
   uint32_t* P0[hmp::kDevMaxImages]{};  // level-0 pixels per slot over its plane rect (box filter)
   bool use_p0 = false;
+  // Copy blocks (three- and N-image box pyramids, hmp_copyplan.h): the pyramid runs over its work
+  // lists only, the canvas gather copies the rest of the write rect, and gated fallback launches
+  // recompute everything when a copy block's source pixels hold alpha 0.
+  bool copy_plan = false;  // planned for this configuration
+  bool copy_on = true;     // hmp_stitcher_set_copy_blocks
+  const uint32_t* fine_list = nullptr;
+  const uint32_t* coarse_list = nullptr;
+  const uint32_t* down_list[2] = {};  // tile_down 32, 64 (nullptr where that tile is not allowed)
+  int n_fine = 0, n_coarse = 0, n_down[2] = {};
+  int* alpha_flag = nullptr;
+  hmp::SkipMap skip{};
+  uint32_t need_w[hmp::kDevMaxImages]{}, need_h[hmp::kDevMaxImages]{};
+  int copy_blocks = 0, empty_blocks = 0, pyramid_blocks = 0;
   cudaStream_t aux = nullptr;
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   double m0_bytes = 0;
@@ -293,7 +307,9 @@ struct hmp_stitcher {
         seg_owner = static_cast<uint8_t*>(so);
       }
     }
-    launches = p.canvas_plane_used ? 1 : 0;
+    // The gather runs when the canvas plane has pixels outside the write rect to fill (copy-block
+    // mode adds its own count below).
+    launches = p.canvas_plane_used && (p.levels == 0 || p.write.w < p.canvas_w || p.write.h < p.canvas_h) ? 1 : 0;
     if (p.levels > 0) {
       const int n = p.n, B = p.batch, L = p.levels;
       for (int k = 0; k < n; ++k) {
@@ -411,6 +427,10 @@ struct hmp_stitcher {
       launches += b5 ? hmp::b5_launches(L) : (L > 1 ? 2 : 0) + 1;
     }
     if (generic) launches = hmp::generic_launches(p.levels, p.canvas_plane_used);
+    if (p.levels > 1 && !b5 && !generic && p.canvas_plane_used && p.rule != hmp::kRuleTwo) {
+      const hmp_status cs = setup_copy_blocks();
+      if (cs.code != HMP_OK) return cs;
+    }
     if (p.canvas_plane_used && p.levels > 0 && !generic) {
       // The pyramid chain (latency-bound, few CTAs) runs on a high-priority stream so that its
       // CTAs are dispatched ahead of the bandwidth-bound canvas gather sharing the SMs.
@@ -437,6 +457,73 @@ struct hmp_stitcher {
     for (auto& m : p.mask_levels) std::vector<float>().swap(m);
     for (auto& m : p.mask_hot) std::vector<uint8_t>().swap(m);
     return ok_status();
+  }
+
+  cudaError_t upload_list(const std::vector<uint32_t>& v, const uint32_t** out) {
+    *out = nullptr;
+    if (v.empty()) return cudaSuccess;
+    void* d = nullptr;
+    cudaError_t e = alloc(&d, v.size() * sizeof(uint32_t));
+    if (e == cudaSuccess) e = cudaMemcpy(d, v.data(), v.size() * sizeof(uint32_t), cudaMemcpyHostToDevice);
+    *out = static_cast<const uint32_t*>(d);
+    return e;
+  }
+
+  // Copy blocks: plans them (for both pyramid down-tile edges the tile setter allows) and uploads
+  // the work lists, the pyramid-block map the resolve pass marks and the alpha flag.
+  hmp_status setup_copy_blocks() {
+    const hmp::Plan& p = plan;
+    const int align = 1 << (p.levels - 1);
+    hmp::CopyPlan cps[2];
+    for (int i = 0; i < 2; ++i) {
+      const int td = i == 0 ? 32 : 64;
+      if (td % align == 0) hmp::plan_copy_blocks(p, td, tile_coarse, cps[i]);
+    }
+    const hmp::CopyPlan& c = cps[1].usable ? cps[1] : cps[0];
+    if (!c.usable) return ok_status();
+    cudaError_t e = upload_list(c.fine_list, &fine_list);
+    if (e == cudaSuccess) e = upload_list(c.coarse_list, &coarse_list);
+    for (int i = 0; i < 2 && e == cudaSuccess; ++i) {
+      if (!cps[i].usable) continue;
+      e = upload_list(cps[i].down_list, &down_list[i]);
+      n_down[i] = int(cps[i].down_list.size());
+    }
+    // The pyramid-block map, then the flag (4-byte aligned; allocations are 256-byte aligned).
+    const size_t flag_off = (c.pyramid_block.size() + 3) / 4 * 4;
+    void* m = nullptr;
+    if (e == cudaSuccess) e = alloc(&m, flag_off + sizeof(int));
+    if (e == cudaSuccess)
+      e = cudaMemcpy(m, c.pyramid_block.data(), c.pyramid_block.size(), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemset(static_cast<char*>(m) + flag_off, 0, sizeof(int));
+    if (e != cudaSuccess) return cuda_status(e, "copy-block upload");
+    n_fine = int(c.fine_list.size());
+    n_coarse = int(c.coarse_list.size());
+    alpha_flag = reinterpret_cast<int*>(static_cast<char*>(m) + flag_off);
+    skip.map = static_cast<const uint8_t*>(m);
+    skip.pitch = c.nfx;
+    skip.x0 = c.fx0 + p.blend.x;
+    skip.y0 = c.fy0 + p.blend.y;
+    skip.nx = c.nfx;
+    skip.ny = c.nfy;
+    skip.wr_x0 = p.write.x;
+    skip.wr_y0 = p.write.y;
+    skip.wr_x1 = p.write.x + p.write.w;
+    skip.wr_y1 = p.write.y + p.write.h;
+    for (int k = 0; k < p.n; ++k) {
+      need_w[k] = c.need_w[k];
+      need_h[k] = c.need_h[k];
+    }
+    copy_blocks = c.copy_blocks;
+    empty_blocks = c.empty_blocks;
+    pyramid_blocks = c.pyramid_blocks;
+    copy_plan = true;
+    return ok_status();
+  }
+
+  // Kernels one process() launches in copy-block mode: the listed pyramid kernels, the gather and
+  // the three gated fallbacks.
+  int copy_launches() const {
+    return (n_down[tile_down == 64 ? 1 : 0] > 0) + (n_coarse > 0) + (n_fine > 0) + 1 + 3;
   }
 
   // Compulsory bytes per process(): outside the write rect, 4 (table) + 1 (seam) + a source and
@@ -740,7 +827,8 @@ struct hmp_stitcher {
         same = same && S.w[i] == geo_w[i] && S.h[i] == geo_h[i] && S.pitch[i] == geo_pitch[i];
       if (!same) {
         const cudaError_t re = hmp::launch_resolve_plane(canvas_raw, const_cast<uint32_t*>(canvas_plane.map), seg_owner,
-                                                         seg_pitch, S, p.n, p.canvas_opaque, s);
+                                                         seg_pitch, S, p.n, p.canvas_opaque,
+                                                         copy_plan ? skip : hmp::SkipMap{}, s);
         if (re != cudaSuccess) return cuda_status(re, "canvas plane resolve launch");
         for (int i = 0; i < p.n; ++i) {
           geo_w[i] = S.w[i];
@@ -757,6 +845,11 @@ struct hmp_stitcher {
     C.w = canvas->width;
     C.h = canvas->height;
 
+    // Copy-block mode for this call: planned, switched on, and every table entry the copy blocks
+    // read lies inside these frames (else it would read as a fill).
+    const int di = tile_down == 64 ? 1 : 0;
+    bool copy = copy_plan && copy_on && (n_fine == 0 || down_list[di] != nullptr);
+    for (int k = 0; copy && k < p.n; ++k) copy = uint32_t(S.w[k]) >= need_w[k] && uint32_t(S.h[k]) >= need_h[k];
     hmp::GatherArgs ga{};
     if (p.canvas_plane_used) {
       ga.S = S;
@@ -766,25 +859,40 @@ struct hmp_stitcher {
       ga.n_owners = p.n;
       ga.seg_owner = seg_owner;
       ga.seg_pitch = seg_pitch;
-      if (p.levels > 0) {
+      if (copy) {
+        // The gather writes the copy blocks too (the pyramid blocks' entries are skips) and checks
+        // the alpha of every source pixel it reads over the blend region.
+        ga.alpha_flag = alpha_flag;
+        ga.chk_x0 = p.blend.x;
+        ga.chk_y0 = p.blend.y;
+        ga.chk_x1 = p.blend.x + p.blend.w;
+        ga.chk_y1 = p.blend.y + p.blend.h;
+      } else if (p.levels > 0) {
         ga.skip_x0 = p.write.x;
         ga.skip_y0 = p.write.y;
         ga.skip_x1 = p.write.x + p.write.w;
         ga.skip_y1 = p.write.y + p.write.h;
       }
     }
+    // Without copy blocks a write rect covering the canvas leaves the gather nothing to do.
+    const bool gather = p.canvas_plane_used &&
+                        (p.levels == 0 || copy || p.write.w < p.canvas_w || p.write.h < p.canvas_h);
     cudaError_t e;
     if (p.levels == 0) {
       tbegin(0, s);
-      e = hmp::launch_canvas_gather(ga, s);
+      e = hmp::launch_canvas_gather(ga, copy_plan, s);
       tend(0, s);
       if (timing && tnext < kTimingSlots) ++tnext;
       if (e != cudaSuccess) return cuda_status(e, "canvas_gather launch");
       return ok_status();
     }
+    if (copy) {
+      e = cudaMemsetAsync(alpha_flag, 0, sizeof(int), s);
+      if (e != cudaSuccess) return cuda_status(e, "copy-block flag reset");
+    }
     // Fork: the pyramid goes to the high-priority stream `aux` when the canvas gather also
     // runs; the gather is launched on the caller stream after the pyramid kernels.
-    const bool fork = p.canvas_plane_used && !serialize;
+    const bool fork = gather && !serialize;
     cudaStream_t ps = s;
     if (fork) {
       e = cudaEventRecord(ev_fork, s);
@@ -836,42 +944,58 @@ struct hmp_stitcher {
       tend(1, ps);
       if (e != cudaSuccess) return failed(e, "Binomial5 pyramid launch");
     }
-    if (p.levels > 1 && !b5) {
-      a.tile = tile_down;
-      a.slots_cap = down_cap;
-      const dim3 grid((p.lw[0] + tile_down - 1) / tile_down, (p.lh[0] + tile_down - 1) / tile_down, p.batch);
-      tbegin(1, ps);
-      e = hmp::launch_pyr_down(a, p.storage, grid, ps);
-      tend(1, ps);
-      if (e != cudaSuccess) return failed(e, "pyr_down launch");
-    }
+    // Dense grids: every down tile of the blend region, the level-1 tiles holding the level-1
+    // pixels the fine pass reads (floor(x/2) and floor(x/2)+1 of the write rect), every 64 x 16
+    // block of the write rect.
     a.R1 = R1;
-    if (p.levels > 1 && !b5) {
-      // Level-1 pixels the fine pass reads: floor(x/2) and floor(x/2)+1 of the write rect.
+    const dim3 dgrid((p.lw[0] + tile_down - 1) / tile_down, (p.lh[0] + tile_down - 1) / tile_down, p.batch);
+    dim3 cgrid(1, 1, 1);
+    if (p.levels > 1) {
       const int x1lo = a.wx0 >> 1, x1hi = std::min(((a.wx1 - 1) >> 1) + 2, p.lw[1]);
       const int y1lo = a.wy0 >> 1, y1hi = std::min(((a.wy1 - 1) >> 1) + 2, p.lh[1]);
-      a.tile = tile_coarse;
-      a.coarse_cap = coarse_cap;
       a.tx0 = x1lo / tile_coarse;
       a.ty0 = y1lo / tile_coarse;
-      const dim3 cgrid((x1hi + tile_coarse - 1) / tile_coarse - a.tx0, (y1hi + tile_coarse - 1) / tile_coarse - a.ty0,
-                       p.batch);
-      tbegin(2, ps);
-      e = hmp::launch_pyr_coarse(a, p.rule, p.storage, cgrid, coarse_smem, ps);
-      tend(2, ps);
-      if (e != cudaSuccess) return failed(e, "pyr_coarse launch");
+      cgrid = dim3((x1hi + tile_coarse - 1) / tile_coarse - a.tx0, (y1hi + tile_coarse - 1) / tile_coarse - a.ty0,
+                   p.batch);
     }
-    if (!b5) {
-      const int fx0 = a.wx0 & ~1, fy0 = a.wy0 & ~1;
-      const dim3 fgrid((a.wx1 - fx0 + 63) / 64, (a.wy1 - fy0 + 15) / 16, p.batch);
-      tbegin(3, ps);
-      e = hmp::launch_pyr_fine(a, p.rule, p.storage, fgrid, ps);
-      tend(3, ps);
-      if (e != cudaSuccess) return failed(e, "pyr_fine launch");
-    }
-    if (p.canvas_plane_used) {
+    const int fx0 = a.wx0 & ~1, fy0 = a.wy0 & ~1;
+    const dim3 fgrid((a.wx1 - fx0 + 63) / 64, (a.wy1 - fy0 + 15) / 16, p.batch);
+    a.slots_cap = down_cap;
+    a.coarse_cap = coarse_cap;
+    // The pyramid chain: dense, or (copy-block mode) over the work lists.
+    const auto chain = [&](const hmp::PyrArgs& base, bool listed, cudaStream_t cs, bool timed) -> hmp_status {
+      hmp::PyrArgs q = base;
+      if (p.levels > 1 && !b5 && (!listed || n_down[di] > 0)) {
+        q.tile = tile_down;
+        q.tiles = listed ? down_list[di] : nullptr;
+        if (timed) tbegin(1, cs);
+        e = hmp::launch_pyr_down(q, p.storage, listed ? dim3(n_down[di], 1, p.batch) : dgrid, cs);
+        if (timed) tend(1, cs);
+        if (e != cudaSuccess) return failed(e, "pyr_down launch");
+      }
+      if (p.levels > 1 && !b5 && (!listed || n_coarse > 0)) {
+        q.tile = tile_coarse;
+        q.tiles = listed ? coarse_list : nullptr;
+        if (timed) tbegin(2, cs);
+        e = hmp::launch_pyr_coarse(q, p.rule, p.storage, listed ? dim3(n_coarse, 1, p.batch) : cgrid, coarse_smem, cs);
+        if (timed) tend(2, cs);
+        if (e != cudaSuccess) return failed(e, "pyr_coarse launch");
+      }
+      if (!b5 && (!listed || n_fine > 0)) {
+        q.tiles = listed ? fine_list : nullptr;
+        if (timed) tbegin(3, cs);
+        e = hmp::launch_pyr_fine(q, p.rule, p.storage, listed ? dim3(n_fine, 1, p.batch) : fgrid, cs);
+        if (timed) tend(3, cs);
+        if (e != cudaSuccess) return failed(e, "pyr_fine launch");
+      }
+      return ok_status();
+    };
+    if (copy) a.alpha_flag = alpha_flag;  // pyr_down checks the tiles marked for it
+    hmp_status cst = chain(a, copy, ps, true);
+    if (cst.code != HMP_OK) return cst;
+    if (gather) {
       tbegin(0, s);
-      e = hmp::launch_canvas_gather(ga, s);
+      e = hmp::launch_canvas_gather(ga, copy_plan, s);
       tend(0, s);
       if (e != cudaSuccess) return failed(e, "canvas_gather launch");
     }
@@ -879,6 +1003,16 @@ struct hmp_stitcher {
       e = cudaEventRecord(ev_join, aux);
       if (e == cudaSuccess) e = cudaStreamWaitEvent(s, ev_join, 0);
       if (e != cudaSuccess) return cuda_status(e, "stream join");
+    }
+    if (copy) {
+      // The fallback: the dense chain on the caller stream, every CTA returning at once unless a
+      // copy block's source pixels held alpha 0 (then it recomputes the whole write rect, copy
+      // blocks included, after the gather wrote them).
+      hmp::PyrArgs f = a;
+      f.alpha_flag = nullptr;
+      f.gate = alpha_flag;
+      cst = chain(f, false, s, false);
+      if (cst.code != HMP_OK) return cst;
     }
     if (timing && tnext < kTimingSlots) ++tnext;
     return ok_status();
@@ -947,10 +1081,25 @@ HMP_API hmp_status hmp_stitcher_get_info(const hmp_stitcher* st, hmp_stitcher_in
   std::memcpy(info->write_rect, wr, sizeof(wr));
   info->tile_down = st->tile_down;
   info->tile_coarse = st->tile_coarse;
-  info->launches_per_process = st->launches;
+  const bool copy = st->copy_plan && st->copy_on;
+  info->launches_per_process = copy ? st->copy_launches() : st->launches;
   info->m0_bytes = st->m0_bytes;
   info->device_bytes = double(st->device_bytes);
+  info->copy_mode = copy ? 1 : 0;
+  info->copy_blocks = st->copy_blocks;
+  info->empty_blocks = st->empty_blocks;
+  info->pyramid_blocks = st->pyramid_blocks;
+  info->pyramid_tiles[0] = st->n_down[st->tile_down == 64 ? 1 : 0];
+  info->pyramid_tiles[1] = st->n_coarse;
+  info->pyramid_tiles[2] = st->n_fine;
   return st->status;
+}
+
+HMP_API hmp_status hmp_stitcher_set_copy_blocks(hmp_stitcher* st, int enable) {
+  if (!st) return make_status(HMP_ERR_INVALID_VALUE, "stitcher is null");
+  if (st->status.code != HMP_OK) return st->status;
+  st->copy_on = enable != 0;
+  return ok_status();
 }
 
 HMP_API hmp_status hmp_stitcher_process(hmp_stitcher* st, const hmp_image* inputs, int n_inputs,
@@ -999,6 +1148,37 @@ HMP_API hmp_status hmp_stitcher_get_timing(hmp_stitcher* st, hmp_kernel_timing* 
   if (!st || !out) return make_status(HMP_ERR_INVALID_VALUE, "null argument");
   const cudaError_t e = st->timing_collect(out);
   if (e != cudaSuccess) return cuda_status(e, "timing events");
+  return ok_status();
+}
+
+HMP_API hmp_status hmp_plan_copy_blocks(const hmp_config* cfg, int* grid, uint8_t* classes, size_t capacity) {
+  if (!cfg || !grid) return make_status(HMP_ERR_INVALID_VALUE, "null argument");
+  hmp::Plan p;
+  std::string msg;
+  int rc = HMP_OK;
+  try {
+    rc = hmp::build_plan(*cfg, p, msg);
+  } catch (const std::bad_alloc&) {
+    return make_status(HMP_ERR_MEMORY_ALLOCATION, "out of host memory");
+  }
+  if (rc != HMP_OK) return make_status(rc, msg);
+  for (int i = 0; i < 4; ++i) grid[i] = 0;
+  if (p.levels < 2) return ok_status();
+  hmp::CopyPlan c;
+  try {
+    hmp::plan_copy_blocks(p, std::max(32, 1 << (p.levels - 1)), std::max(32, 1 << (p.levels - 2)), c);
+  } catch (const std::bad_alloc&) {
+    return make_status(HMP_ERR_MEMORY_ALLOCATION, "out of host memory");
+  }
+  if (!c.usable) return ok_status();
+  grid[0] = c.fx0 + p.blend.x;
+  grid[1] = c.fy0 + p.blend.y;
+  grid[2] = c.nfx;
+  grid[3] = c.nfy;
+  if (classes) {
+    if (capacity < c.block_class.size()) return make_status(HMP_ERR_INVALID_VALUE, "classes buffer too small");
+    std::memcpy(classes, c.block_class.data(), c.block_class.size());
+  }
   return ok_status();
 }
 

@@ -19,6 +19,7 @@ from .pano import (
     SpatialTiff,
     StitchServer,
     load_control_dir,
+    plan_copy_blocks,
     plan_geometry,
     read_seam_png,
     read_tiff_u16,
@@ -40,6 +41,7 @@ __all__ = [
     "StitchServer",
     "UNMAPPED_POSITION_VALUE",
     "load_control_dir",
+    "plan_copy_blocks",
     "plan_geometry",
     "read_seam_png",
     "read_tiff_u16",

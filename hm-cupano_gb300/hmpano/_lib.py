@@ -75,6 +75,11 @@ class StitcherInfo(C.Structure):
         ("launches_per_process", C.c_int),
         ("m0_bytes", C.c_double),
         ("device_bytes", C.c_double),
+        ("copy_mode", C.c_int),
+        ("copy_blocks", C.c_int),
+        ("empty_blocks", C.c_int),
+        ("pyramid_blocks", C.c_int),
+        ("pyramid_tiles", C.c_int * 3),
     ]
 
 
@@ -135,9 +140,11 @@ SIGNATURES = {
     "hmp_stitcher_process": ([C.c_void_p, C.POINTER(Image), C.c_int, C.POINTER(Image), C.c_void_p], Status),
     "hmp_stitcher_set_timing": ([C.c_void_p, C.c_int], Status),
     "hmp_stitcher_set_tiles": ([C.c_void_p, C.c_int, C.c_int], Status),
+    "hmp_stitcher_set_copy_blocks": ([C.c_void_p, C.c_int], Status),
     "hmp_stitcher_dump_pyramid": ([C.c_void_p, C.c_char_p, C.c_void_p], Status),
     "hmp_stitcher_get_timing": ([C.c_void_p, C.POINTER(KernelTiming)], Status),
     "hmp_plan_geometry": ([C.POINTER(Config), C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)], Status),
+    "hmp_plan_copy_blocks": ([C.POINTER(Config), C.POINTER(C.c_int), C.c_void_p, C.c_size_t], Status),
     "hmp_server_create": ([C.POINTER(ServerOptions), C.POINTER(C.c_void_p)], Status),
     "hmp_server_destroy": ([C.c_void_p], None),
     "hmp_server_add_config": ([C.c_void_p, C.POINTER(Config), C.POINTER(C.c_int)], Status),

@@ -503,11 +503,22 @@ class _Stitcher:
             "launches_per_process": inf.launches_per_process,
             "m0_bytes": inf.m0_bytes,
             "device_bytes": inf.device_bytes,
+            "copy_mode": bool(inf.copy_mode),
+            "copy_blocks": inf.copy_blocks,
+            "empty_blocks": inf.empty_blocks,
+            "pyramid_blocks": inf.pyramid_blocks,
+            "pyramid_tiles": tuple(inf.pyramid_tiles),
         }
 
     def set_tiles(self, tile_down: int, tile_coarse: int = 32) -> None:
         """Pyramid tile edges (tuning only: every choice gives the same bits)."""
         s = _status(_lib.lib().hmp_stitcher_set_tiles(self._handle, int(tile_down), int(tile_coarse)))
+        if not s.ok():
+            raise CudaStatusError(s)
+
+    def set_copy_blocks(self, enable: bool) -> None:
+        """Copy blocks on (default) or off (tuning and tests only: both give the same bits)."""
+        s = _status(_lib.lib().hmp_stitcher_set_copy_blocks(self._handle, 1 if enable else 0))
         if not s.ok():
             raise CudaStatusError(s)
 
@@ -680,6 +691,29 @@ def plan_geometry(kind: int, control_masks, num_levels: int, minimize_blend: boo
         raise CudaStatusError(st)
     v = list(out)
     return {"canvas": (cw.value, ch.value), "blend": tuple(v[0:4]), "write": tuple(v[4:8]), "levels": v[8]}
+
+
+def plan_copy_blocks(kind: int, control_masks, num_levels: int, minimize_blend: bool = True) -> dict:
+    """Host-only copy-block classes of a configuration (hmp_plan_copy_blocks): the canvas origin
+    and counts of its 64 x 16 blocks and a [ny, nx] uint8 array, 0 = copy, 1 = pyramid, 2 = empty
+    (None when the configuration has no copy blocks)."""
+    import numpy as np
+
+    cfg, keep = build_config(kind, control_masks, num_levels, 1, minimize_blend)
+    grid = (C.c_int * 4)()
+    st = _status(_lib.lib().hmp_plan_copy_blocks(C.byref(cfg), grid, None, 0))
+    if not st.ok():
+        raise CudaStatusError(st)
+    x0, y0, nx, ny = list(grid)
+    classes = None
+    if nx and ny:
+        classes = np.zeros((ny, nx), dtype=np.uint8)
+        st = _status(_lib.lib().hmp_plan_copy_blocks(C.byref(cfg), grid, classes.ctypes.data_as(C.c_void_p),
+                                                     classes.size))
+        if not st.ok():
+            raise CudaStatusError(st)
+    del keep
+    return {"origin": (x0, y0), "blocks": (nx, ny), "classes": classes}
 
 
 class StitchServer:

@@ -143,6 +143,15 @@ typedef struct hmp_stitcher_info {
   int launches_per_process; /* kernels one process() launches */
   double m0_bytes;   /* compulsory bytes per frame (maps, seam, sources, canvas) */
   double device_bytes; /* device memory held by the stitcher */
+  /* Copy blocks (three- and N-image box pyramids; see hmp_stitcher_set_copy_blocks): 1 if they
+   * are planned and switched on; the write rect's 64 x 16 blocks the canvas gather copies (one
+   * image's pixels) or zeroes, and those the pyramid computes; the pyramid kernels' work-list
+   * lengths (down tiles, coarse tiles, fine blocks). */
+  int copy_mode;
+  int copy_blocks;
+  int empty_blocks;
+  int pyramid_blocks;
+  int pyramid_tiles[3];
 } hmp_stitcher_info;
 
 /* ---- Control directory (host only; no GPU needed) ----
@@ -227,6 +236,21 @@ typedef struct hmp_kernel_timing {
   double total_ms[4];
   long long launches[4];
 } hmp_kernel_timing;
+
+/* Copy blocks: on (1, the default) or off (0). No counterpart in the reference.
+ * Three-image and N-image blend regions cover most of the canvas, but wherever the seam mask is
+ * one image's at every level of a pixel's reconstruction and that image is valid there, the
+ * pyramid's result is that image's pixel exactly (the box filter and bilinear upsample keep every
+ * value a short dyadic fraction, so FP32 rounds nothing). The stitcher plans such 64 x 16 blocks
+ * of the write rect at construction; per call the canvas gather copies them and the pyramid runs
+ * over the remaining blocks and the tiles their reconstruction reads. Two conditions are checked
+ * per call, and the full pyramid runs when either fails: the frames must contain every table
+ * entry the copy blocks read (host check), and every source pixel behind a copy block must have
+ * alpha != 0 (device check; a failure runs the whole write rect through the pyramid in three
+ * extra launches that otherwise return at once). Results are identical either way; off forces
+ * the full pyramid every call. Applies to RGBA8 stitchers of 3..8 images with the box filter and
+ * two or more levels. */
+HMP_API hmp_status hmp_stitcher_set_copy_blocks(hmp_stitcher* st, int enable);
 
 /* Enable (1) or disable (0) per-kernel event timing; enabling clears the accumulated times.
  * Mode 2 also serialises the kernels on the caller stream (no concurrent pyramid stream), so that
@@ -334,6 +358,13 @@ HMP_API hmp_status hmp_batch_capture(hmp_batch* batch, void* stream);
 HMP_API hmp_status hmp_batch_launch(hmp_batch* batch, void* stream);
 
 HMP_API hmp_status hmp_plan_geometry(const hmp_config* cfg, int* canvas_w, int* canvas_h, int* out9);
+
+/* The copy-block classes a stitcher of `cfg` plans (see hmp_stitcher_set_copy_blocks), host only,
+ * for inspection and tests; no counterpart in the reference. grid receives the canvas position of
+ * block (0, 0) and the block counts across and down (blocks are 64 x 16 pixels of the write rect;
+ * all zero when the configuration has no copy blocks). With classes non-NULL it receives one byte
+ * per block, row-major: 0 = copy (the label image's pixel), 1 = pyramid, 2 = empty (0, 0, 0, 0). */
+HMP_API hmp_status hmp_plan_copy_blocks(const hmp_config* cfg, int* grid, uint8_t* classes, size_t capacity);
 
 #ifdef __cplusplus
 }
