@@ -8,7 +8,8 @@ namespace hmp {
 void plan_copy_blocks(const Plan& p, int td, int t1, CopyPlan& cp) {
   cp = CopyPlan{};
   const int L = p.levels, n = p.n;
-  if (p.rule == kRuleTwo || L < 2 || p.filter != HMP_FILTER_REFBOX || p.generic() || !p.canvas_plane_used) return;
+  if (p.rule == kRuleTwo || n < 3 || L < 2 || p.filter != HMP_FILTER_REFBOX || p.generic() || !p.canvas_plane_used)
+    return;
   const int bw = p.lw[0], bh = p.lh[0];
   if (bw <= 0 || bh <= 0 || int(p.mask0.size()) != bw * bh || int(p.slots.size()) != n) return;
   // Level-(L-1) pixel q covers level-0 block q of edge G; per block: the label if uniform, and per
@@ -162,13 +163,11 @@ void plan_copy_blocks(const Plan& p, int td, int t1, CopyPlan& cp) {
   for (int ty = 0; ty < ndy; ++ty)
     for (int tx = 0; tx < ndx; ++tx) {
       if (!dmark[size_t(ty) * ndx + tx]) continue;
-      // Check the tile's source alpha if it meets a copy block's support.
-      bool chk = false;
-      const int x0 = tx * td, y0 = ty * td, x1 = std::min(x0 + td, bw) - 1, y1 = std::min(y0 + td, bh) - 1;
-      for (int by = y0 / G; by <= y1 / G && !chk; ++by)
-        for (int bx = x0 / G; bx <= x1 / G && !chk; ++bx) chk = support_mark[size_t(by) * gx + bx] != 0;
-      cp.down_list.push_back(uint32_t(tx) | (uint32_t(ty) << 16) | (chk ? 0x80000000u : 0u));
+      cp.down_list.push_back(uint32_t(tx) | (uint32_t(ty) << 16));
     }
+  cp.support_mark = std::move(support_mark);
+  cp.support_pitch = gx;
+  cp.support_shift = L - 1;
   cp.usable = cp.copy_blocks + cp.empty_blocks > 0 && ndx < 0x8000 && ndy < 0x8000 && ncx < 0x8000 &&
               ncy < 0x8000 && cp.nfx < 0x8000 && cp.nfy < 0x8000;
 }

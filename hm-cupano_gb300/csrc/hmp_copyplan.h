@@ -26,9 +26,10 @@
 // Per frame two conditions are checked, and either failure falls back to the full pyramid:
 //   * the table entries the copy blocks read must lie inside the frames (need_w / need_h, checked
 //     by the host per call: an out-of-range entry would read as a fill);
-//   * every source pixel in a copy block's support must have alpha != 0 (checked on the device by
-//     the gather for the pixels it copies and by pyr_down in the tiles marked for it; any alpha 0
-//     gates on the fallback launches, which recompute the whole write rect).
+//   * every source pixel in a copy block's support must have alpha != 0 (checked on the device:
+//     by the gather over the blend region, for the pixels it copies and those outside the write
+//     rect, and by pyr_fine for the pyramid-block pixels inside a support, the only others a
+//     support holds; any alpha 0 gates on the fallback launches, which recompute the write rect).
 // The pyramid then runs only where it is needed: pyr_fine over the pyramid blocks, pyr_coarse over
 // the level-1 tiles those read (R^1), pyr_down over the level-0 tiles whose levels either reads.
 #pragma once
@@ -49,16 +50,21 @@ struct CopyPlan {
   std::vector<uint8_t> block_class;         // [nfy][nfx]: kBlockCopy, kBlockPyramid or kBlockEmpty
   std::vector<uint32_t> fine_list;          // tx | ty << 16 of the pyramid blocks
   std::vector<uint32_t> coarse_list;        // absolute level-1 tiles of edge tile_coarse
-  std::vector<uint32_t> down_list;          // level-0 tiles of edge tile_down; bit 31: check alpha
+  std::vector<uint32_t> down_list;          // level-0 tiles of edge tile_down
+  // [gy][gx], one byte per 2^(L-1) block of the blend region: 1 inside some copy block's support
+  // (one label there, whose image has a source pixel at every pixel).
+  std::vector<uint8_t> support_mark;
+  int support_pitch = 0, support_shift = 0;
   uint32_t need_w[kMaxImages] = {}, need_h[kMaxImages] = {};  // frame size the copy blocks' entries need
   int copy_blocks = 0, empty_blocks = 0, pyramid_blocks = 0;
   long long dense_down = 0, dense_coarse = 0;  // tiles of the dense grids, for reports
 };
 
 // Plans copy blocks for `p` (its slot planes and level-0 labels must still be held on the host).
-// Leaves out.usable false where they do not apply: the two-image rule (its minimised strip is
-// seam-near throughout), fewer than two levels, the Binomial5 filter (its 5-tap sums are not short
-// dyadic fractions), and non-RGBA8 pixels.
+// Leaves out.usable false where they do not apply: fewer than three images (the two-image rule's
+// minimised strip is seam-near throughout, and two-image pyramid kernels carry no work lists),
+// fewer than two levels, the Binomial5 filter (its 5-tap sums are not short dyadic fractions), and
+// non-RGBA8 pixels.
 void plan_copy_blocks(const Plan& p, int tile_down, int tile_coarse, CopyPlan& out);
 
 }  // namespace hmp

@@ -55,11 +55,15 @@ struct PyrArgs {
   int coarse_cap; // N-way pyr_coarse: likewise, per coarse tile
   int fine_cap;   // N-way pyr_fine: likewise, per 64 x 16 level-0 block (with its upsample halo)
   int pdl;        // launch pyr_coarse / pyr_fine as programmatic dependents of the kernel before them
-  // Work list of the launch (copy-block mode): entry blockIdx.x is the CTA's tile, tx | ty << 16,
-  // with bit 31 set on pyr_down tiles whose source pixels feed a copy block's reconstruction
-  // (checked for alpha 0, which sets *alpha_flag). nullptr: the dense grid.
+  // Work list of the launch (copy-block mode): entry blockIdx.x is the CTA's tile, tx | ty << 16.
+  // nullptr: the dense grid.
   const uint32_t* tiles;
+  // Copy-block mode, pyr_fine: a level-0 pixel whose block of 2^sm_shift pixels is marked in
+  // support_mark ([.][sm_pitch], blend coordinates) lies in a copy block's reconstruction support;
+  // alpha 0 of its label image's pixel there sets *alpha_flag.
   int* alpha_flag;
+  const uint8_t* support_mark;
+  int sm_pitch, sm_shift;
   // Fallback launches: every CTA returns at once unless *gate != 0 (a copy block's source pixels
   // held alpha 0, so the whole write rect is recomputed). nullptr: always run.
   const int* gate;

@@ -316,7 +316,7 @@ int build_plan(const hmp_config& c, Plan& p, std::string& m) {
     seam_owner_plane(c, p);
     p.canvas_plane_used = true;
     p.canvas_opaque = false;
-  } else if (p.rule != kRuleTwo && p.levels >= 2 && p.filter == HMP_FILTER_REFBOX && !p.generic()) {
+  } else if (p.rule != kRuleTwo && p.n >= 3 && p.levels >= 2 && p.filter == HMP_FILTER_REFBOX && !p.generic()) {
     // Three images, or N without a minimised blend region: the pyramid covers the whole canvas,
     // and the seam-selected plane serves the copy blocks, where the pyramid's result is the
     // label's pixel (hmp_copyplan.h).

@@ -100,25 +100,31 @@ __device__ __forceinline__ Store* level_of(const PyrArgs& a, int k, int l, int b
 __device__ __forceinline__ void grid_dep_wait() { asm volatile("griddepcontrol.wait;\n" ::: "memory"); }
 
 // The tile of this CTA: blockIdx.x / y of the dense grid, or entry blockIdx.x of the launch's work
-// list (copy-block mode: tx | ty << 16, bit 31 = check the tile's source alpha). Returns false
+// list (copy-block mode: tx | ty << 16). Returns false
 // when the launch is a gated-off fallback (the gate is written before the launch's stream reaches
 // it, so every thread of every CTA reads the same value and returns together). Copy blocks apply
 // to three or more images only; the two-image kernels are compiled without this code (kLists
 // false), since extra code in them measured slower beside the canvas gather.
 template <bool kLists>
-__device__ __forceinline__ bool cta_tile(const PyrArgs& a, int& tx, int& ty, bool& check) {
+__device__ __forceinline__ bool cta_tile(const PyrArgs& a, int& tx, int& ty) {
   tx = int(blockIdx.x);
   ty = int(blockIdx.y);
-  check = false;
   if constexpr (!kLists) return true;
   if (a.gate != nullptr && *a.gate == 0) return false;
   if (a.tiles != nullptr) {
     const uint32_t t = __ldg(a.tiles + blockIdx.x);
     tx = int(t & 0xFFFFu);
-    ty = int((t >> 16) & 0x7FFFu);
-    check = (t >> 31) != 0u && a.alpha_flag != nullptr;
+    ty = int(t >> 16);
   }
   return true;
+}
+
+// Copy-block mode, at a pyramid-block pixel (blend coordinates x, y) with the label image's level-0
+// value v: inside a copy block's reconstruction support (support_mark, one byte per 2^(L-1) block)
+// that image's table entry is a source pixel, so alpha 0 there is the source's own, which breaks
+// the exactness the copy blocks rely on.
+__device__ __forceinline__ bool support_alpha_zero(const PyrArgs& a, int x, int y, uint32_t v) {
+  return (v >> 24) == 0u && __ldg(a.support_mark + (long long)(y >> a.sm_shift) * a.sm_pitch + (x >> a.sm_shift)) != 0;
 }
 
 template <int NMAX, typename Store, int TD>
@@ -135,12 +141,8 @@ __global__ void __launch_bounds__(256) pyr_down_kernel(const __grid_constant__ P
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int b = blockIdx.z;
   int tx, ty;
-  bool check;
-  if (!cta_tile<kKeepLevel0>(a, tx, ty, check)) return;
+  if (!cta_tile<kKeepLevel0>(a, tx, ty)) return;
   const int X0 = tx * TD, Y0 = ty * TD;
-  // Copy-block mode: which level-0 pixels are source reads, one ballot word per warp row and 32
-  // pixels, [slot][row][TD / 32] over the level-2 buffer (written only after the check).
-  uint32_t* src_bits = reinterpret_cast<uint32_t*>(bufB);
   const bool opaque = a.opaque != 0;
   const int L = a.levels;
   const int lw0 = a.lw[0], lh0 = a.lh[0], lw1 = a.lw[1], lh1 = a.lh[1];
@@ -196,37 +198,11 @@ __global__ void __launch_bounds__(256) pyr_down_kernel(const __grid_constant__ P
           cp_async<4>(d, sp);
         else
           *d = fill;
-        if constexpr (kKeepLevel0) {
-          if (check) {
-            const unsigned m = __ballot_sync(0xFFFFFFFFu, sp != nullptr);
-            if (lane == 0) src_bits[(k * TD + r) * (TD / 32) + j] = m;
-          }
-        }
       }
     }
   }
   cp_async_commit_wait_all();
   __syncthreads();
-  if constexpr (kKeepLevel0) {
-    // Copy-block mode: a source pixel with alpha 0 breaks the exactness a copy block relies on,
-    // so it sends the frame to the fallback (the whole write rect through the pyramid).
-    if (check) {
-      bool bad = false;
-#pragma unroll
-      for (int k = 0; k < NMAX; ++k) {
-        if (!active[k]) continue;
-        for (int r = warp; r < TD; r += 8)
-#pragma unroll
-          for (int j = 0; j < TD / 32; ++j) {
-            const unsigned m = src_bits[(k * TD + r) * (TD / 32) + j];
-            const uint32_t v = pix[k * TD * TD + r * TD + 32 * j + lane];
-            bad = bad || (((m >> lane) & 1u) != 0u && (v >> 24) == 0u);
-          }
-      }
-      if (__any_sync(0xFFFFFFFFu, bad) && lane == 0) atomicOr(a.alpha_flag, 1);
-      __syncthreads();  // the bits overlay the level-2 buffer written below
-    }
-  }
   // Level 0 for pyr_fine: each slot's gathered pixels inside its plane rect, so that the level-0
   // pass reads them back directly instead of repeating the table lookups and gathers.
   if constexpr (kKeepLevel0) {
@@ -354,10 +330,8 @@ __global__ void __launch_bounds__(256) pyr_down_n_kernel(const __grid_constant__
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int b = blockIdx.z;
   int tx, ty;
-  bool check;
-  if (!cta_tile<true>(a, tx, ty, check)) return;
+  if (!cta_tile<true>(a, tx, ty)) return;
   const int X0 = tx * TD, Y0 = ty * TD;
-  uint32_t* src_bits = reinterpret_cast<uint32_t*>(bufB);  // as in pyr_down_kernel, per list entry
   const bool opaque = a.opaque != 0;
   const int L = a.levels;
   const int lw0 = a.lw[0], lh0 = a.lh[0], lw1 = a.lw[1], lh1 = a.lh[1];
@@ -409,29 +383,11 @@ __global__ void __launch_bounds__(256) pyr_down_n_kernel(const __grid_constant__
           cp_async<4>(d, sp);
         else
           *d = fill;
-        if (check) {
-          const unsigned m = __ballot_sync(0xFFFFFFFFu, sp != nullptr);
-          if (lane == 0) src_bits[(c * TD + r) * (TD / 32) + j] = m;
-        }
       }
     }
   }
   cp_async_commit_wait_all();
   __syncthreads();
-  if (check) {  // as in pyr_down_kernel
-    bool bad = false;
-#pragma unroll 1
-    for (int c = 0; c < na; ++c)
-      for (int r = warp; r < TD; r += 8)
-#pragma unroll
-        for (int j = 0; j < TD / 32; ++j) {
-          const unsigned m = src_bits[(c * TD + r) * (TD / 32) + j];
-          const uint32_t v = pix[c * TD * TD + r * TD + 32 * j + lane];
-          bad = bad || (((m >> lane) & 1u) != 0u && (v >> 24) == 0u);
-        }
-    if (__any_sync(0xFFFFFFFFu, bad) && lane == 0) atomicOr(a.alpha_flag, 1);
-    __syncthreads();
-  }
   if (a.use_p0) {
 #pragma unroll 1
     for (int c = 0; c < na; ++c) {
@@ -564,8 +520,7 @@ __global__ void __launch_bounds__(256) pyr_coarse_kernel(const __grid_constant__
   extern __shared__ float4 sm[];
   char* smb = reinterpret_cast<char*>(sm);
   int tx, ty;
-  bool check;
-  if (!cta_tile<RULE != kRuleTwo>(a, tx, ty, check)) return;
+  if (!cta_tile<RULE != kRuleTwo>(a, tx, ty)) return;
   if (RULE == kRuleTwo || a.tiles == nullptr) tx += a.tx0, ty += a.ty0;
   grid_dep_wait();  // G^l of pyr_down
   const int n = RULE == kRuleNway ? a.n : NMAX;
@@ -785,8 +740,7 @@ __global__ void __launch_bounds__(256) pyr_coarse_n_kernel(const __grid_constant
   extern __shared__ float4 sm[];
   char* smb = reinterpret_cast<char*>(sm);
   int tx, ty;
-  bool check;
-  if (!cta_tile<true>(a, tx, ty, check)) return;
+  if (!cta_tile<true>(a, tx, ty)) return;
   if (a.tiles == nullptr) tx += a.tx0, ty += a.ty0;
   grid_dep_wait();  // G^l of pyr_down
   const int n = a.n, K = a.K, cap = a.coarse_cap;
@@ -990,8 +944,7 @@ template <int RULE, int NMAX, typename Store, bool P0M>
 __global__ void __launch_bounds__(256) pyr_fine_kernel(const __grid_constant__ PyrArgs a) {
   extern __shared__ float4 fsm[];  // R^1 tile, then G^1 tiles of slots 0..n-1 (Store)
   int tx, ty;
-  bool check;
-  if (!cta_tile<RULE != kRuleTwo>(a, tx, ty, check)) return;
+  if (!cta_tile<RULE != kRuleTwo>(a, tx, ty)) return;
   const int n = RULE == kRuleNway ? a.n : NMAX;
   const int b = blockIdx.z;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -1079,6 +1032,7 @@ __global__ void __launch_bounds__(256) pyr_fine_kernel(const __grid_constant__ P
       asm volatile("cp.async.wait_group 0;\n" ::: "memory");
       __syncthreads();
     }
+    bool bad = false;  // copy-block mode: alpha 0 of the label image inside a copy block's support
 #pragma unroll
     for (int u = 0; u < QB; ++u) {
       const int q = q0 + u;
@@ -1087,7 +1041,14 @@ __global__ void __launch_bounds__(256) pyr_fine_kernel(const __grid_constant__ P
       float al[NMAX];
 #pragma unroll
       for (int k = 0; k < NMAX; ++k) al[k] = float(src[u][k].w);
+
       const int pk = blend_pick0<RULE, NMAX>(n, al, mv[u]);
+      if constexpr (P0M && RULE != kRuleTwo) {
+        // The three- and N-way picks return the label's image exactly when it has alpha, so a
+        // valid label picked otherwise had alpha 0.
+        if (a.alpha_flag != nullptr && mv[u] < n && pk != mv[u])
+          bad = bad || support_alpha_zero(a, X + (q & 1), Y + (q >> 1), 0u);
+      }
       float4 r = make_float4(0.f, 0.f, 0.f, 0.f);
       if (pk >= 0) {
         uchar4 sp = src[u][0];
@@ -1128,6 +1089,9 @@ __global__ void __launch_bounds__(256) pyr_fine_kernel(const __grid_constant__ P
                                                (long long)(py + a.cy_off) * a.C.pitch);
       crow[px + a.cx_off] = pack_rgba(r);
     }
+    if constexpr (P0M && RULE != kRuleTwo) {
+      if (a.alpha_flag != nullptr && __any_sync(0xFFFFFFFFu, bad) && lane == 0) atomicOr(a.alpha_flag, 1);
+    }
   }
 }
 
@@ -1140,8 +1104,7 @@ template <typename Store>
 __global__ void __launch_bounds__(256) pyr_fine_n_kernel(const __grid_constant__ PyrArgs a) {
   extern __shared__ float4 fsm[];
   int tx, ty;
-  bool check;
-  if (!cta_tile<true>(a, tx, ty, check)) return;
+  if (!cta_tile<true>(a, tx, ty)) return;
   grid_dep_wait();  // R^1 of pyr_coarse; G^1 and level 0 of pyr_down
   const int n = a.n, cap = a.fine_cap;
   const int b = blockIdx.z;
@@ -1192,6 +1155,13 @@ __global__ void __launch_bounds__(256) pyr_fine_n_kernel(const __grid_constant__
         if ((unsigned)rx < (unsigned)P.w && (unsigned)ry < (unsigned)P.h)
           p[q] = __ldg(a.P0[v[q]] + (long long)b * P.w * P.h + (long long)ry * P.w + rx);
       }
+    }
+    if (a.alpha_flag != nullptr) {  // copy-block mode, as in pyr_fine_kernel
+      bool bad = false;
+#pragma unroll
+      for (int q = 0; q < 4; ++q)
+        bad = bad || (live[q] && v[q] < n && support_alpha_zero(a, X + (q & 1), Y + (q >> 1), p[q]));
+      if (__any_sync(0xFFFFFFFFu, bad) && lane == 0) atomicOr(a.alpha_flag, 1);
     }
 #pragma unroll
     for (int q = 0; q < 4; ++q) {

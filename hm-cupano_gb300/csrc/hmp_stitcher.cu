@@ -138,6 +138,8 @@ struct hmp_stitcher {
   const uint32_t* down_list[2] = {};  // tile_down 32, 64 (nullptr where that tile is not allowed)
   int n_fine = 0, n_coarse = 0, n_down[2] = {};
   int* alpha_flag = nullptr;
+  const uint8_t* support_mark = nullptr;  // per 2^(L-1) block of the blend region (pyr_fine's check)
+  int sm_pitch = 0, sm_shift = 0;
   hmp::SkipMap skip{};
   uint32_t need_w[hmp::kDevMaxImages]{}, need_h[hmp::kDevMaxImages]{};
   int copy_blocks = 0, empty_blocks = 0, pyramid_blocks = 0;
@@ -499,6 +501,13 @@ struct hmp_stitcher {
     n_fine = int(c.fine_list.size());
     n_coarse = int(c.coarse_list.size());
     alpha_flag = reinterpret_cast<int*>(static_cast<char*>(m) + flag_off);
+    void* sm = nullptr;
+    e = alloc(&sm, c.support_mark.size());
+    if (e == cudaSuccess) e = cudaMemcpy(sm, c.support_mark.data(), c.support_mark.size(), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return cuda_status(e, "copy-block support upload");
+    support_mark = static_cast<const uint8_t*>(sm);
+    sm_pitch = c.support_pitch;
+    sm_shift = c.support_shift;
     skip.map = static_cast<const uint8_t*>(m);
     skip.pitch = c.nfx;
     skip.x0 = c.fx0 + p.blend.x;
@@ -990,7 +999,12 @@ struct hmp_stitcher {
       }
       return ok_status();
     };
-    if (copy) a.alpha_flag = alpha_flag;  // pyr_down checks the tiles marked for it
+    if (copy) {  // pyr_fine checks the pyramid-block pixels inside copy blocks' supports
+      a.alpha_flag = alpha_flag;
+      a.support_mark = support_mark;
+      a.sm_pitch = sm_pitch;
+      a.sm_shift = sm_shift;
+    }
     hmp_status cst = chain(a, copy, ps, true);
     if (cst.code != HMP_OK) return cst;
     if (gather) {

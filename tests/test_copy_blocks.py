@@ -55,7 +55,7 @@ def test_copy_blocks_equal_the_oracle_pyramid(oracle_lib):
 
 def test_copy_blocks_cover_most_of_the_named_rigs():
     """The three-image stream of the batched workload and the eight-image rig: most write-rect
-    blocks are copies. The two-image rule and one-level pyramids have none."""
+    blocks are copies. Two images and one-level pyramids have none."""
     import hmpano
     from hmpano import synth
 
@@ -68,3 +68,5 @@ def test_copy_blocks_cover_most_of_the_named_rigs():
     assert hmpano.plan_copy_blocks(2, masks_for_rig(rig), 6)["classes"] is None
     rig = synth.workload_rig("pano3_2704x1520_to_6000x1800", seed=3, kind=3, scale=0.25)
     assert hmpano.plan_copy_blocks(3, masks_for_rig(rig), 1)["classes"] is None
+    rig = synth.make_rig(600, 300, 2, 400, 280, 0.3, seed=5, kind=1)  # N-image stitcher of two images
+    assert hmpano.plan_copy_blocks(1, masks_for_rig(rig), 4, False)["classes"] is None
