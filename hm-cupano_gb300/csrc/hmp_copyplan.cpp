@@ -8,8 +8,11 @@ namespace hmp {
 void plan_copy_blocks(const Plan& p, int td, int t1, CopyPlan& cp) {
   cp = CopyPlan{};
   const int L = p.levels, n = p.n;
-  if (p.rule == kRuleTwo || n < 3 || L < 2 || p.filter != HMP_FILTER_REFBOX || p.generic() || !p.canvas_plane_used)
-    return;
+  if (L < 2 || p.filter != HMP_FILTER_REFBOX || p.generic() || !p.canvas_plane_used) return;
+  const bool two = p.rule == kRuleTwo;
+  // Two images: the minimised strip only, whose content lines up with the canvas (image 1's table
+  // at column 0); three or more: any blend region.
+  if (two ? (!p.minimized || p.strip_shift != 0) : n < 3) return;
   const int bw = p.lw[0], bh = p.lh[0];
   if (bw <= 0 || bh <= 0 || int(p.mask0.size()) != bw * bh || int(p.slots.size()) != n) return;
   // Level-(L-1) pixel q covers level-0 block q of edge G; per block: the label if uniform, and per
@@ -29,15 +32,16 @@ void plan_copy_blocks(const Plan& p, int td, int t1, CopyPlan& cp) {
         b = kMixed;
     }
   }
+  // Per slot: whether every / any pixel of a block has a non-sentinel entry; per image: the largest
+  // coordinates its entries there hold (a two-image strip's second slot mixes images 1 and 2).
   const size_t nb = size_t(gx) * gy;
   std::vector<uint8_t> all_valid(size_t(n) * nb, 1), any_valid(size_t(n) * nb, 0);
   std::vector<uint16_t> max_sx(size_t(n) * nb, 0), max_sy(size_t(n) * nb, 0);
+  std::vector<uint8_t> img2_any(two ? nb : 0, 0);  // two images: any entry of image 2 in the block
   for (int k = 0; k < n; ++k) {
     const GatherPlane& s = p.slots[k];
     uint8_t* av = &all_valid[size_t(k) * nb];
     uint8_t* an = &any_valid[size_t(k) * nb];
-    uint16_t* mx = &max_sx[size_t(k) * nb];
-    uint16_t* my = &max_sy[size_t(k) * nb];
     // Blocks not wholly inside the plane's rect hold pixels without an entry.
     for (int by = 0; by < gy; ++by)
       for (int bx = 0; bx < gx; ++bx) {
@@ -52,15 +56,19 @@ void plan_copy_blocks(const Plan& p, int td, int t1, CopyPlan& cp) {
         const int x = s.rect.x + rx;
         const size_t i = size_t(ry) * s.rect.w + rx;
         const uint32_t e = s.map[i];
-        const bool mine = s.owner.empty() ? s.default_owner == k : s.owner[i] == k;
+        const int o = s.owner.empty() ? s.default_owner : s.owner[i];
         const size_t b = size_t(y / G) * gx + x / G;
-        if (!mine || (e & 0xFFFFu) == 0xFFFFu) {
+        if (two && o == 1) img2_any[b] = 1;
+        // Three or more images: each slot holds its own image only.
+        if (o >= n || (!two && o != k) || (e & 0xFFFFu) == 0xFFFFu) {
           av[b] = 0;
           continue;
         }
         an[b] = 1;
-        mx[b] = std::max<uint16_t>(mx[b], uint16_t(e & 0xFFFFu));
-        my[b] = std::max<uint16_t>(my[b], uint16_t(e >> 16));
+        uint16_t& mx = max_sx[size_t(o) * nb + b];
+        uint16_t& my = max_sy[size_t(o) * nb + b];
+        mx = std::max<uint16_t>(mx, uint16_t(e & 0xFFFFu));
+        my = std::max<uint16_t>(my, uint16_t(e >> 16));
       }
     }
   }
@@ -85,12 +93,18 @@ void plan_copy_blocks(const Plan& p, int td, int t1, CopyPlan& cp) {
       const int y0 = std::max(cp.fy0 + 16 * j, wy0), y1 = std::min(cp.fy0 + 16 * j + 16, wy1);
       const int sx0 = x0 >> (L - 1), sx1 = hi_chain(x1 - 1, p.lw);
       const int sy0 = y0 >> (L - 1), sy1 = hi_chain(y1 - 1, p.lh);
-      const int k = lab[size_t(sy0) * gx + sx0];
+      // The slot whose pixel the block copies: the label's image; with two images the seam value
+      // 1 selects slot 0 (image 1) and 0 slot 1 (image 2, or image 1 where image 2 has no table).
+      const int label = lab[size_t(sy0) * gx + sx0];
+      const int k = two ? (label == 1 ? 0 : (label == 0 ? 1 : n)) : label;
       bool copy = k < n, empty = true;
       for (int by = sy0; by <= sy1; ++by)
         for (int bx = sx0; bx <= sx1; ++bx) {
           const size_t b = size_t(by) * gx + bx;
-          if (copy && (lab[b] != k || !all_valid[size_t(k) * nb + b])) copy = false;
+          if (copy && (lab[b] != label || !all_valid[size_t(k) * nb + b])) copy = false;
+          // Two images, slot 0: the blend keeps slot 1's alpha where slot 1 has any, and the canvas
+          // plane there holds image 2, so image 2's table must be absent from the support.
+          if (copy && two && k == 0 && img2_any[b]) copy = false;
           for (int q = 0; q < n && empty; ++q)
             if (any_valid[size_t(q) * nb + b]) empty = false;
         }
@@ -101,9 +115,12 @@ void plan_copy_blocks(const Plan& p, int td, int t1, CopyPlan& cp) {
         for (int by = sy0; by <= sy1; ++by)
           for (int bx = sx0; bx <= sx1; ++bx) {
             const size_t b = size_t(by) * gx + bx;
-            support_mark[b] = 1;
-            cp.need_w[k] = std::max<uint32_t>(cp.need_w[k], uint32_t(max_sx[size_t(k) * nb + b]) + 1u);
-            cp.need_h[k] = std::max<uint32_t>(cp.need_h[k], uint32_t(max_sy[size_t(k) * nb + b]) + 1u);
+            support_mark[b] = uint8_t(1 + k);
+            for (int o = 0; o < n; ++o) {  // every image the slot's entries select (one, or two)
+              if (!two && o != k) continue;
+              cp.need_w[o] = std::max<uint32_t>(cp.need_w[o], uint32_t(max_sx[size_t(o) * nb + b]) + 1u);
+              cp.need_h[o] = std::max<uint32_t>(cp.need_h[o], uint32_t(max_sy[size_t(o) * nb + b]) + 1u);
+            }
           }
       } else if (empty) {
         ++cp.empty_blocks;

@@ -51,8 +51,8 @@ struct CopyPlan {
   std::vector<uint32_t> fine_list;          // tx | ty << 16 of the pyramid blocks
   std::vector<uint32_t> coarse_list;        // absolute level-1 tiles of edge tile_coarse
   std::vector<uint32_t> down_list;          // level-0 tiles of edge tile_down
-  // [gy][gx], one byte per 2^(L-1) block of the blend region: 1 inside some copy block's support
-  // (one label there, whose image has a source pixel at every pixel).
+  // [gy][gx], one byte per 2^(L-1) block of the blend region: 1 + the slot a copy block copies
+  // inside its support (one label there, and that slot has a source pixel at every pixel), else 0.
   std::vector<uint8_t> support_mark;
   int support_pitch = 0, support_shift = 0;
   uint32_t need_w[kMaxImages] = {}, need_h[kMaxImages] = {};  // frame size the copy blocks' entries need
@@ -61,10 +61,10 @@ struct CopyPlan {
 };
 
 // Plans copy blocks for `p` (its slot planes and level-0 labels must still be held on the host).
-// Leaves out.usable false where they do not apply: fewer than three images (the two-image rule's
-// minimised strip is seam-near throughout, and two-image pyramid kernels carry no work lists),
-// fewer than two levels, the Binomial5 filter (its 5-tap sums are not short dyadic fractions), and
-// non-RGBA8 pixels.
+// Leaves out.usable false where they do not apply: two images without the minimised strip (or with
+// image 1's table off column 0, which shifts the strip's content against the canvas), N-image
+// stitchers of two images, fewer than two levels, the Binomial5 filter (its 5-tap sums are not
+// short dyadic fractions), and non-RGBA8 pixels.
 void plan_copy_blocks(const Plan& p, int tile_down, int tile_coarse, CopyPlan& out);
 
 }  // namespace hmp

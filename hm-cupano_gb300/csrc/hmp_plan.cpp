@@ -257,6 +257,7 @@ int plan_geometry(const hmp_config& c, Plan& p, std::string& m) {
       p.minimized = true;
       p.blend = Rect{x_start, 0, x_end - x_start, H};
       p.write = p.blend;
+      p.strip_shift = x1;
     }
   } else if (c.kind == HMP_KIND_PANO3) {
     p.rule = kRuleThree;

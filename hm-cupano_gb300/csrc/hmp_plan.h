@@ -72,6 +72,9 @@ struct Plan {
   std::vector<std::vector<float>> mask_levels;  // levels >= 1: lw*lh*mask_k floats
   std::vector<std::vector<uint8_t>> mask_hot;   // N-way rule, levels >= 1: lw*lh MaskHot classes
   std::vector<int> lw, lh;          // level dims
+  // Two images, minimised: the blend strip's content is the canvas shifted by image 1's table
+  // column (the reference copies full1 / full2 out of the canvas at that offset).
+  int strip_shift = 0;
   std::vector<int> src_w, src_h;    // expected source sizes (0 = unknown)
 };
 

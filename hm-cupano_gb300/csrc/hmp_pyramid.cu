@@ -127,7 +127,9 @@ __device__ __forceinline__ bool support_alpha_zero(const PyrArgs& a, int x, int 
   return (v >> 24) == 0u && __ldg(a.support_mark + (long long)(y >> a.sm_shift) * a.sm_pitch + (x >> a.sm_shift)) != 0;
 }
 
-template <int NMAX, typename Store, int TD>
+// kListed: work lists and the fallback gate (copy-block mode); always on for three or more images,
+// a separate instantiation for two, whose dense kernels stay free of that code.
+template <int NMAX, typename Store, int TD, bool kListed = false>
 __global__ void __launch_bounds__(256) pyr_down_kernel(const __grid_constant__ PyrArgs a) {
   // Only the three- and N-image kernels keep level 0 for pyr_fine; the two-image kernel is
   // compiled without that code (it measured faster that way, running beside the canvas gather).
@@ -141,7 +143,7 @@ __global__ void __launch_bounds__(256) pyr_down_kernel(const __grid_constant__ P
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int b = blockIdx.z;
   int tx, ty;
-  if (!cta_tile<kKeepLevel0>(a, tx, ty)) return;
+  if (!cta_tile<kKeepLevel0 || kListed>(a, tx, ty)) return;
   const int X0 = tx * TD, Y0 = ty * TD;
   const bool opaque = a.opaque != 0;
   const int L = a.levels;
@@ -515,13 +517,14 @@ __host__ __device__ inline CoarseLayout coarse_layout(int n, int K, int T1, int 
   return o;
 }
 
-template <int RULE, int NMAX, typename Store, int T1>
+template <int RULE, int NMAX, typename Store, int T1, bool kListed = false>
 __global__ void __launch_bounds__(256) pyr_coarse_kernel(const __grid_constant__ PyrArgs a) {
   extern __shared__ float4 sm[];
   char* smb = reinterpret_cast<char*>(sm);
   int tx, ty;
-  if (!cta_tile<RULE != kRuleTwo>(a, tx, ty)) return;
-  if (RULE == kRuleTwo || a.tiles == nullptr) tx += a.tx0, ty += a.ty0;
+  constexpr bool kLists = RULE != kRuleTwo || kListed;
+  if (!cta_tile<kLists>(a, tx, ty)) return;
+  if (!kLists || a.tiles == nullptr) tx += a.tx0, ty += a.ty0;
   grid_dep_wait();  // G^l of pyr_down
   const int n = RULE == kRuleNway ? a.n : NMAX;
   const int K = RULE == kRuleTwo ? 1 : (RULE == kRuleThree ? 3 : a.K);
@@ -940,11 +943,11 @@ __device__ __forceinline__ float3 up_tile(const T* t, int i, bool ox, bool oy) {
 // source gathers, and waits for the tiles only after that. Per pixel: Lap = G^0 - up(G^1) of the
 // picked image (of every image where the weights are fractional), blend, add up(R^1), truncating
 // pack into the canvas.
-template <int RULE, int NMAX, typename Store, bool P0M>
+template <int RULE, int NMAX, typename Store, bool P0M, bool kListed = false>
 __global__ void __launch_bounds__(256) pyr_fine_kernel(const __grid_constant__ PyrArgs a) {
   extern __shared__ float4 fsm[];  // R^1 tile, then G^1 tiles of slots 0..n-1 (Store)
   int tx, ty;
-  if (!cta_tile<RULE != kRuleTwo>(a, tx, ty)) return;
+  if (!cta_tile<RULE != kRuleTwo || kListed>(a, tx, ty)) return;
   const int n = RULE == kRuleNway ? a.n : NMAX;
   const int b = blockIdx.z;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -1048,6 +1051,13 @@ __global__ void __launch_bounds__(256) pyr_fine_kernel(const __grid_constant__ P
         // valid label picked otherwise had alpha 0.
         if (a.alpha_flag != nullptr && mv[u] < n && pk != mv[u])
           bad = bad || support_alpha_zero(a, X + (q & 1), Y + (q >> 1), 0u);
+      } else if constexpr (RULE == kRuleTwo && kListed) {
+        // Two images: the support's mark names the slot its copy block copies (1 + slot).
+        if (a.alpha_flag != nullptr && (al[0] == 0.f || al[1] == 0.f)) {
+          const int x = X + (q & 1), y = Y + (q >> 1);
+          const int m = __ldg(a.support_mark + (long long)(y >> a.sm_shift) * a.sm_pitch + (x >> a.sm_shift));
+          bad = bad || (m == 1 && al[0] == 0.f) || (m == 2 && al[1] == 0.f);
+        }
       }
       float4 r = make_float4(0.f, 0.f, 0.f, 0.f);
       if (pk >= 0) {
@@ -1089,7 +1099,7 @@ __global__ void __launch_bounds__(256) pyr_fine_kernel(const __grid_constant__ P
                                                (long long)(py + a.cy_off) * a.C.pitch);
       crow[px + a.cx_off] = pack_rgba(r);
     }
-    if constexpr (P0M && RULE != kRuleTwo) {
+    if constexpr ((P0M && RULE != kRuleTwo) || (RULE == kRuleTwo && kListed)) {
       if (a.alpha_flag != nullptr && __any_sync(0xFFFFFFFFu, bad) && lane == 0) atomicOr(a.alpha_flag, 1);
     }
   }
@@ -1218,20 +1228,21 @@ __global__ void __launch_bounds__(256) pyr_fine_n_kernel(const __grid_constant__
   }
 }
 
-template <int NMAX, typename Store, int T>
+template <int NMAX, typename Store, int T, bool L = false>
 void set_down_attr() {
-  cudaFuncSetAttribute(pyr_down_kernel<NMAX, Store, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+  cudaFuncSetAttribute(pyr_down_kernel<NMAX, Store, T, L>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
 }
 
-template <int RULE, int NMAX, typename Store, int T>
+template <int RULE, int NMAX, typename Store, int T, bool L = false>
 void set_up_attr() {
-  cudaFuncSetAttribute(pyr_coarse_kernel<RULE, NMAX, Store, T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  cudaFuncSetAttribute(pyr_coarse_kernel<RULE, NMAX, Store, T, L>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        227 * 1024);
 }
 
 template <typename Store, int T>
 void set_down_attrs() {
   set_down_attr<2, Store, T>();
+  set_down_attr<2, Store, T, true>();
   set_down_attr<3, Store, T>();
   set_down_attr<8, Store, T>();
   cudaFuncSetAttribute(pyr_down_n_kernel<Store, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
@@ -1240,6 +1251,7 @@ void set_down_attrs() {
 template <typename Store, int T>
 void set_coarse_attrs() {
   set_up_attr<kRuleTwo, 2, Store, T>();
+  set_up_attr<kRuleTwo, 2, Store, T, true>();
   set_up_attr<kRuleThree, 3, Store, T>();
   set_up_attr<kRuleNway, 8, Store, T>();
   cudaFuncSetAttribute(pyr_coarse_n_kernel<Store, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
@@ -1247,7 +1259,9 @@ void set_coarse_attrs() {
 
 template <typename Store, int T>
 void down_dispatch(const PyrArgs& a, dim3 grid, size_t smem, cudaStream_t stream) {
-  if (a.n <= 2)
+  if (a.n <= 2 && (a.tiles != nullptr || a.gate != nullptr))
+    pyr_down_kernel<2, Store, T, true><<<grid, 256, smem, stream>>>(a);
+  else if (a.n <= 2)
     pyr_down_kernel<2, Store, T><<<grid, 256, smem, stream>>>(a);
   else if (a.n == 3)
     pyr_down_kernel<3, Store, T><<<grid, 256, smem, stream>>>(a);
@@ -1276,7 +1290,9 @@ void launch_pyr(Kern k, dim3 grid, size_t smem, cudaStream_t stream, const PyrAr
 
 template <typename Store, int T>
 void coarse_dispatch(const PyrArgs& a, int rule, dim3 grid, size_t smem, cudaStream_t stream) {
-  if (rule == kRuleTwo)
+  if (rule == kRuleTwo && (a.tiles != nullptr || a.gate != nullptr))
+    launch_pyr(pyr_coarse_kernel<kRuleTwo, 2, Store, T, true>, grid, smem, stream, a);
+  else if (rule == kRuleTwo)
     launch_pyr(pyr_coarse_kernel<kRuleTwo, 2, Store, T>, grid, smem, stream, a);
   else if (rule == kRuleThree)
     launch_pyr(pyr_coarse_kernel<kRuleThree, 3, Store, T>, grid, smem, stream, a);
@@ -1288,7 +1304,9 @@ void coarse_dispatch(const PyrArgs& a, int rule, dim3 grid, size_t smem, cudaStr
 
 template <typename Store, bool P0M>
 void fine_dispatch2(const PyrArgs& a, int rule, dim3 grid, size_t smem, cudaStream_t stream) {
-  if (rule == kRuleTwo)
+  if (rule == kRuleTwo && (a.tiles != nullptr || a.gate != nullptr))
+    launch_pyr(pyr_fine_kernel<kRuleTwo, 2, Store, P0M, true>, grid, smem, stream, a);
+  else if (rule == kRuleTwo)
     launch_pyr(pyr_fine_kernel<kRuleTwo, 2, Store, P0M>, grid, smem, stream, a);
   else if (rule == kRuleThree)
     launch_pyr(pyr_fine_kernel<kRuleThree, 3, Store, P0M>, grid, smem, stream, a);

@@ -429,7 +429,7 @@ struct hmp_stitcher {
       launches += b5 ? hmp::b5_launches(L) : (L > 1 ? 2 : 0) + 1;
     }
     if (generic) launches = hmp::generic_launches(p.levels, p.canvas_plane_used);
-    if (p.levels > 1 && !b5 && !generic && p.canvas_plane_used && p.rule != hmp::kRuleTwo) {
+    if (p.levels > 1 && !b5 && !generic && p.canvas_plane_used) {
       const hmp_status cs = setup_copy_blocks();
       if (cs.code != HMP_OK) return cs;
     }

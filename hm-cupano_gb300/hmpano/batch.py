@@ -10,7 +10,8 @@ streams' kernels overlap on the GPU and one graph launch runs the whole job. Fra
 synthetic frames, shifted per stream and frame.
 
 The plain per-frame path for comparison runs the same frames one process() at a time (batch 1,
-no graph) on one stream.
+no graph) on one stream: FP32 level storage, the drop-in form the speed-up is quoted against, and
+also with FP16 storage.
 """
 from __future__ import annotations
 
@@ -183,15 +184,16 @@ def autotune(job: Job, batches=(1, 2, 4, 8), tiles=(32, 64), reps: int = 3, use_
     return dict(result, cached=False)
 
 
-def plain_path(job: Job, keep_last: bool = False):
-    """Seconds for the job through the plain per-frame path: batch 1, no graph, one stream
-    (with keep_last, also each stream's last canvas)."""
+def plain_path(job: Job, keep_last: bool = False, storage: str | None = None):
+    """Seconds for the job through the plain per-frame path: batch 1, no graph, one stream, the
+    job's level storage unless `storage` is given (with keep_last, also each stream's last
+    canvas)."""
     import torch
 
     sts, cvs, cts = [], [], []
     for s in job.streams:
         cls = pano.CudaStitchPano if s["kind"] == 2 else pano.CudaStitchPano3
-        st = cls(1, job.levels, s["masks"], quiet=True, storage=job.storage)
+        st = cls(1, job.levels, s["masks"], quiet=True, storage=storage or job.storage)
         sts.append(st)
         cts.append(torch.empty((1, s["rig"].canvas_h, s["rig"].canvas_w, 4), dtype=torch.uint8, device=job.device))
         cvs.append(pano._image(cts[-1]))
@@ -228,10 +230,14 @@ def run(device, use_cache: bool = False) -> dict:
     t = tune["tile_down"]
     plan = Plan(job, tune["batch"], {int(k): v for k, v in t.items()} if isinstance(t, dict) else t)
     sec = plan.time(5)
-    plain_sec = plain_path(job)
+    plain_sec = plain_path(job, storage="f32")
+    plain16_sec = plain_path(job, storage="f16")
     frames = len(job.streams) * job.frames
     return {"workload": "4 x pano2_5120x2880_to_8500x3300 + 4 x pano3_2704x1520_to_6000x1800, 32 frames each, L=6",
             "storage": job.storage, "batch": tune["batch"], "tile_down": tune["tile_down"], "graph": True,
             "fps": round(frames / sec, 1), "mpix_s": round(job.mpix_total / sec, 1),
+            "plain_storage": "f32",
             "plain_fps": round(frames / plain_sec, 1), "plain_mpix_s": round(job.mpix_total / plain_sec, 1),
-            "speedup_vs_plain": round(plain_sec / sec, 3), "autotune": tune}
+            "speedup_vs_plain": round(plain_sec / sec, 3),
+            "plain_f16_fps": round(frames / plain16_sec, 1), "speedup_vs_plain_f16": round(plain16_sec / sec, 3),
+            "autotune": tune}

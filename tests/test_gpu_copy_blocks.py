@@ -22,11 +22,13 @@ pytestmark = pytest.mark.gpu
 
 CASES = [
     # (workload, kind, levels, scale, batch, minimize)
+    ("pano2_5120x2880_to_8500x3300", 2, 6, 0.5, 1, True),
     ("pano3_2704x1520_to_6000x1800", 3, 6, 0.5, 1, True),
     ("pano3_2704x1520_to_6000x1800", 3, 4, 0.25, 2, True),
     ("panon8_2000x1500_to_9000x2400", 1, 6, 0.5, 1, True),
     ("panon8_2000x1500_to_9000x2400", 1, 5, 0.25, 2, False),
     ("panon8_2000x1500_to_9000x2400", 1, 7, 0.5, 1, True),
+    ("pano2_1280x720_to_2200x800", 2, 5, 1.0, 2, True),
 ]
 
 
@@ -65,6 +67,17 @@ def test_copy_blocks_after_a_full_frame(oracle_lib, workload, kind, levels, scal
     _exact(gpu_stitch(st, fa), o.run(fa), "copy blocks on, second frame")
 
 
+def _copied_image(rig, kind, x, y):
+    """The image a copy block at canvas (x, y) copies: the label's; with two images image 2 where
+    the seam value is 0 and image 2's table covers the pixel, else image 1."""
+    label = int(rig.seam[y, x])
+    if kind != 2:
+        return label
+    h, w = rig.map_x[1].shape
+    covered = 0 <= x - rig.pos_x[1] < w and 0 <= y - rig.pos_y[1] < h
+    return 1 if label == 0 and covered else 0
+
+
 def _copy_and_pyramid_neighbours(st, rig, kind, levels):
     """Canvas pixels 5 columns right of a copy block's right edge that lie in a pyramid block
     (inside the copy block's reconstruction support), with the image of the copy block."""
@@ -78,7 +91,7 @@ def _copy_and_pyramid_neighbours(st, rig, kind, levels):
             continue
         x, y = ox + 64 * i + 64 + 5, oy + 16 * j + 3
         if x < rig.canvas_w and y < rig.canvas_h:
-            pts.append((x, y, int(rig.seam[y, x])))
+            pts.append((x, y, _copied_image(rig, kind, x, y)))
     return pts
 
 
@@ -96,7 +109,7 @@ def _zero_alpha_at(rig, frames, k, x, y, rgb_zero=False):
     return True
 
 
-@pytest.mark.parametrize("workload,kind,levels,scale,batch,minimize", CASES[:3])
+@pytest.mark.parametrize("workload,kind,levels,scale,batch,minimize", CASES[:4])
 def test_alpha_zero_runs_the_fallback(oracle_lib, workload, kind, levels, scale, batch, minimize):
     from hmpano import synth
 
