@@ -52,6 +52,9 @@ struct PyrArgs {
   uint32_t* P0[kDevMaxImages];
   int use_p0;
   int slots_cap;  // N-way pyr_down: shared memory holds this many slots (the most any tile has)
+  // pyr_down's dynamic shared memory is at least this many bytes (0: what it needs). Reserving
+  // more caps how many of its CTAs share an SM, which shapes how it packs beside the gather.
+  int down_smem_floor;
   int coarse_cap; // N-way pyr_coarse: likewise, per coarse tile
   int fine_cap;   // N-way pyr_fine: likewise, per 64 x 16 level-0 block (with its upsample halo)
   int pdl;        // launch pyr_coarse / pyr_fine as programmatic dependents of the kernel before them
@@ -142,6 +145,9 @@ cudaError_t launch_b5_pyramid(const PyrArgs& a, int rule, int storage, int batch
 int b5_launches(int levels);
 
 size_t pyr_down_smem(int n, int tile);
+// Dynamic shared memory per CTA that leaves room for at most `ctas_per_sm` CTAs on an SM of the
+// current device (1 KB of it reserved per CTA); 0 for no cap.
+size_t residency_smem(int ctas_per_sm);
 // Shared memory of a pyr_coarse CTA (levels 2..L-1 of its tile with halos).
 size_t pyr_coarse_smem(int n, int k, int tile1, int levels, int storage);
 

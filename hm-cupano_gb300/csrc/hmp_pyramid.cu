@@ -25,6 +25,8 @@
 // product is fused into a sum): downsample sums in (0,0),(1,0),(0,1),(1,1) order divided by the
 // count; alpha-aware bilinear taps in 00,10,01,11 order over taps with alpha != 0; blends as in
 // cudaBlend.cu:520-576, cudaBlend3.cu:376-531, cudaBlendN.cu:199-288.
+#include <algorithm>
+
 #include "hmp_blend.cuh"
 
 namespace hmp {
@@ -1259,6 +1261,7 @@ void set_coarse_attrs() {
 
 template <typename Store, int T>
 void down_dispatch(const PyrArgs& a, dim3 grid, size_t smem, cudaStream_t stream) {
+  smem = std::max(smem, size_t(a.down_smem_floor));
   if (a.n <= 2 && (a.tiles != nullptr || a.gate != nullptr))
     pyr_down_kernel<2, Store, T, true><<<grid, 256, smem, stream>>>(a);
   else if (a.n <= 2)
@@ -1266,7 +1269,8 @@ void down_dispatch(const PyrArgs& a, dim3 grid, size_t smem, cudaStream_t stream
   else if (a.n == 3)
     pyr_down_kernel<3, Store, T><<<grid, 256, smem, stream>>>(a);
   else if (a.slots_cap > 0)
-    pyr_down_n_kernel<Store, T><<<grid, 256, pyr_down_smem(a.slots_cap, T), stream>>>(a);
+    pyr_down_n_kernel<Store, T><<<grid, 256, std::max(pyr_down_smem(a.slots_cap, T), size_t(a.down_smem_floor)), stream>>>(
+        a);
   else
     pyr_down_kernel<8, Store, T><<<grid, 256, smem, stream>>>(a);
 }
@@ -1386,6 +1390,17 @@ __global__ void dump_recon_kernel(const float4* lo, int lw, int lh, const float4
 dim3 dump_grid(int w, int h, int batch) { return dim3((w + 255) / 256, h, batch); }
 
 }  // namespace
+
+size_t residency_smem(int ctas_per_sm) {
+  if (ctas_per_sm <= 0) return 0;
+  int dev = 0, per_sm = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev) != cudaSuccess)
+    per_sm = 228 * 1024;
+  // One CTA more than the cap must not fit: (cap + 1) * (s + 1 KB) > per_sm, s in 128-byte units.
+  const size_t s = (size_t(per_sm) / size_t(ctas_per_sm + 1) + 128) / 128 * 128 - 1024;
+  return std::min<size_t>(s, 227 * 1024);
+}
 
 size_t pyr_down_smem(int n, int tile) {
   const int t2 = tile / 4;

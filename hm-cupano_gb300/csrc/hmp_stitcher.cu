@@ -119,6 +119,7 @@ struct hmp_stitcher {
   const uint8_t* mask0 = nullptr;
   int mask0_pitch = 0;
   int tile_down = 0, tile_coarse = 0;
+  int down_residency = 0;  // pyr_down CTAs per SM, capped through its shared memory (0: no cap)
   int down_cap = 0;  // N-way pyr_down: slots held in shared memory (the most any tile overlaps)
   int coarse_cap = 0;  // N-way pyr_coarse: likewise per coarse tile
   int fine_cap = 0;    // N-way pyr_fine: likewise per 64 x 16 level-0 block and its upsample halo
@@ -606,16 +607,12 @@ struct hmp_stitcher {
           v->push_back(static_cast<float4*>(q));
         }
     }
-    hmp::PyrArgs a{};
-    a.S = last_src;
-    for (int k = 0; k < p.n; ++k) a.slot[k] = slot_planes[k];
-    a.n = p.n;
-    a.levels = L;
-    for (int l = 0; l < L; ++l) {
-      a.lw[l] = p.lw[l];
-      a.lh[l] = p.lh[l];
+    hmp::PyrArgs a = pyr_args(last_src, hmp::CanvasDev{});
+    if (copy_plan && L > 1) {
+      // Copy-block mode computes the Gaussian levels only where the pyramid runs: all of them here.
+      const dim3 dgrid((p.lw[0] + tile_down - 1) / tile_down, (p.lh[0] + tile_down - 1) / tile_down, B);
+      e = hmp::launch_pyr_down(a, p.storage, dgrid, s);
     }
-    a.opaque = p.slot_opaque ? 1 : 0;
     for (int k = 0; k < 2 && e == cudaSuccess; ++k) {
       e = hmp::launch_dump_level0(a, k, g[k][0], B, s);
       for (int l = 1; l < L && e == cudaSuccess; ++l)
@@ -728,6 +725,43 @@ struct hmp_stitcher {
     tnext = 0;
     std::fill(tused.begin(), tused.end(), 0);
     return cudaSuccess;
+  }
+
+  // Parameters of the pyramid kernels for frames S and canvas C (dense grids; no work lists).
+  hmp::PyrArgs pyr_args(const hmp::SrcSet& S, const hmp::CanvasDev& C) const {
+    const hmp::Plan& p = plan;
+    hmp::PyrArgs a{};
+    a.S = S;
+    for (int k = 0; k < p.n; ++k) a.slot[k] = slot_planes[k];
+    a.n = p.n;
+    a.levels = p.levels;
+    for (int l = 0; l < p.levels; ++l) {
+      a.lw[l] = p.lw[l];
+      a.lh[l] = p.lh[l];
+      a.maskL[l] = maskL[l];
+      a.hotL[l] = hotL[l];
+      for (int k = 0; k < p.n; ++k) a.G[k][l] = G[k][l];
+    }
+    a.mask0 = mask0;
+    a.mask0_pitch = mask0_pitch;
+    a.K = p.mask_k;
+    a.opaque = p.slot_opaque ? 1 : 0;
+    a.C = C;
+    a.wx0 = p.write.x - p.blend.x;
+    a.wy0 = p.write.y - p.blend.y;
+    a.wx1 = a.wx0 + p.write.w;
+    a.wy1 = a.wy0 + p.write.h;
+    a.cx_off = p.blend.x;
+    a.cy_off = p.blend.y;
+    a.use_p0 = use_p0 ? 1 : 0;
+    a.fine_cap = fine_cap;
+    a.pdl = p.levels > 1 && !b5 ? 1 : 0;  // pyr_coarse follows pyr_down, pyr_fine pyr_coarse
+    for (int k = 0; k < p.n; ++k) a.P0[k] = P0[k];
+    a.slots_cap = down_cap;
+    a.coarse_cap = coarse_cap;
+    a.tile = tile_down;
+    a.down_smem_floor = int(hmp::residency_smem(down_residency));
+    return a;
   }
 
   hmp::SrcSet sources(const hmp_image* inputs) const {
@@ -918,33 +952,7 @@ struct hmp_stitcher {
       }
       return cuda_status(err, what);
     };
-    hmp::PyrArgs a{};
-    a.S = S;
-    for (int k = 0; k < p.n; ++k) a.slot[k] = slot_planes[k];
-    a.n = p.n;
-    a.levels = p.levels;
-    for (int l = 0; l < p.levels; ++l) {
-      a.lw[l] = p.lw[l];
-      a.lh[l] = p.lh[l];
-      a.maskL[l] = maskL[l];
-      a.hotL[l] = hotL[l];
-      for (int k = 0; k < p.n; ++k) a.G[k][l] = G[k][l];
-    }
-    a.mask0 = mask0;
-    a.mask0_pitch = mask0_pitch;
-    a.K = p.mask_k;
-    a.opaque = p.slot_opaque ? 1 : 0;
-    a.C = C;
-    a.wx0 = p.write.x - p.blend.x;
-    a.wy0 = p.write.y - p.blend.y;
-    a.wx1 = a.wx0 + p.write.w;
-    a.wy1 = a.wy0 + p.write.h;
-    a.cx_off = p.blend.x;
-    a.cy_off = p.blend.y;
-    a.use_p0 = use_p0 ? 1 : 0;
-    a.fine_cap = fine_cap;
-    a.pdl = p.levels > 1 && !b5 ? 1 : 0;  // pyr_coarse follows pyr_down, pyr_fine pyr_coarse
-    for (int k = 0; k < p.n; ++k) a.P0[k] = P0[k];
+    hmp::PyrArgs a = pyr_args(S, C);
     if (b5) {
       // Binomial5: the level-by-level chain (its time is reported under pyr_down).
       for (int l = 1; l < p.levels; ++l) a.Rl[l] = Rl[l];
@@ -969,8 +977,6 @@ struct hmp_stitcher {
     }
     const int fx0 = a.wx0 & ~1, fy0 = a.wy0 & ~1;
     const dim3 fgrid((a.wx1 - fx0 + 63) / 64, (a.wy1 - fy0 + 15) / 16, p.batch);
-    a.slots_cap = down_cap;
-    a.coarse_cap = coarse_cap;
     // The pyramid chain: dense, or (copy-block mode) over the work lists.
     const auto chain = [&](const hmp::PyrArgs& base, bool listed, cudaStream_t cs, bool timed) -> hmp_status {
       hmp::PyrArgs q = base;
@@ -1107,6 +1113,14 @@ HMP_API hmp_status hmp_stitcher_get_info(const hmp_stitcher* st, hmp_stitcher_in
   info->pyramid_tiles[1] = st->n_coarse;
   info->pyramid_tiles[2] = st->n_fine;
   return st->status;
+}
+
+HMP_API hmp_status hmp_stitcher_set_down_residency(hmp_stitcher* st, int ctas_per_sm) {
+  if (!st) return make_status(HMP_ERR_INVALID_VALUE, "stitcher is null");
+  if (st->status.code != HMP_OK) return st->status;
+  if (ctas_per_sm < 0 || ctas_per_sm > 8) return make_status(HMP_ERR_INVALID_VALUE, "ctas_per_sm must be in 0..8");
+  st->down_residency = ctas_per_sm;
+  return ok_status();
 }
 
 HMP_API hmp_status hmp_stitcher_set_copy_blocks(hmp_stitcher* st, int enable) {

@@ -516,6 +516,12 @@ class _Stitcher:
         if not s.ok():
             raise CudaStatusError(s)
 
+    def set_down_residency(self, ctas_per_sm: int) -> None:
+        """Caps the Gaussian-pyramid kernel at ctas_per_sm CTAs per SM (0 = no cap); tuning only."""
+        s = _status(_lib.lib().hmp_stitcher_set_down_residency(self._handle, int(ctas_per_sm)))
+        if not s.ok():
+            raise CudaStatusError(s)
+
     def set_copy_blocks(self, enable: bool) -> None:
         """Copy blocks on (default) or off (tuning and tests only: both give the same bits)."""
         s = _status(_lib.lib().hmp_stitcher_set_copy_blocks(self._handle, 1 if enable else 0))

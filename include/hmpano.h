@@ -237,6 +237,12 @@ typedef struct hmp_kernel_timing {
   long long launches[4];
 } hmp_kernel_timing;
 
+/* Caps the Gaussian-pyramid kernel at ctas_per_sm CTAs per SM (0 = no cap) by reserving shared
+ * memory for it. Tuning only (every setting gives the same bits): with the pyramid running beside
+ * the canvas gather, how its few CTAs spread over the SMs changes the frame time. No counterpart in
+ * the reference. */
+HMP_API hmp_status hmp_stitcher_set_down_residency(hmp_stitcher* st, int ctas_per_sm);
+
 /* Copy blocks: on (1, the default) or off (0). No counterpart in the reference.
  * Three-image and N-image blend regions cover most of the canvas, but wherever the seam mask is
  * one image's at every level of a pixel's reconstruction and that image is valid there, the
