@@ -264,6 +264,13 @@ struct hmp_stitcher {
     return best;
   }
 
+  // Default cap on pyr_down's CTAs per SM. Two images, 64-pixel tiles: 4. Its 40 KB of shared
+  // memory and ~48 registers would let five share an SM, and five measured slower beside the
+  // canvas gather (8500x3300 at L=6: 0.103 -> 0.090 ms per frame with the cap; three would do as
+  // well, two is slower); packed five to an SM the one-wave kernel bunches onto fewer SMs. Other
+  // configurations are held to three or fewer by their shared memory already.
+  int default_residency() const { return plan.n == 2 && tile_down == 64 ? 4 : 0; }
+
   // pyr_coarse's shared memory: the N-way kernel holds `coarse_cap` slots and no mask values.
   size_t coarse_smem_for(int t1) const {
     const hmp::Plan& p = plan;
@@ -395,6 +402,7 @@ struct hmp_stitcher {
         }
       }
       tile_coarse = std::max(32, align / 2);
+      down_residency = default_residency();
       coarse_cap = (n > 3 && L > 2) ? coarse_cap_for(tile_coarse) : 0;
       coarse_smem = coarse_smem_for(tile_coarse);
       b5 = p.filter == HMP_FILTER_BINOMIAL5 && L > 1;
@@ -1153,6 +1161,7 @@ HMP_API hmp_status hmp_stitcher_set_tiles(hmp_stitcher* st, int tile_down, int t
   if (hmp::pyr_down_smem(cap > 0 ? cap : p.n, tile_down) > 227 * 1024)
     return make_status(HMP_ERR_NOT_SUPPORTED, "pyramid tile does not fit in shared memory");
   st->tile_down = tile_down;
+  st->down_residency = st->default_residency();
   st->down_cap = cap;
   st->tile_coarse = tile_coarse;
   st->coarse_smem = st->coarse_smem_for(tile_coarse);

@@ -75,7 +75,8 @@ class Plan:
 
     def __init__(self, job: Job, batch: int, tile_down):
         """tile_down: one pyramid down-tile edge for every stream, or {kind: edge} per stream kind
-        (2 = two-image, 3 = three-image)."""
+        (2 = two-image, 3 = three-image); an edge may be an (edge, CTAs per SM) pair, which also
+        caps the down kernel's residency (hmp_stitcher_set_down_residency)."""
         import torch
 
         if job.frames % batch:
@@ -87,7 +88,7 @@ class Plan:
             st = cls(batch, job.levels, s["masks"], quiet=True, storage=job.storage)
             if not st.status.ok():
                 raise pano.CudaStatusError(st.status)
-            st.set_tiles(self.tile_for(s["kind"]))
+            self._apply(st, s["kind"])
             self.sts.append(st)
             h, w = s["rig"].canvas_h, s["rig"].canvas_w
             self.canvases.append([torch.empty((batch, h, w, 4), dtype=torch.uint8, device=job.device) for _ in range(2)])
@@ -95,7 +96,14 @@ class Plan:
         self.graph = None
         self.rebuild()
 
-    def tile_for(self, kind: int) -> int:
+    def _apply(self, st, kind: int) -> None:
+        spec = self.tile_for(kind)
+        tile, res = (spec, None) if isinstance(spec, int) else (int(spec[0]), int(spec[1]))
+        st.set_tiles(tile)
+        if res is not None:
+            st.set_down_residency(res)
+
+    def tile_for(self, kind: int):
         t = self.tile_down
         return int(t[kind] if isinstance(t, dict) else t)
 
@@ -103,7 +111,7 @@ class Plan:
         """New tiles (one edge, or {kind: edge}); the graph is rebuilt."""
         self.tile_down = tile_down
         for st, s in zip(self.sts, self.job.streams):
-            st.set_tiles(self.tile_for(s["kind"]))
+            self._apply(st, s["kind"])
         self.rebuild()
 
     def rebuild(self) -> None:
@@ -144,9 +152,11 @@ class Plan:
         return [c[last % 2][-1] for c in self.canvases]
 
 
-def autotune(job: Job, batches=(1, 2, 4, 8), tiles=(32, 64), reps: int = 3, use_cache: bool = True) -> dict:
+def autotune(job: Job, batches=(1, 2, 4, 8), tiles=(32, 64), residencies=(0, 4), reps: int = 3,
+             use_cache: bool = True) -> dict:
     """Time every frames-per-call candidate with every pyramid down-tile edge per stream kind
-    (two-image and three-image streams choose theirs separately); keep and cache the fastest."""
+    (two-image and three-image streams choose theirs separately; two-image streams with 64-pixel
+    tiles also try each cap on the down kernel's CTAs per SM); keep and cache the fastest."""
     key = job.signature()
     cache = {}
     if use_cache and CACHE.exists():
@@ -157,7 +167,15 @@ def autotune(job: Job, batches=(1, 2, 4, 8), tiles=(32, 64), reps: int = 3, use_
     if use_cache and key in cache:
         return dict(cache[key], cached=True)
     kinds = sorted({s["kind"] for s in job.streams})
-    combos = [dict(zip(kinds, c)) for c in itertools.product(tiles, repeat=len(kinds))]
+
+    def options(kind):
+        out = []
+        for tile in tiles:
+            for res in (residencies if kind == 2 and tile == 64 else (0,)):
+                out.append((tile, res))
+        return out
+
+    combos = [dict(zip(kinds, c)) for c in itertools.product(*[options(k) for k in kinds])]
     trials = []
     t0 = time.perf_counter()
     for b in batches:
@@ -168,7 +186,7 @@ def autotune(job: Job, batches=(1, 2, 4, 8), tiles=(32, 64), reps: int = 3, use_
             else:
                 plan.set_tiles(combo)
             sec = plan.time(reps)
-            trials.append({"batch": b, "tile_down": {str(k): v for k, v in combo.items()},
+            trials.append({"batch": b, "tile_down": {str(k): list(v) for k, v in combo.items()},
                            "fps": round(len(job.streams) * job.frames / sec, 1)})
         del plan
     best = max(trials, key=lambda t: t["fps"])

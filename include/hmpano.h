@@ -239,8 +239,9 @@ typedef struct hmp_kernel_timing {
 
 /* Caps the Gaussian-pyramid kernel at ctas_per_sm CTAs per SM (0 = no cap) by reserving shared
  * memory for it. Tuning only (every setting gives the same bits): with the pyramid running beside
- * the canvas gather, how its few CTAs spread over the SMs changes the frame time. No counterpart in
- * the reference. */
+ * the canvas gather, how its few CTAs spread over the SMs changes the frame time. The default is 4
+ * for two-image stitchers with 64-pixel down tiles, else 0; hmp_stitcher_set_tiles restores it.
+ * No counterpart in the reference. */
 HMP_API hmp_status hmp_stitcher_set_down_residency(hmp_stitcher* st, int ctas_per_sm);
 
 /* Copy blocks: on (1, the default) or off (0). No counterpart in the reference.
