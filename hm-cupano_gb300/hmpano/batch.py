@@ -105,7 +105,8 @@ class Plan:
 
     def tile_for(self, kind: int):
         t = self.tile_down
-        return int(t[kind] if isinstance(t, dict) else t)
+        v = t[kind] if isinstance(t, dict) else t
+        return int(v) if isinstance(v, (int, float, str)) else (int(v[0]), int(v[1]))
 
     def set_tiles(self, tile_down) -> None:
         """New tiles (one edge, or {kind: edge}); the graph is rebuilt."""
