@@ -13,6 +13,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <climits>
 #include <cstdio>
 #include <cstring>
@@ -43,6 +44,18 @@ hmp_status cuda_status(cudaError_t e, const char* what) {
 }
 
 inline int round_up(int v, int a) { return (v + a - 1) / a * a; }
+
+// Allocation-failure injection for tests (hmp_debug_fail_allocation): the device allocation that
+// brings this countdown from 1 to 0 fails without allocating. Also the count of allocations made.
+std::atomic<long long> g_alloc_fail_countdown{0};
+std::atomic<long long> g_alloc_count{0};
+
+bool injected_allocation_failure() {
+  long long v = g_alloc_fail_countdown.load();
+  while (v > 0)
+    if (g_alloc_fail_countdown.compare_exchange_weak(v, v - 1)) return v == 1;
+  return false;
+}
 
 // Little-endian baseline TIFF of float32 samples, uncompressed, one strip: ch = 1 (grey) or 4
 // (RGBA, unassociated alpha), rows top to bottom, `px` holding ch floats per pixel.
@@ -173,6 +186,11 @@ struct hmp_stitcher {
   }
 
   cudaError_t alloc(void** p, size_t bytes) {
+    ++g_alloc_count;
+    if (injected_allocation_failure()) {
+      *p = nullptr;
+      return cudaErrorMemoryAllocation;
+    }
     cudaError_t e = cudaMalloc(p, bytes);
     if (e == cudaSuccess) {
       allocations.push_back(*p);
@@ -1072,6 +1090,7 @@ HMP_API hmp_status hmp_stitcher_create(const hmp_config* cfg, hmp_stitcher** out
     // Release device memory now; keep the object for its sticky status.
     for (void* p : st->allocations) cudaFree(p);
     st->allocations.clear();
+    st->device_bytes = 0;
   }
   if (out)
     *out = st;
@@ -1084,6 +1103,10 @@ HMP_API hmp_status hmp_stitcher_create(const hmp_config* cfg, hmp_stitcher** out
 }
 
 HMP_API void hmp_stitcher_destroy(hmp_stitcher* st) { delete st; }
+
+HMP_API void hmp_debug_fail_allocation(long long k) { g_alloc_fail_countdown.store(k > 0 ? k : 0); }
+
+HMP_API long long hmp_debug_allocation_count(void) { return g_alloc_count.load(); }
 
 HMP_API hmp_status hmp_stitcher_status(const hmp_stitcher* st) {
   if (!st) return make_status(HMP_ERR_INVALID_VALUE, "stitcher is null");

@@ -197,6 +197,14 @@ HMP_API const char* hmp_version(void);
  * hmp_stitcher_destroy. */
 HMP_API hmp_status hmp_stitcher_create(const hmp_config* cfg, hmp_stitcher** out);
 
+/* For tests of the construction-error path (no counterpart in the reference, whose construct
+ * errors come from cudaMalloc itself, src/pano/cudaPano.inl:28-31): the k-th device allocation a
+ * stitcher makes from now on (any stitcher of the process, counting from 1) fails with
+ * HMP_ERR_MEMORY_ALLOCATION without allocating; 0 switches it off. hmp_debug_allocation_count()
+ * returns how many device allocations stitchers have made so far (injected failures included). */
+HMP_API void hmp_debug_fail_allocation(long long k);
+HMP_API long long hmp_debug_allocation_count(void);
+
 HMP_API void hmp_stitcher_destroy(hmp_stitcher* st);
 
 /* Sticky status (construction error or the first failed process()). */

@@ -231,6 +231,13 @@ def test_c_abi_rejects_bad_arguments_before_any_device_work(lib):
     d = C.POINTER(_lib.ControlDir)()
     assert lib.hmp_control_dir_load(b"/nonexistent", 99, 2, C.byref(d)).code == 1 and not d
 
+    # The allocation-failure hook is host state only: set, read back through the counter, cleared.
+    n = lib.hmp_debug_allocation_count()
+    assert n >= 0
+    lib.hmp_debug_fail_allocation(3)
+    lib.hmp_debug_fail_allocation(0)
+    assert lib.hmp_debug_allocation_count() == n
+
 
 def test_noalloc_blend_rejects_bad_arguments_before_any_device_work(lib):
     """hmp_blend2_noalloc checks every argument before its first CUDA call, so fake non-null
