@@ -592,9 +592,9 @@ struct hmp_stitcher {
     if (!directory) return make_status(HMP_ERR_INVALID_VALUE, "directory is null");
     if (p.levels == 0)
       return make_status(HMP_ERR_INVALID_VALUE, "Soft-blend pyramid is only available when num_levels > 0");
-    if (p.rule != hmp::kRuleTwo || b5 || generic)
+    if (p.rule != hmp::kRuleTwo || b5 || (generic && p.channels != 4))
       return make_status(HMP_ERR_NOT_SUPPORTED,
-                         "the pyramid dump covers the two-image RGBA8 stitcher with the box filter");
+                         "the pyramid dump covers two-image stitchers of RGBA pixels with the box filter");
     if (!have_last) return make_status(HMP_ERR_INVALID_VALUE, "No Laplacian workspace is populated yet: call process() first");
     int dev = -1;
     cudaGetDevice(&dev);
@@ -640,9 +640,16 @@ struct hmp_stitcher {
       e = hmp::launch_pyr_down(a, p.storage, dgrid, s);
     }
     for (int k = 0; k < 2 && e == cudaSuccess; ++k) {
-      e = hmp::launch_dump_level0(a, k, g[k][0], B, s);
-      for (int l = 1; l < L && e == cudaSuccess; ++l)
-        e = hmp::launch_dump_widen(G[k][l], p.storage, (long long)B * p.lw[l] * p.lh[l], g[k][l], s);
+      if (generic) {
+        // float4 pixels: the level-by-level kernels keep every Gaussian level, level 0 included.
+        e = cudaMemcpyAsync(g[k][0], G0[k], level_bytes(0), cudaMemcpyDeviceToDevice, s);
+        for (int l = 1; l < L && e == cudaSuccess; ++l)
+          e = cudaMemcpyAsync(g[k][l], G[k][l], level_bytes(l), cudaMemcpyDeviceToDevice, s);
+      } else {
+        e = hmp::launch_dump_level0(a, k, g[k][0], B, s);
+        for (int l = 1; l < L && e == cudaSuccess; ++l)
+          e = hmp::launch_dump_widen(G[k][l], p.storage, (long long)B * p.lw[l] * p.lh[l], g[k][l], s);
+      }
       for (int l = 0; l + 1 < L && e == cudaSuccess; ++l)
         e = hmp::launch_dump_lap(g[k][l], p.lw[l], p.lh[l], g[k][l + 1], p.lw[l + 1], p.lh[l + 1], lap[k][l], B, s);
       if (e == cudaSuccess)  // the coarsest Laplacian is the Gaussian itself
@@ -1103,6 +1110,22 @@ HMP_API hmp_status hmp_stitcher_create(const hmp_config* cfg, hmp_stitcher** out
 }
 
 HMP_API void hmp_stitcher_destroy(hmp_stitcher* st) { delete st; }
+
+HMP_API hmp_status hmp_laplacian_rgba(const float* high, int high_w, int high_h, const float* low, int low_w,
+                                      int low_h, float* out, int batch, void* stream) {
+  if (!high || !low || !out) return make_status(HMP_ERR_INVALID_VALUE, "null argument");
+  if (high_w <= 0 || high_h <= 0 || low_w <= 0 || low_h <= 0 || batch <= 0 || high_w > (1 << 20) ||
+      high_h > (1 << 20) || low_w > high_w || low_h > high_h || batch > 65536)
+    return make_status(HMP_ERR_INVALID_VALUE, "invalid level sizes or batch");
+  if (reinterpret_cast<uintptr_t>(high) % 16 || reinterpret_cast<uintptr_t>(low) % 16 ||
+      reinterpret_cast<uintptr_t>(out) % 16)
+    return make_status(HMP_ERR_INVALID_VALUE, "levels must be 16-byte aligned float RGBA");
+  const cudaError_t e = hmp::launch_dump_lap(reinterpret_cast<const float4*>(high), high_w, high_h,
+                                             reinterpret_cast<const float4*>(low), low_w, low_h,
+                                             reinterpret_cast<float4*>(out), batch, static_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) return cuda_status(e, "laplacian launch");
+  return ok_status();
+}
 
 HMP_API void hmp_debug_fail_allocation(long long k) { g_alloc_fail_countdown.store(k > 0 ? k : 0); }
 

@@ -141,6 +141,8 @@ SIGNATURES = {
     "hmp_stitcher_set_timing": ([C.c_void_p, C.c_int], Status),
     "hmp_stitcher_set_tiles": ([C.c_void_p, C.c_int, C.c_int], Status),
     "hmp_stitcher_set_copy_blocks": ([C.c_void_p, C.c_int], Status),
+    "hmp_laplacian_rgba": ([C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_int,
+                            C.c_void_p], Status),
     "hmp_debug_fail_allocation": ([C.c_longlong], None),
     "hmp_debug_allocation_count": ([], C.c_longlong),
     "hmp_stitcher_set_down_residency": ([C.c_void_p, C.c_int], Status),

@@ -586,6 +586,7 @@ class _Stitcher:
         status = _status(s)
         if not status.ok():
             raise CudaStatusError(status)
+        self._last_handle = handle  # the dump reads the stitcher of the last call's pixel type
         return canvas
 
 
@@ -621,8 +622,9 @@ class CudaStitchPano(_Stitcher):
         """Write the soft-blend pyramid of the last process() under `directory`
         (cupano/pano.py:466-551, src/pano/cudaPano.inl:420-458): metadata.txt and float32 TIFF
         files gauss1 / gauss2 / lap1 / lap2 / blend / reconstruct `level_<l>_batch_<b>.tiff` and
-        mask `level_<l>.tiff`. The last call's input tensors must still hold their frames.
-        `device` and `channels` are accepted for the reference's signature (one device, RGBA)."""
+        mask `level_<l>.tiff`, for the pixel type of the last process() (RGBA: uint8 or float).
+        The last call's input tensors must still hold their frames. `device` and `channels` are
+        accepted for the reference's signature (one device, RGBA)."""
         import torch
 
         del device, channels
@@ -630,7 +632,8 @@ class CudaStitchPano(_Stitcher):
             stream = torch.cuda.current_stream().cuda_stream
         elif hasattr(stream, "cuda_stream"):
             stream = stream.cuda_stream
-        s = _status(_lib.lib().hmp_stitcher_dump_pyramid(self._handle, str(directory).encode(), C.c_void_p(stream)))
+        handle = getattr(self, "_last_handle", None) or self._handle
+        s = _status(_lib.lib().hmp_stitcher_dump_pyramid(handle, str(directory).encode(), C.c_void_p(stream)))
         if not s.ok():
             raise CudaStatusError(s)
 

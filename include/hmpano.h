@@ -197,6 +197,13 @@ HMP_API const char* hmp_version(void);
  * hmp_stitcher_destroy. */
 HMP_API hmp_status hmp_stitcher_create(const hmp_config* cfg, hmp_stitcher** out);
 
+/* Alpha-aware Laplacian of one pyramid level, as the stitchers form it: out = high minus the
+ * bilinear upsample of low over its taps with alpha != 0 (renormalised), in colour, and high's
+ * alpha (cupano/ops.py compute_laplacian; src/cuda/cudaBlend.cu:356-456). Float RGBA levels on the
+ * device, [batch][h][w][4], 16-byte aligned; low is the next level (at most high's size). */
+HMP_API hmp_status hmp_laplacian_rgba(const float* high, int high_w, int high_h, const float* low, int low_w,
+                                      int low_h, float* out, int batch, void* stream);
+
 /* For tests of the construction-error path (no counterpart in the reference, whose construct
  * errors come from cudaMalloc itself, src/pano/cudaPano.inl:28-31): the k-th device allocation a
  * stitcher makes from now on (any stitcher of the process, counting from 1) fails with
