@@ -475,7 +475,8 @@ def main() -> None:
     canvas_px = W * H
     # 4 table bytes once per call (the entry carries the owner), 4 source + 4 canvas bytes per
     # frame of the batch.
-    gather_px = (canvas_px - wr[2] * wr[3]) if info["levels"] else canvas_px
+    # Canvas pixels the gather writes: outside the write rect, plus the copy blocks inside it.
+    gather_px = info["gather_pixels"]
     gather_bytes = gather_px * (4.0 + 8.0 * B)
     dom_bytes = {"canvas_gather": gather_bytes}.get(dom)
     achieved = dom_bytes / (per_launch_ms / 1e3) / 1e9 if dom_bytes else None
@@ -526,8 +527,9 @@ def main() -> None:
         "kernel_ms": {k: round(v[0] / max(v[1], 1), 5) for k, v in ktimes.items()},
         "kernel_ms_serialized": {k: round(v[0] / max(v[1], 1), 5) for k, v in ktimes_serial.items()},
         # Kernels launched in the headline timed region (every rank): each process() launches
-        # exactly launches_per_process of this library's kernels (4 here: pyr_down, pyr_coarse,
-        # pyr_fine, canvas_gather), counted per kernel by the instrumented pass.
+        # exactly launches_per_process of this library's kernels (here 8: the copy-block flag
+        # reset, pyr_down, pyr_coarse, pyr_fine over their work lists, canvas_gather, and the three
+        # gated fallbacks, which return at once unless a copy block's source alpha was 0).
         "gpu_launches": world * args.steps * int(info["launches_per_process"]),
         "e2e": e2e,
         "clocks": dict(sampler.summary(), window_s=round(t_region1 - t_region0, 3),

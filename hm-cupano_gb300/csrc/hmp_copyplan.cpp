@@ -127,6 +127,7 @@ void plan_copy_blocks(const Plan& p, int td, int t1, CopyPlan& cp) {
         cls = kBlockEmpty;
       } else {
         ++cp.pyramid_blocks;
+        cp.pyramid_pixels += (long long)(x1 - x0) * (y1 - y0);
         cp.pyramid_block[size_t(j) * cp.nfx + i] = 1;
         cp.fine_list.push_back(uint32_t(i) | (uint32_t(j) << 16));
       }

@@ -57,6 +57,7 @@ struct CopyPlan {
   int support_pitch = 0, support_shift = 0;
   uint32_t need_w[kMaxImages] = {}, need_h[kMaxImages] = {};  // frame size the copy blocks' entries need
   int copy_blocks = 0, empty_blocks = 0, pyramid_blocks = 0;
+  long long pyramid_pixels = 0;  // write-rect pixels of the pyramid blocks
   long long dense_down = 0, dense_coarse = 0;  // tiles of the dense grids, for reports
 };
 

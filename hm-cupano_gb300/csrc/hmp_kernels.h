@@ -130,6 +130,8 @@ cudaError_t launch_resolve_plane(const PlaneDev& raw, uint32_t* res, uint8_t* se
 
 // copy_blocks: the plane holds copy-block skips (kOffSkip) or the call checks source alpha.
 cudaError_t launch_canvas_gather(const GatherArgs& a, bool copy_blocks, cudaStream_t stream);
+// Copy-block mode: zeroes the alpha flag (one thread).
+cudaError_t launch_flag_reset(int* flag, cudaStream_t stream);
 
 // Gaussian levels 1..L-1 of every slot; grid = tiles over the blend region x batch.
 cudaError_t launch_pyr_down(const PyrArgs& a, int storage, dim3 grid, cudaStream_t stream);

@@ -157,6 +157,7 @@ struct hmp_stitcher {
   hmp::SkipMap skip{};
   uint32_t need_w[hmp::kDevMaxImages]{}, need_h[hmp::kDevMaxImages]{};
   int copy_blocks = 0, empty_blocks = 0, pyramid_blocks = 0;
+  long long pyramid_pixels = 0;
   cudaStream_t aux = nullptr;
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   double m0_bytes = 0;
@@ -552,14 +553,15 @@ struct hmp_stitcher {
     copy_blocks = c.copy_blocks;
     empty_blocks = c.empty_blocks;
     pyramid_blocks = c.pyramid_blocks;
+    pyramid_pixels = c.pyramid_pixels;
     copy_plan = true;
     return ok_status();
   }
 
-  // Kernels one process() launches in copy-block mode: the listed pyramid kernels, the gather and
-  // the three gated fallbacks.
+  // Kernels one process() launches in copy-block mode: the flag reset, the listed pyramid kernels,
+  // the gather and the three gated fallbacks.
   int copy_launches() const {
-    return (n_down[tile_down == 64 ? 1 : 0] > 0) + (n_coarse > 0) + (n_fine > 0) + 1 + 3;
+    return 1 + (n_down[tile_down == 64 ? 1 : 0] > 0) + (n_coarse > 0) + (n_fine > 0) + 1 + 3;
   }
 
   // Compulsory bytes per process(): outside the write rect, 4 (table) + 1 (seam) + a source and
@@ -963,7 +965,7 @@ struct hmp_stitcher {
       return ok_status();
     }
     if (copy) {
-      e = cudaMemsetAsync(alpha_flag, 0, sizeof(int), s);
+      e = hmp::launch_flag_reset(alpha_flag, s);
       if (e != cudaSuccess) return cuda_status(e, "copy-block flag reset");
     }
     // Fork: the pyramid goes to the high-priority stream `aux` when the canvas gather also
@@ -1166,6 +1168,15 @@ HMP_API hmp_status hmp_stitcher_get_info(const hmp_stitcher* st, hmp_stitcher_in
   info->pyramid_tiles[0] = st->n_down[st->tile_down == 64 ? 1 : 0];
   info->pyramid_tiles[1] = st->n_coarse;
   info->pyramid_tiles[2] = st->n_fine;
+  const double canvas_px = double(p.canvas_w) * p.canvas_h;
+  if (!p.canvas_plane_used)
+    info->gather_pixels = 0;
+  else if (p.levels == 0)
+    info->gather_pixels = canvas_px;
+  else if (copy)
+    info->gather_pixels = canvas_px - double(st->pyramid_pixels);
+  else
+    info->gather_pixels = canvas_px - double(p.write.w) * p.write.h;
   return st->status;
 }
 

@@ -80,6 +80,7 @@ class StitcherInfo(C.Structure):
         ("empty_blocks", C.c_int),
         ("pyramid_blocks", C.c_int),
         ("pyramid_tiles", C.c_int * 3),
+        ("gather_pixels", C.c_double),
     ]
 
 

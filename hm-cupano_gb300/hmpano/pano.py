@@ -508,6 +508,7 @@ class _Stitcher:
             "empty_blocks": inf.empty_blocks,
             "pyramid_blocks": inf.pyramid_blocks,
             "pyramid_tiles": tuple(inf.pyramid_tiles),
+            "gather_pixels": inf.gather_pixels,
         }
 
     def set_tiles(self, tile_down: int, tile_coarse: int = 32) -> None:

@@ -152,6 +152,7 @@ typedef struct hmp_stitcher_info {
   int empty_blocks;
   int pyramid_blocks;
   int pyramid_tiles[3];
+  double gather_pixels; /* canvas pixels the canvas gather writes per frame */
 } hmp_stitcher_info;
 
 /* ---- Control directory (host only; no GPU needed) ----
