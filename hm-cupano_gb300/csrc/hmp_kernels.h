@@ -68,8 +68,10 @@ struct PyrArgs {
   const uint8_t* support_mark;
   int sm_pitch, sm_shift;
   // Fallback launches: every CTA returns at once unless *gate != 0 (a copy block's source pixels
-  // held alpha 0, so the whole write rect is recomputed). nullptr: always run.
+  // held alpha 0, so the whole write rect is recomputed); then the launch's CTAs walk the dense
+  // grid of fb_nx x fb_ny tiles of fb_batch frames with a grid stride. nullptr: no gate.
   const int* gate;
+  int fb_nx, fb_ny, fb_batch;
   CanvasDev C;
   int wx0, wy0, wx1, wy1;  // write rect, blend coordinates, end exclusive
   int cx_off, cy_off;      // canvas = blend + offset

@@ -133,6 +133,7 @@ struct hmp_stitcher {
   int mask0_pitch = 0;
   int tile_down = 0, tile_coarse = 0;
   int down_residency = 0;  // pyr_down CTAs per SM, capped through its shared memory (0: no cap)
+  long long fallback_ctas = 608;  // CTAs of a gated fallback launch: four per SM
   int down_cap = 0;  // N-way pyr_down: slots held in shared memory (the most any tile overlaps)
   int coarse_cap = 0;  // N-way pyr_coarse: likewise per coarse tile
   int fine_cap = 0;    // N-way pyr_fine: likewise per 64 x 16 level-0 block and its upsample halo
@@ -422,6 +423,11 @@ struct hmp_stitcher {
       }
       tile_coarse = std::max(32, align / 2);
       down_residency = default_residency();
+      {
+        int sms = 0;
+        if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) == cudaSuccess && sms > 0)
+          fallback_ctas = 4LL * sms;
+      }
       coarse_cap = (n > 3 && L > 2) ? coarse_cap_for(tile_coarse) : 0;
       coarse_smem = coarse_smem_for(tile_coarse);
       b5 = p.filter == HMP_FILTER_BINOMIAL5 && L > 1;
@@ -1012,29 +1018,48 @@ struct hmp_stitcher {
     }
     const int fx0 = a.wx0 & ~1, fy0 = a.wy0 & ~1;
     const dim3 fgrid((a.wx1 - fx0 + 63) / 64, (a.wy1 - fy0 + 15) / 16, p.batch);
-    // The pyramid chain: dense, or (copy-block mode) over the work lists.
+    // The pyramid chain: dense, or (copy-block mode) over the work lists, or as the gated fallback,
+    // whose few CTAs walk the dense grids (every tile of every frame) only when the gate is set.
+    const auto walk = [&](const dim3& dense) {
+      const long long tiles = (long long)dense.x * dense.y * dense.z;
+      return dim3(unsigned(std::min<long long>(tiles, fallback_ctas)), 1, 1);
+    };
     const auto chain = [&](const hmp::PyrArgs& base, bool listed, cudaStream_t cs, bool timed) -> hmp_status {
       hmp::PyrArgs q = base;
+      const bool gated = q.gate != nullptr;
+      const auto grid_of = [&](const dim3& dense, int n_list) {
+        if (listed) return dim3(unsigned(n_list), 1, unsigned(p.batch));
+        if (gated) {
+          q.fb_nx = int(dense.x);
+          q.fb_ny = int(dense.y);
+          q.fb_batch = int(dense.z);
+          return walk(dense);
+        }
+        return dense;
+      };
       if (p.levels > 1 && !b5 && (!listed || n_down[di] > 0)) {
         q.tile = tile_down;
         q.tiles = listed ? down_list[di] : nullptr;
+        const dim3 g = grid_of(dgrid, n_down[di]);
         if (timed) tbegin(1, cs);
-        e = hmp::launch_pyr_down(q, p.storage, listed ? dim3(n_down[di], 1, p.batch) : dgrid, cs);
+        e = hmp::launch_pyr_down(q, p.storage, g, cs);
         if (timed) tend(1, cs);
         if (e != cudaSuccess) return failed(e, "pyr_down launch");
       }
       if (p.levels > 1 && !b5 && (!listed || n_coarse > 0)) {
         q.tile = tile_coarse;
         q.tiles = listed ? coarse_list : nullptr;
+        const dim3 g = grid_of(cgrid, n_coarse);
         if (timed) tbegin(2, cs);
-        e = hmp::launch_pyr_coarse(q, p.rule, p.storage, listed ? dim3(n_coarse, 1, p.batch) : cgrid, coarse_smem, cs);
+        e = hmp::launch_pyr_coarse(q, p.rule, p.storage, g, coarse_smem, cs);
         if (timed) tend(2, cs);
         if (e != cudaSuccess) return failed(e, "pyr_coarse launch");
       }
       if (!b5 && (!listed || n_fine > 0)) {
         q.tiles = listed ? fine_list : nullptr;
+        const dim3 g = grid_of(fgrid, n_fine);
         if (timed) tbegin(3, cs);
-        e = hmp::launch_pyr_fine(q, p.rule, p.storage, listed ? dim3(n_fine, 1, p.batch) : fgrid, cs);
+        e = hmp::launch_pyr_fine(q, p.rule, p.storage, g, cs);
         if (timed) tend(3, cs);
         if (e != cudaSuccess) return failed(e, "pyr_fine launch");
       }
