@@ -178,10 +178,19 @@ void plan_copy_blocks(const Plan& p, int td, int t1, CopyPlan& cp) {
       }
       mark_down(f0x, f0y, f1x - 1, f1y - 1);
     }
+  // Down tiles that meet a pyramid block's pixels: pyr_fine reads their kept level-0 pixels.
+  std::vector<uint8_t> keep0(size_t(ndx) * ndy, 0);
+  for (uint32_t f : cp.fine_list) {
+    const int i = int(f & 0xFFFFu), j = int(f >> 16);
+    const int x0 = std::max(cp.fx0 + 64 * i, wx0), x1 = std::min(cp.fx0 + 64 * i + 64, wx1) - 1;
+    const int y0 = std::max(cp.fy0 + 16 * j, wy0), y1 = std::min(cp.fy0 + 16 * j + 16, wy1) - 1;
+    for (int ty = y0 / td; ty <= y1 / td; ++ty)
+      for (int tx = x0 / td; tx <= x1 / td; ++tx) keep0[size_t(ty) * ndx + tx] = 1;
+  }
   for (int ty = 0; ty < ndy; ++ty)
     for (int tx = 0; tx < ndx; ++tx) {
       if (!dmark[size_t(ty) * ndx + tx]) continue;
-      cp.down_list.push_back(uint32_t(tx) | (uint32_t(ty) << 16));
+      cp.down_list.push_back(uint32_t(tx) | (uint32_t(ty) << 16) | (keep0[size_t(ty) * ndx + tx] ? 0x80000000u : 0u));
     }
   cp.support_mark = std::move(support_mark);
   cp.support_pitch = gx;

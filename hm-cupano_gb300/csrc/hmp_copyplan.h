@@ -50,7 +50,8 @@ struct CopyPlan {
   std::vector<uint8_t> block_class;         // [nfy][nfx]: kBlockCopy, kBlockPyramid or kBlockEmpty
   std::vector<uint32_t> fine_list;          // tx | ty << 16 of the pyramid blocks
   std::vector<uint32_t> coarse_list;        // absolute level-1 tiles of edge tile_coarse
-  std::vector<uint32_t> down_list;          // level-0 tiles of edge tile_down
+  std::vector<uint32_t> down_list;          // level-0 tiles of edge tile_down; bit 31: pyr_fine reads
+                                            // the tile's kept level-0 pixels
   // [gy][gx], one byte per 2^(L-1) block of the blend region: 1 + the slot a copy block copies
   // inside its support (one label there, and that slot has a source pixel at every pixel), else 0.
   std::vector<uint8_t> support_mark;

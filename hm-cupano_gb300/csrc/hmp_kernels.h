@@ -58,9 +58,11 @@ struct PyrArgs {
   int coarse_cap; // N-way pyr_coarse: likewise, per coarse tile
   int fine_cap;   // N-way pyr_fine: likewise, per 64 x 16 level-0 block (with its upsample halo)
   int pdl;        // launch pyr_coarse / pyr_fine as programmatic dependents of the kernel before them
-  // Work list of the launch (copy-block mode): entry blockIdx.x is the CTA's tile, tx | ty << 16.
+  // Work list of the launch (copy-block mode): entry blockIdx.x is the CTA's tile, tx | ty << 16;
+  // in pyr_down's list bit 31 marks the tiles whose kept level-0 pixels pyr_fine reads.
   // nullptr: the dense grid.
   const uint32_t* tiles;
+  int list_frames;  // listed launches: grid.x = entries x list_frames, frame = blockIdx.x % list_frames
   // Copy-block mode, pyr_fine: a level-0 pixel whose block of 2^sm_shift pixels is marked in
   // support_mark ([.][sm_pitch], blend coordinates) lies in a copy block's reconstruction support;
   // alpha 0 of its label image's pixel there sets *alpha_flag.

@@ -101,6 +101,17 @@ __device__ __forceinline__ Store* level_of(const PyrArgs& a, int k, int l, int b
 // kernel has completed and its writes are visible (at once after a normal launch).
 __device__ __forceinline__ void grid_dep_wait() { asm volatile("griddepcontrol.wait;\n" ::: "memory"); }
 
+// pyr_down in copy-block mode: bit 31 of a listed tile says whether pyr_fine reads the tile's kept
+// level-0 pixels (the tile meets a pyramid block); other listed tiles feed only coarser levels.
+// Dense and walking launches keep every tile's.
+template <bool kLists, bool kWalk>
+__device__ __forceinline__ bool keeps_level0(const PyrArgs& a) {
+  if constexpr (kLists && !kWalk) {
+    if (a.tiles != nullptr) return (__ldg(a.tiles + blockIdx.x / a.list_frames) >> 31) != 0u;
+  }
+  return true;
+}
+
 // Work item w (0, 1, ...) of this CTA: its tile (tx, ty) and frame b. Without kWalk, one item:
 // blockIdx.x / y of the dense grid, or entry blockIdx.x of the launch's work list (copy-block mode:
 // tx | ty << 16), frame blockIdx.z. kWalk (the gated fallback of copy-block mode): false at once
@@ -128,9 +139,13 @@ __device__ __forceinline__ bool cta_tile(const PyrArgs& a, int w, int& tx, int& 
   } else {
     if constexpr (kLists) {
       if (a.tiles != nullptr) {
-        const uint32_t t = __ldg(a.tiles + blockIdx.x);
+        // Listed launches put the frame fastest: the CTAs of one tile for every frame of the call
+        // run together and share its table entries in L2.
+        const int i = int(blockIdx.x) / a.list_frames;
+        b = int(blockIdx.x) - i * a.list_frames;
+        const uint32_t t = __ldg(a.tiles + i);
         tx = int(t & 0xFFFFu);
-        ty = int(t >> 16);
+        ty = int((t >> 16) & 0x7FFFu);
       }
     }
     return true;
@@ -230,7 +245,7 @@ __global__ void __launch_bounds__(256) pyr_down_kernel(const __grid_constant__ P
     if constexpr (kKeepLevel0) {
   #pragma unroll
       for (int k = 0; k < NMAX; ++k) {
-        if (!active[k] || !a.use_p0) continue;
+        if (!active[k] || !a.use_p0 || !keeps_level0<(NMAX >= 3 || kListed), kWalk>(a)) continue;
         const PlaneDev& P = a.slot[k];
         uint32_t* dst = a.P0[k] + (long long)b * P.w * P.h;
         const uint32_t* pk = pix + k * TD * TD;
@@ -414,7 +429,7 @@ __global__ void __launch_bounds__(256) pyr_down_n_kernel(const __grid_constant__
     }
     cp_async_commit_wait_all();
     __syncthreads();
-    if (a.use_p0) {
+    if (a.use_p0 && keeps_level0<true, kWalk>(a)) {
   #pragma unroll 1
       for (int c = 0; c < na; ++c) {
         const int k = (list >> (4 * c)) & 15u;

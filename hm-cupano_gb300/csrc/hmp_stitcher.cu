@@ -802,6 +802,7 @@ struct hmp_stitcher {
     a.coarse_cap = coarse_cap;
     a.tile = tile_down;
     a.down_smem_floor = int(hmp::residency_smem(down_residency));
+    a.list_frames = 1;
     return a;
   }
 
@@ -932,7 +933,10 @@ struct hmp_stitcher {
     // Copy-block mode for this call: planned, switched on, and every table entry the copy blocks
     // read lies inside these frames (else it would read as a fill).
     const int di = tile_down == 64 ? 1 : 0;
-    bool copy = copy_plan && copy_on && (n_fine == 0 || down_list[di] != nullptr);
+    // Listed launches interleave the call's frames in grid.x, which must hold entries x frames.
+    const long long longest = std::max<long long>({n_down[di], n_coarse, n_fine});
+    bool copy = copy_plan && copy_on && (n_fine == 0 || down_list[di] != nullptr) &&
+                longest * p.batch < (1LL << 31) - 1;
     for (int k = 0; copy && k < p.n; ++k) copy = uint32_t(S.w[k]) >= need_w[k] && uint32_t(S.h[k]) >= need_h[k];
     hmp::GatherArgs ga{};
     if (p.canvas_plane_used) {
@@ -1028,7 +1032,10 @@ struct hmp_stitcher {
       hmp::PyrArgs q = base;
       const bool gated = q.gate != nullptr;
       const auto grid_of = [&](const dim3& dense, int n_list) {
-        if (listed) return dim3(unsigned(n_list), 1, unsigned(p.batch));
+        if (listed) {
+          q.list_frames = p.batch;
+          return dim3(unsigned(n_list) * unsigned(p.batch), 1, 1);
+        }
         if (gated) {
           q.fb_nx = int(dense.x);
           q.fb_ny = int(dense.y);
