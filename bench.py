@@ -542,7 +542,8 @@ def main() -> None:
         # levels (FP32 and FP16), and the headline frame with FP16 storage, Binomial5, 0 levels.
         from hmpano import variants
 
-        line["variants"] = variants.run(dev, max(50, min(args.steps, 300)), peak)
+        line["variants"] = variants.run(dev, max(50, min(args.steps, 300)), peak,
+                                        only=[v[0] for v in variants.VARIANTS if v[0] != "pano2_l6_f32"])
     if not args.no_batched and world == 1:
         # Batched streaming job: 4 two-image + 4 three-image streams x 32 frames, FP16 storage, one
         # CUDA graph, frames per call and tiles autotuned.

@@ -22,6 +22,7 @@ from . import _lib, pano, synth
 
 VARIANTS = [
     # (name, workload, kind, levels, storage, filter)
+    ("pano2_l6_f32", "pano2_5120x2880_to_8500x3300", 2, 6, "f32", "refbox"),
     ("pano2_l6_f16", "pano2_5120x2880_to_8500x3300", 2, 6, "f16", "refbox"),
     ("pano2_l6_binomial5", "pano2_5120x2880_to_8500x3300", 2, 6, "f32", "binomial5"),
     ("pano2_l0", "pano2_5120x2880_to_8500x3300", 2, 0, "f32", "refbox"),
@@ -107,3 +108,21 @@ def run(device, steps: int, peak_gbs: float, warmup: int = 5, only=None) -> dict
         del st
     torch.cuda.synchronize(device)
     return out
+
+
+if __name__ == "__main__":
+    import argparse
+    import json
+
+    import torch
+
+    ap = argparse.ArgumentParser(description="Frame times of the named workloads (one stitcher each, one stream).")
+    ap.add_argument("--only", default="", help="comma-separated variant names (default: all): "
+                    + ", ".join(v[0] for v in VARIANTS))
+    ap.add_argument("--steps", type=int, default=300)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--peak-gbs", type=float, default=6695.8, help="copy bandwidth for hbm_frac_frame")
+    args = ap.parse_args()
+    only = [s for s in args.only.split(",") if s] or None
+    for name, res in run(torch.device("cuda", 0), args.steps, args.peak_gbs, args.warmup, only).items():
+        print(json.dumps({"variant": name, **res}), flush=True)
