@@ -223,6 +223,26 @@ def cpu_baseline(rig, frames, levels: int, seconds: float = 10.0) -> dict:
                       f"{dt * 1e3:.0f} ms/frame", "fps": round(1.0 / dt, 3)}
 
 
+def cpu_baseline_stabilize(seconds: float = 8.0) -> dict:
+    """The stabiliser oracle (C port of src/cuda/cudaStabilize.cu, one core) on the GPU leg's
+    3840x2160 frame pair: as many runs as fit in about `seconds`."""
+    from hmpano import stabilize_bench
+    from oracle import oracle
+
+    oracle.build()
+    prev, nxt = stabilize_bench.frames(2160, 3840)
+    st = oracle.Stabilize()
+    t0 = time.perf_counter()
+    st.run(prev, nxt)
+    runs = max(2, int(seconds / max(time.perf_counter() - t0, 1e-3)))
+    t0 = time.perf_counter()
+    for _ in range(runs):
+        st.run(prev, nxt)
+    dt = (time.perf_counter() - t0) / runs
+    return {"value": round(dt * 1e3, 2), "unit": "ms/frame", "cores": 1, "kind": "port",
+            "sample": f"{runs} runs of the 3840x2160 pair after 1 warm-up"}
+
+
 def reference_arm(args) -> None:
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -278,6 +298,7 @@ def main() -> None:
     ap.add_argument("--no-serve", action="store_true", help="skip the serving sweep (p50/p99 latency)")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched multi-stream graph job")
     ap.add_argument("--no-variants", action="store_true", help="skip the other workloads' frame times")
+    ap.add_argument("--no-stabilize", action="store_true", help="skip the frame stabiliser timings")
     ap.add_argument("--serve-seconds", type=float, default=1.0, help="arrival window per offered rate")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
@@ -555,6 +576,13 @@ def main() -> None:
         from hmpano import serve_bench
 
         line["serve"] = serve_bench.sweep(dev, seconds=args.serve_seconds)
+    if not args.no_stabilize and world == 1:
+        # Frame stabiliser (Harris corners, Lucas-Kanade flow, warp) on a 3840x2160 float frame pair.
+        from hmpano import stabilize_bench
+
+        line["stabilize"] = stabilize_bench.run(dev, peak)
+        if not args.no_cpu_baseline:
+            line["stabilize"]["cpu_baseline"] = cpu_baseline_stabilize()
     if rank == 0:
         print(json.dumps(line), flush=True)
     reps.close()

@@ -37,6 +37,7 @@ UNITS = {
     "hmp_control_dir.cpp": [],
     "hmp_generic.cu": ["-fmad=false"],
     "hmp_batch.cpp": [],
+    "hmp_stabilize.cu": ["-fmad=false"],
 }
 HEADERS = ["hmp_plan.h", "hmp_copyplan.h", "hmp_device.cuh", "hmp_kernels.h", "hmp_blend.cuh", "hmp_admission.h"]
 

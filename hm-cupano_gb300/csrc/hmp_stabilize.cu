@@ -1,0 +1,412 @@
+// hmp_stabilize.cu -- frame stabiliser (hmp_stabilizer_* in include/hmpano.h).
+//
+// The reference ships it as a demo beside the stitcher (src/cuda/cudaStabilize.cu): Harris corners
+// of the previous frame, sparse Lucas-Kanade flow of each into the next frame, the mean flow as the
+// global motion, and the next frame translated by it. There every step round-trips through the
+// host (the response map is copied out for thresholding, the features copied in, the flow copied
+// out and averaged on the CPU) with a synchronize after each kernel and allocations per call. Here
+// a stabiliser allocates once and every step stays on the device, asynchronous on the caller's
+// stream:
+//   harris      Sobel gradients and the 3x3 Harris response of a 32 x 8 tile, the image tile (with
+//               a 2-pixel halo) and its gradients staged in shared memory;
+//   corners     threshold + 3x3 non-maximum suppression: a warp per row counts its corners with
+//               ballots, one CTA scans the row counts, and a warp per row writes its corners at its
+//               offset, so the list is in raster order as the reference's host loop builds it;
+//   flow        Lucas-Kanade per feature, one thread each, the reference's sums in its order;
+//   motion      one thread sums the flow in feature order (the reference's host sum) and rounds;
+//   warp        translation by the rounded mean, zero fill.
+// Operation order follows the reference (this file is compiled with -fmad=false); where the
+// reference reads memory it never defines, the values are fixed as the oracle documents
+// (oracle/hmp_stabilize_oracle.c): gradients and responses outside the interior are 0, flow taps
+// in column 0 or row 0 are skipped, and no corners means no motion.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <new>
+
+#include "hmpano.h"
+
+namespace {
+
+struct Motion {
+  int corners;     // corners found (the list holds at most the stabiliser's capacity)
+  float dx, dy;    // mean flow
+  int sx, sy;      // its rounding, the translation applied
+};
+
+constexpr int kTX = 32, kTY = 8;
+
+// A displacement rounded to whole pixels: the float-to-int conversion saturates and maps NaN to 0;
+// the clamp at +-2^24 keeps the index sums in range (a shift that large leaves the frame either way).
+__device__ __forceinline__ int shift_of(float v) {
+  if (!(v == v)) return 0;
+  return int(fminf(fmaxf(roundf(v), -16777216.0f), 16777216.0f));
+}
+
+__global__ void __launch_bounds__(256) harris_kernel(const float* __restrict__ img, int w, int h, float k,
+                                                     float* __restrict__ resp) {
+  __shared__ float t[kTY + 4][kTX + 4];      // image, origin (X0 - 2, Y0 - 2); 0 outside
+  __shared__ float gx[kTY + 2][kTX + 2];     // gradients, origin (X0 - 1, Y0 - 1); 0 off the interior
+  __shared__ float gy[kTY + 2][kTX + 2];
+  const int X0 = blockIdx.x * kTX, Y0 = blockIdx.y * kTY;
+  const int tid = threadIdx.y * kTX + threadIdx.x;
+  for (int i = tid; i < (kTY + 4) * (kTX + 4); i += kTX * kTY) {
+    const int tx = i % (kTX + 4), ty = i / (kTX + 4);
+    const int x = X0 - 2 + tx, y = Y0 - 2 + ty;
+    t[ty][tx] = (x >= 0 && x < w && y >= 0 && y < h) ? img[(long long)y * w + x] : 0.f;
+  }
+  __syncthreads();
+  for (int i = tid; i < (kTY + 2) * (kTX + 2); i += kTX * kTY) {
+    const int tx = i % (kTX + 2), ty = i / (kTX + 2);
+    const int x = X0 - 1 + tx, y = Y0 - 1 + ty;
+    float vx = 0.f, vy = 0.f;
+    if (x > 0 && x < w - 1 && y > 0 && y < h - 1) {
+      // t[ty + 1][tx + 1] is pixel (x, y)
+      const float* r0 = &t[ty][tx + 1];
+      const float* r1 = &t[ty + 1][tx + 1];
+      const float* r2 = &t[ty + 2][tx + 1];
+      vx = r0[1] + 2.0f * r1[1] + r2[1] - r0[-1] - 2.0f * r1[-1] - r2[-1];
+      vy = r0[-1] + 2.0f * r0[0] + r0[1] - r2[-1] - 2.0f * r2[0] - r2[1];
+    }
+    gx[ty][tx] = vx;
+    gy[ty][tx] = vy;
+  }
+  __syncthreads();
+  const int x = X0 + threadIdx.x, y = Y0 + threadIdx.y;
+  if (x >= w || y >= h) return;
+  float r = 0.f;
+  if (x > 0 && x < w - 1 && y > 0 && y < h - 1) {
+    float sxx = 0.f, sxy = 0.f, syy = 0.f;
+#pragma unroll
+    for (int j = -1; j <= 1; ++j)
+#pragma unroll
+      for (int i = -1; i <= 1; ++i) {
+        const float ix = gx[threadIdx.y + 1 + j][threadIdx.x + 1 + i];
+        const float iy = gy[threadIdx.y + 1 + j][threadIdx.x + 1 + i];
+        sxx += ix * ix;
+        sxy += ix * iy;
+        syy += iy * iy;
+      }
+    const float det = sxx * syy - sxy * sxy;
+    const float tr = sxx + syy;
+    r = det - k * tr * tr;
+  }
+  resp[(long long)y * w + x] = r;
+}
+
+// Threshold and 3x3 non-maximum suppression (a neighbour strictly above removes the pixel).
+__device__ __forceinline__ bool is_corner(const float* resp, int w, int h, float thr, int x, int y) {
+  if (x < 1 || x >= w - 1 || y < 1 || y >= h - 1) return false;
+  const float r = __ldg(resp + (long long)y * w + x);
+  if (!(r > thr)) return false;
+  for (int j = -1; j <= 1; ++j)
+    for (int i = -1; i <= 1; ++i)
+      if (__ldg(resp + (long long)(y + j) * w + (x + i)) > r) return false;
+  return true;
+}
+
+// A warp per row: its corner count.
+__global__ void __launch_bounds__(256) corner_count_kernel(const float* resp, int w, int h, float thr, int* row_count) {
+  const int lane = threadIdx.x & 31, y = blockIdx.x * 8 + (threadIdx.x >> 5);
+  if (y >= h) return;
+  int c = 0;
+  for (int x0 = 0; x0 < w; x0 += 32) c += __popc(__ballot_sync(0xFFFFFFFFu, is_corner(resp, w, h, thr, x0 + lane, y)));
+  if (lane == 0) row_count[y] = c;
+}
+
+// One CTA: row offsets (exclusive scan of the counts, in chunks of 1024 rows) and the total.
+__global__ void __launch_bounds__(1024) corner_scan_kernel(const int* row_count, int h, int* row_off, Motion* m) {
+  __shared__ int warp_sum[32];
+  __shared__ int carry;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (threadIdx.x == 0) carry = 0;
+  __syncthreads();
+  for (int base = 0; base < h; base += 1024) {
+    const int y = base + threadIdx.x;
+    const int v = y < h ? row_count[y] : 0;
+    int s = v;  // inclusive scan within the warp
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      const int u = __shfl_up_sync(0xFFFFFFFFu, s, d);
+      if (lane >= d) s += u;
+    }
+    if (lane == 31) warp_sum[wid] = s;
+    __syncthreads();
+    if (wid == 0) {
+      int ws = warp_sum[lane];
+#pragma unroll
+      for (int d = 1; d < 32; d <<= 1) {
+        const int u = __shfl_up_sync(0xFFFFFFFFu, ws, d);
+        if (lane >= d) ws += u;
+      }
+      warp_sum[lane] = ws;  // inclusive over warps
+    }
+    __syncthreads();
+    const int before = carry + (wid > 0 ? warp_sum[wid - 1] : 0) + s - v;
+    if (y < h) row_off[y] = before;
+    __syncthreads();
+    if (threadIdx.x == 1023) carry = before + v;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) m->corners = carry;
+}
+
+// A warp per row: its corners, in x order, at the row's offset (those within the capacity).
+__global__ void __launch_bounds__(256) corner_emit_kernel(const float* resp, int w, int h, float thr,
+                                                          const int* row_off, int2* xy, int cap) {
+  const int lane = threadIdx.x & 31, y = blockIdx.x * 8 + (threadIdx.x >> 5);
+  if (y >= h) return;
+  int at = row_off[y];
+  for (int x0 = 0; x0 < w; x0 += 32) {
+    const bool c = is_corner(resp, w, h, thr, x0 + lane, y);
+    const unsigned bits = __ballot_sync(0xFFFFFFFFu, c);
+    const int pos = at + __popc(bits & ((1u << lane) - 1u));
+    if (c && pos < cap) xy[pos] = make_int2(x0 + lane, y);
+    at += __popc(bits);
+  }
+}
+
+// Lucas-Kanade per feature: 10 iterations over a window_size window, the displacement rounded to
+// whole pixels for sampling the next frame (the reference's scheme and sum order).
+__global__ void __launch_bounds__(256) flow_kernel(const float* __restrict__ prev, const float* __restrict__ next,
+                                                   const int2* xy, const Motion* m, int cap, int w, int h, int window,
+                                                   float2* flow) {
+  const int f = blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= min(m->corners, cap)) return;
+  const int2 p = xy[f];
+  const int half = window / 2;
+  float dx = 0.f, dy = 0.f;
+  for (int iter = 0; iter < 10; ++iter) {
+    float sxx = 0.f, syy = 0.f, sxy = 0.f, stx = 0.f, sty = 0.f;
+    const int rdx = shift_of(dx), rdy = shift_of(dy);
+    for (int j = -half; j <= half; ++j)
+      for (int i = -half; i <= half; ++i) {
+        const int x = p.x + i, y = p.y + j, xn = x + rdx, yn = y + rdy;
+        if (x < 1 || x >= w - 1 || y < 1 || y >= h - 1 || xn < 0 || xn >= w - 1 || yn < 0 || yn >= h - 1) continue;
+        const long long o = (long long)y * w + x;
+        const float ix = (__ldg(prev + o + 1) - __ldg(prev + o - 1)) * 0.5f;
+        const float iy = (__ldg(prev + o + w) - __ldg(prev + o - w)) * 0.5f;
+        const float it = __ldg(next + (long long)yn * w + xn) - __ldg(prev + o);
+        sxx += ix * ix;
+        syy += iy * iy;
+        sxy += ix * iy;
+        stx += ix * it;
+        sty += iy * it;
+      }
+    const float det = sxx * syy - sxy * sxy;
+    if (fabsf(det) < 1e-6f) break;
+    const float ddx = (-syy * stx + sxy * sty) / det;
+    const float ddy = (sxy * stx - sxx * sty) / det;
+    dx += ddx;
+    dy += ddy;
+    if (sqrtf(ddx * ddx + ddy * ddy) < 0.01f) break;
+  }
+  flow[f] = make_float2(dx, dy);
+}
+
+// The global motion: the flow summed in feature order (as the reference's host loop), its mean and
+// the rounded translation.
+__global__ void motion_kernel(const float2* flow, int cap, Motion* m) {
+  const int n = min(m->corners, cap);
+  float sx = 0.f, sy = 0.f;
+  for (int f = 0; f < n; ++f) {
+    sx += flow[f].x;
+    sy += flow[f].y;
+  }
+  m->dx = n > 0 ? sx / float(n) : 0.f;
+  m->dy = n > 0 ? sy / float(n) : 0.f;
+  m->sx = shift_of(m->dx);
+  m->sy = shift_of(m->dy);
+}
+
+__global__ void __launch_bounds__(256) warp_kernel(const float* __restrict__ in, float* __restrict__ out, int w, int h,
+                                                   const Motion* m) {
+  const int x = blockIdx.x * kTX + threadIdx.x, y = blockIdx.y * kTY + threadIdx.y;
+  if (x >= w || y >= h) return;
+  const int u = x - m->sx, v = y - m->sy;
+  out[(long long)y * w + x] = (u >= 0 && u < w && v >= 0 && v < h) ? in[(long long)v * w + u] : 0.f;
+}
+
+__global__ void copy_kernel(const float* __restrict__ in, float* __restrict__ out, long long n) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = in[i];
+}
+
+hmp_status status_of(int code, const char* msg) {
+  hmp_status s;
+  s.code = code;
+  std::snprintf(s.message, sizeof(s.message), "%s", msg);
+  return s;
+}
+
+hmp_status cuda_failure(cudaError_t e, const char* what) {
+  hmp_status s;
+  s.code = int(e);
+  std::snprintf(s.message, sizeof(s.message), "%s: %s", what, cudaGetErrorString(e));
+  return s;
+}
+
+}  // namespace
+
+struct hmp_stabilizer {
+  int w = 0, h = 0, cap = 0, device = -1;
+  float* resp = nullptr;
+  int* row_count = nullptr;
+  int* row_off = nullptr;
+  int2* xy = nullptr;
+  float2* flow = nullptr;
+  Motion* motion = nullptr;
+  float* temp = nullptr;  // an in-place warp's output before the copy back
+  ~hmp_stabilizer() {
+    for (void* p : {static_cast<void*>(resp), static_cast<void*>(row_count), static_cast<void*>(row_off),
+                    static_cast<void*>(xy), static_cast<void*>(flow), static_cast<void*>(motion),
+                    static_cast<void*>(temp)})
+      if (p) cudaFree(p);
+  }
+  hmp_status check(const void* a, const void* b) const {
+    int dev = -1;
+    cudaGetDevice(&dev);
+    if (dev != device) return status_of(HMP_ERR_INVALID_VALUE, "stabilizer used on another device");
+    if (!a || !b) return status_of(HMP_ERR_INVALID_DEVICE_POINTER, "frame is null");
+    return status_of(HMP_OK, "");
+  }
+};
+
+extern "C" {
+
+HMP_API hmp_status hmp_stabilizer_create(int width, int height, int max_features, hmp_stabilizer** out) {
+  if (!out) return status_of(HMP_ERR_INVALID_VALUE, "out is null");
+  *out = nullptr;
+  if (width < 3 || height < 3 || width > (1 << 15) || height > (1 << 15))
+    return status_of(HMP_ERR_INVALID_VALUE, "frames must be 3..32768 pixels per side");
+  const long long interior = (long long)(width - 2) * (height - 2);
+  if (max_features < 0) return status_of(HMP_ERR_INVALID_VALUE, "max_features must be >= 0 (0: every interior pixel)");
+  hmp_stabilizer* st = new (std::nothrow) hmp_stabilizer();
+  if (!st) return status_of(HMP_ERR_MEMORY_ALLOCATION, "out of host memory");
+  st->w = width;
+  st->h = height;
+  st->cap = int(max_features == 0 ? interior : std::min<long long>(max_features, interior));
+  cudaError_t e = cudaGetDevice(&st->device);
+  const size_t px = size_t(width) * height;
+  if (e == cudaSuccess) e = cudaMalloc(&st->resp, px * sizeof(float));
+  if (e == cudaSuccess) e = cudaMalloc(&st->row_count, size_t(height) * sizeof(int));
+  if (e == cudaSuccess) e = cudaMalloc(&st->row_off, size_t(height) * sizeof(int));
+  if (e == cudaSuccess) e = cudaMalloc(&st->xy, size_t(std::max(st->cap, 1)) * sizeof(int2));
+  if (e == cudaSuccess) e = cudaMalloc(&st->flow, size_t(std::max(st->cap, 1)) * sizeof(float2));
+  if (e == cudaSuccess) e = cudaMalloc(&st->motion, sizeof(Motion));
+  if (e == cudaSuccess) e = cudaMalloc(&st->temp, px * sizeof(float));
+  if (e == cudaSuccess) e = cudaMemset(st->motion, 0, sizeof(Motion));
+  if (e != cudaSuccess) {
+    delete st;
+    return cuda_failure(e, "stabilizer allocation");
+  }
+  *out = st;
+  return status_of(HMP_OK, "");
+}
+
+HMP_API void hmp_stabilizer_destroy(hmp_stabilizer* st) { delete st; }
+
+HMP_API hmp_status hmp_stabilizer_corners(hmp_stabilizer* st, const float* img, float k, float threshold,
+                                          void* stream) {
+  if (!st) return status_of(HMP_ERR_INVALID_VALUE, "stabilizer is null");
+  hmp_status s = st->check(img, img);
+  if (s.code) return s;
+  const cudaStream_t cs = static_cast<cudaStream_t>(stream);
+  const dim3 tiles((st->w + kTX - 1) / kTX, (st->h + kTY - 1) / kTY);
+  harris_kernel<<<tiles, dim3(kTX, kTY), 0, cs>>>(img, st->w, st->h, k, st->resp);
+  const int rows = (st->h + 7) / 8;
+  corner_count_kernel<<<rows, 256, 0, cs>>>(st->resp, st->w, st->h, threshold, st->row_count);
+  corner_scan_kernel<<<1, 1024, 0, cs>>>(st->row_count, st->h, st->row_off, st->motion);
+  corner_emit_kernel<<<rows, 256, 0, cs>>>(st->resp, st->w, st->h, threshold, st->row_off, st->xy, st->cap);
+  const cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? status_of(HMP_OK, "") : cuda_failure(e, "corner launch");
+}
+
+HMP_API hmp_status hmp_stabilizer_flow(hmp_stabilizer* st, const float* prev, const float* next, int window_size,
+                                       void* stream) {
+  if (!st) return status_of(HMP_ERR_INVALID_VALUE, "stabilizer is null");
+  hmp_status s = st->check(prev, next);
+  if (s.code) return s;
+  if (window_size < 1 || window_size > 255) return status_of(HMP_ERR_INVALID_VALUE, "window_size must be in 1..255");
+  const cudaStream_t cs = static_cast<cudaStream_t>(stream);
+  flow_kernel<<<(std::max(st->cap, 1) + 255) / 256, 256, 0, cs>>>(prev, next, st->xy, st->motion, st->cap, st->w,
+                                                                   st->h, window_size, st->flow);
+  motion_kernel<<<1, 1, 0, cs>>>(st->flow, st->cap, st->motion);
+  const cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? status_of(HMP_OK, "") : cuda_failure(e, "flow launch");
+}
+
+HMP_API hmp_status hmp_stabilizer_warp(hmp_stabilizer* st, const float* frame, float* out, void* stream) {
+  if (!st) return status_of(HMP_ERR_INVALID_VALUE, "stabilizer is null");
+  hmp_status s = st->check(frame, out);
+  if (s.code) return s;
+  const cudaStream_t cs = static_cast<cudaStream_t>(stream);
+  const dim3 tiles((st->w + kTX - 1) / kTX, (st->h + kTY - 1) / kTY);
+  const long long px = (long long)st->w * st->h;
+  if (out == frame) {
+    warp_kernel<<<tiles, dim3(kTX, kTY), 0, cs>>>(frame, st->temp, st->w, st->h, st->motion);
+    copy_kernel<<<unsigned((px + 255) / 256), 256, 0, cs>>>(st->temp, out, px);
+  } else {
+    warp_kernel<<<tiles, dim3(kTX, kTY), 0, cs>>>(frame, out, st->w, st->h, st->motion);
+  }
+  const cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? status_of(HMP_OK, "") : cuda_failure(e, "warp launch");
+}
+
+HMP_API hmp_status hmp_stabilizer_run(hmp_stabilizer* st, const float* prev, const float* next, float* out, float k,
+                                      float threshold, int window_size, void* stream) {
+  hmp_status s = hmp_stabilizer_corners(st, prev, k, threshold, stream);
+  if (s.code == HMP_OK) s = hmp_stabilizer_flow(st, prev, next, window_size, stream);
+  if (s.code == HMP_OK) s = hmp_stabilizer_warp(st, next, out, stream);
+  return s;
+}
+
+HMP_API hmp_status hmp_stabilizer_get_features(hmp_stabilizer* st, int* xy, float* flow, int capacity,
+                                               hmp_stabilize_info* info, void* stream) {
+  if (!st || !info || capacity < 0 || (capacity > 0 && (!xy || !flow)))
+    return status_of(HMP_ERR_INVALID_VALUE, "invalid argument");
+  const cudaStream_t cs = static_cast<cudaStream_t>(stream);
+  cudaError_t e = cudaStreamSynchronize(cs);
+  Motion m{};
+  if (e == cudaSuccess) e = cudaMemcpy(&m, st->motion, sizeof(m), cudaMemcpyDeviceToHost);
+  const int n = std::min({m.corners, st->cap, capacity});
+  if (e == cudaSuccess && n > 0) e = cudaMemcpy(xy, st->xy, size_t(n) * sizeof(int2), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess && n > 0) e = cudaMemcpy(flow, st->flow, size_t(n) * sizeof(float2), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return cuda_failure(e, "feature copy");
+  info->corners = m.corners;
+  info->kept = std::min(m.corners, st->cap);
+  info->dx = m.dx;
+  info->dy = m.dy;
+  info->shift_x = m.sx;
+  info->shift_y = m.sy;
+  return status_of(HMP_OK, "");
+}
+
+HMP_API hmp_status hmp_stabilizer_get_response(hmp_stabilizer* st, float* out, size_t capacity, void* stream) {
+  if (!st || !out) return status_of(HMP_ERR_INVALID_VALUE, "invalid argument");
+  const size_t px = size_t(st->w) * st->h;
+  if (capacity < px) return status_of(HMP_ERR_INVALID_VALUE, "capacity below width * height");
+  const cudaStream_t cs = static_cast<cudaStream_t>(stream);
+  cudaError_t e = cudaStreamSynchronize(cs);
+  if (e == cudaSuccess) e = cudaMemcpy(out, st->resp, px * sizeof(float), cudaMemcpyDeviceToHost);
+  return e == cudaSuccess ? status_of(HMP_OK, "") : cuda_failure(e, "response copy");
+}
+
+HMP_API hmp_status hmp_stabilizer_set_features(hmp_stabilizer* st, const int* xy, int n, void* stream) {
+  if (!st || n < 0 || (n > 0 && !xy)) return status_of(HMP_ERR_INVALID_VALUE, "invalid argument");
+  if (n > st->cap) return status_of(HMP_ERR_INVALID_VALUE, "more features than the stabilizer holds");
+  for (int i = 0; i < n; ++i)  // the window's index sums stay in range for points on the frame
+    if (xy[2 * i] < 0 || xy[2 * i] >= st->w || xy[2 * i + 1] < 0 || xy[2 * i + 1] >= st->h)
+      return status_of(HMP_ERR_INVALID_VALUE, "feature outside the frame");
+  const cudaStream_t cs = static_cast<cudaStream_t>(stream);
+  Motion m{};
+  m.corners = n;
+  cudaError_t e = cudaSuccess;
+  if (n > 0) e = cudaMemcpyAsync(st->xy, xy, size_t(n) * sizeof(int2), cudaMemcpyHostToDevice, cs);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(st->motion, &m, sizeof(m), cudaMemcpyHostToDevice, cs);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(cs);  // the host arrays may go once this returns
+  return e == cudaSuccess ? status_of(HMP_OK, "") : cuda_failure(e, "feature upload");
+}
+
+}  // extern "C"

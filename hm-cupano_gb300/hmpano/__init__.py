@@ -24,6 +24,7 @@ from .pano import (
     read_seam_png,
     read_tiff_u16,
 )
+from .stabilize import Motion, Stabilizer
 
 __all__ = [
     "Batch",
@@ -36,8 +37,10 @@ __all__ = [
     "CudaStitchPano",
     "CudaStitchPano3",
     "CudaStitchPanoN",
+    "Motion",
     "Rect",
     "SpatialTiff",
+    "Stabilizer",
     "StitchServer",
     "UNMAPPED_POSITION_VALUE",
     "load_control_dir",

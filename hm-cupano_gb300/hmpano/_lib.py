@@ -128,6 +128,17 @@ class ControlDir(C.Structure):
     ]
 
 
+class StabilizeInfo(C.Structure):
+    _fields_ = [
+        ("corners", C.c_int),
+        ("kept", C.c_int),
+        ("dx", C.c_float),
+        ("dy", C.c_float),
+        ("shift_x", C.c_int),
+        ("shift_y", C.c_int),
+    ]
+
+
 # Every symbol include/hmpano.h declares, with its signature.
 SIGNATURES = {
     "hmp_version": ([], C.c_char_p),
@@ -172,6 +183,17 @@ SIGNATURES = {
     "hmp_batch_add": ([C.c_void_p, C.c_void_p, C.POINTER(Image), C.c_int, C.POINTER(Image), C.c_int], Status),
     "hmp_batch_capture": ([C.c_void_p, C.c_void_p], Status),
     "hmp_batch_launch": ([C.c_void_p, C.c_void_p], Status),
+    "hmp_stabilizer_create": ([C.c_int, C.c_int, C.c_int, C.POINTER(C.c_void_p)], Status),
+    "hmp_stabilizer_destroy": ([C.c_void_p], None),
+    "hmp_stabilizer_corners": ([C.c_void_p, C.c_void_p, C.c_float, C.c_float, C.c_void_p], Status),
+    "hmp_stabilizer_flow": ([C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p], Status),
+    "hmp_stabilizer_warp": ([C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p], Status),
+    "hmp_stabilizer_run": ([C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_float, C.c_float, C.c_int,
+                            C.c_void_p], Status),
+    "hmp_stabilizer_get_features": ([C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.POINTER(StabilizeInfo),
+                                     C.c_void_p], Status),
+    "hmp_stabilizer_get_response": ([C.c_void_p, C.c_void_p, C.c_size_t, C.c_void_p], Status),
+    "hmp_stabilizer_set_features": ([C.c_void_p, C.c_void_p, C.c_int, C.c_void_p], Status),
 }
 
 NOALLOC_SCRATCH_BYTES = 48 * 1024 * 1024  # HMP_NOALLOC_SCRATCH_BYTES

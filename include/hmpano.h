@@ -23,6 +23,8 @@
  *   hmp_control_dir_load  <- ControlMasks::load / ControlMasks3::load / ControlMasksN::load
  *                            src/pano/controlMasks.cpp:133-326, controlMasks3.cpp:186-300,
  *                            controlMasksN.cpp:22-193
+ *   hmp_stabilizer_*      <- the frame stabiliser src/cuda/cudaStabilize.cu: harrisCornerDetection
+ *                            (:157-204), computeOpticalFlow (:210-238), stabilizeFrame (:243-267)
  *   hmp_batch_*, hmp_server_*, hmp_blend2_noalloc: no counterpart (the reference stitches one
  *                            configuration per process, one call at a time, and every blend it
  *                            offers allocates its own device buffers)
@@ -388,6 +390,50 @@ HMP_API hmp_status hmp_plan_geometry(const hmp_config* cfg, int* canvas_w, int* 
  * all zero when the configuration has no copy blocks). With classes non-NULL it receives one byte
  * per block, row-major: 0 = copy (the label image's pixel), 1 = pyramid, 2 = empty (0, 0, 0, 0). */
 HMP_API hmp_status hmp_plan_copy_blocks(const hmp_config* cfg, int* grid, uint8_t* classes, size_t capacity);
+
+/* Frame stabiliser (src/cuda/cudaStabilize.cu): Harris corners of the previous frame, their
+ * Lucas-Kanade flow into the next frame, the mean flow as the global motion, and the next frame
+ * translated by its rounding. Frames are grayscale float, width x height contiguous, on the device.
+ * The reference copies the response map, the features and the flow through the host between
+ * steps and allocates per call; a stabiliser allocates at create (max_features corners, 0 = as
+ * many as the frame has interior pixels) and every step stays on the device, asynchronous on
+ * `stream`, so a whole run can be captured in a CUDA graph. Corners are listed in raster order;
+ * beyond max_features they are counted but not tracked. Reference defaults: k 0.04,
+ * threshold 1e6, window 15 (cudaStabilize.cu:294-300). */
+typedef struct hmp_stabilizer hmp_stabilizer;
+typedef struct hmp_stabilize_info {
+  int corners;          /* corners found in the previous frame */
+  int kept;             /* of them, tracked (min(corners, max_features)) */
+  float dx, dy;         /* mean flow, next relative to previous (0, 0 without corners) */
+  int shift_x, shift_y; /* the translation applied: dx, dy rounded to whole pixels */
+} hmp_stabilize_info;
+HMP_API hmp_status hmp_stabilizer_create(int width, int height, int max_features, hmp_stabilizer** out);
+HMP_API void hmp_stabilizer_destroy(hmp_stabilizer* st);
+/* harrisCornerDetection(d_img, width, height, k, threshold, corners) cudaStabilize.cu:157 */
+HMP_API hmp_status hmp_stabilizer_corners(hmp_stabilizer* st, const float* img, float k, float threshold,
+                                          void* stream);
+/* computeOpticalFlow(d_prev, d_next, features, flow, ..., window_size) cudaStabilize.cu:210, over
+ * the stabiliser's current features, then the mean flow (stabilizeFrame's first half, :244-252). */
+HMP_API hmp_status hmp_stabilizer_flow(hmp_stabilizer* st, const float* prev, const float* next, int window_size,
+                                       void* stream);
+/* The warp of stabilizeFrame (:254-266, warpFrameKernel :137-150) by the current motion; out may be frame (in place, as the
+ * reference does it). */
+HMP_API hmp_status hmp_stabilizer_warp(hmp_stabilizer* st, const float* frame, float* out, void* stream);
+/* corners(prev) + flow(prev, next) + warp(next -> out): the reference's main() (:274-314). */
+HMP_API hmp_status hmp_stabilizer_run(hmp_stabilizer* st, const float* prev, const float* next, float* out, float k,
+                                      float threshold, int window_size, void* stream);
+/* Waits for `stream`, then reads the motion and the first min(kept, capacity) features: xy as
+ * (x, y) int pairs, flow as (dx, dy) float pairs (both may be NULL when capacity is 0). */
+HMP_API hmp_status hmp_stabilizer_get_features(hmp_stabilizer* st, int* xy, float* flow, int capacity,
+                                               hmp_stabilize_info* info, void* stream);
+/* Waits for `stream`, then copies the last Harris response map (width * height floats, 0 on the
+ * border) to host memory `out` of `capacity` floats (the map harrisCornerDetection reads back,
+ * cudaStabilize.cu:176-177). */
+HMP_API hmp_status hmp_stabilizer_get_response(hmp_stabilizer* st, float* out, size_t capacity, void* stream);
+/* Replaces the features with n host (x, y) pairs (the reference's computeOpticalFlow takes any
+ * feature list); n <= max_features, each point on the frame (HMP_ERR_INVALID_VALUE otherwise).
+ * Waits for the upload before returning. */
+HMP_API hmp_status hmp_stabilizer_set_features(hmp_stabilizer* st, const int* xy, int n, void* stream);
 
 #ifdef __cplusplus
 }

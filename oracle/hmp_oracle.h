@@ -110,6 +110,16 @@ int hmpo_laplacian_blend_ch_f32(const float* const* inputs, int n, const float* 
 void hmpo_set_threads(int n);
 int hmpo_get_threads(void);
 
+/* Frame stabiliser (src/cuda/cudaStabilize.cu; hmp_stabilize_oracle.c). Grayscale float frames,
+ * w x h contiguous. gx, gy, resp: w*h scratch / output (the Harris response, 0 on the border).
+ * hmpo_stab_corners returns the number of corners and writes the first `cap` as (x, y) pairs. */
+void hmpo_stab_harris(const float* img, int w, int h, float k, float* gx, float* gy, float* resp);
+int hmpo_stab_corners(const float* resp, int w, int h, float threshold, int* xy, int cap);
+void hmpo_stab_flow(const float* prev, const float* next, const int* xy, int n, int w, int h, int window,
+                    float* flow);
+void hmpo_stab_mean(const float* flow, int n, float* dx, float* dy);
+void hmpo_stab_warp(const float* in, int w, int h, float dx, float dy, float* out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -24,11 +24,11 @@ FILTER_BINOMIAL5 = 1
 
 
 def build(force: bool = False) -> Path:
-    src = [HERE / "hmp_oracle.c", HERE / "hmp_oracle_body.h", HERE / "hmp_oracle.h"]
+    src = [HERE / "hmp_oracle.c", HERE / "hmp_oracle_body.h", HERE / "hmp_oracle.h", HERE / "hmp_stabilize_oracle.c"]
     if LIB_PATH.exists() and not force and all(LIB_PATH.stat().st_mtime >= s.stat().st_mtime for s in src):
         return LIB_PATH
     cmd = ["gcc", "-O2", "-std=c11", "-ffp-contract=off", "-fopenmp", "-fPIC", "-shared", "-Wall",
-           "-o", str(LIB_PATH) + ".tmp", str(HERE / "hmp_oracle.c")]
+           "-o", str(LIB_PATH) + ".tmp", str(HERE / "hmp_oracle.c"), str(HERE / "hmp_stabilize_oracle.c"), "-lm"]
     subprocess.run(cmd, check=True)
     os.replace(str(LIB_PATH) + ".tmp", LIB_PATH)
     return LIB_PATH
@@ -80,6 +80,14 @@ def lib() -> C.CDLL:
         L.hmpo_laplacian_blend_ch_f32.argtypes = [P(P(C.c_float)), C.c_int, P(C.c_float), C.c_int, C.c_int, C.c_int,
                                                   C.c_int, C.c_int, C.c_int, P(C.c_float)]
         L.hmpo_laplacian_blend_ch_f32.restype = C.c_int
+        L.hmpo_stab_harris.argtypes = [P(C.c_float), C.c_int, C.c_int, C.c_float, P(C.c_float), P(C.c_float),
+                                       P(C.c_float)]
+        L.hmpo_stab_corners.argtypes = [P(C.c_float), C.c_int, C.c_int, C.c_float, P(C.c_int), C.c_int]
+        L.hmpo_stab_corners.restype = C.c_int
+        L.hmpo_stab_flow.argtypes = [P(C.c_float), P(C.c_float), P(C.c_int), C.c_int, C.c_int, C.c_int, C.c_int,
+                                     P(C.c_float)]
+        L.hmpo_stab_mean.argtypes = [P(C.c_float), C.c_int, P(C.c_float), P(C.c_float)]
+        L.hmpo_stab_warp.argtypes = [P(C.c_float), C.c_int, C.c_int, C.c_float, C.c_float, P(C.c_float)]
         L.hmpo_set_threads.argtypes = [C.c_int]
         L.hmpo_get_threads.restype = C.c_int
         _lib = L
@@ -277,3 +285,40 @@ def load_golden_case(npz, name: str):
         "canvas": npz[f"{name}/canvas"],
     }
     return case
+
+
+class Stabilize:
+    """Frame stabiliser of src/cuda/cudaStabilize.cu on the CPU: Harris corners of `prev`, their
+    Lucas-Kanade flow into `next`, the mean flow, and `next` translated by its rounding as the
+    reference's warp does it (output (x, y) = next(x - shift_x, y - shift_y), zero outside)."""
+
+    def __init__(self, k: float = 0.04, threshold: float = 1e6, window: int = 15, max_features: int = 0):
+        self.k, self.threshold, self.window = float(k), float(threshold), int(window)
+        self.max_features = int(max_features)  # 0: no limit; else only the first ones are tracked
+
+    def run(self, prev: np.ndarray, nxt: np.ndarray, features=None) -> dict:
+        """features: an (n, 2) list of (x, y) to track instead of prev's corners."""
+        L = lib()
+        prev = np.ascontiguousarray(prev, dtype=np.float32)
+        nxt = np.ascontiguousarray(nxt, dtype=np.float32)
+        h, w = prev.shape
+        gx, gy, resp = (np.zeros((h, w), np.float32) for _ in range(3))
+        L.hmpo_stab_harris(_ptr(prev, C.c_float), w, h, self.k, _ptr(gx, C.c_float), _ptr(gy, C.c_float),
+                           _ptr(resp, C.c_float))
+        found = L.hmpo_stab_corners(_ptr(resp, C.c_float), w, h, self.threshold, None, 0)
+        xy = np.zeros((max(found, 1), 2), np.int32)
+        L.hmpo_stab_corners(_ptr(resp, C.c_float), w, h, self.threshold, _ptr(xy, C.c_int), found)
+        n = min(found, self.max_features) if self.max_features else found
+        if features is not None:
+            xy = np.ascontiguousarray(features, dtype=np.int32).reshape(-1, 2)
+            found = n = len(xy)
+            xy = xy if n else np.zeros((1, 2), np.int32)
+        flow = np.zeros((max(n, 1), 2), np.float32)
+        L.hmpo_stab_flow(_ptr(prev, C.c_float), _ptr(nxt, C.c_float), _ptr(xy, C.c_int), n, w, h, self.window,
+                         _ptr(flow, C.c_float))
+        dx, dy = C.c_float(), C.c_float()
+        L.hmpo_stab_mean(_ptr(flow, C.c_float), n, C.byref(dx), C.byref(dy))
+        out = np.zeros((h, w), np.float32)
+        L.hmpo_stab_warp(_ptr(nxt, C.c_float), w, h, dx.value, dy.value, _ptr(out, C.c_float))
+        return {"response": resp, "found": found, "corners": xy[:n], "flow": flow[:n], "dx": dx.value, "dy": dy.value,
+                "out": out}
