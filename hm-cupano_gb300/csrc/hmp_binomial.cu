@@ -12,11 +12,16 @@
 //
 // The 5-tap filter has a halo, so the box pyramid's tile-local level walk does not apply; the
 // pyramid is built level by level through HBM (L2-resident at these sizes):
-//   b5_down0   level 0 (gathered through the slot planes) -> G^1, 16x16 output tiles, halo in smem
+//   b5_down0   level 0 (gathered through the slot planes) -> G^1, 16x16 output tiles; the 35x35
+//              source tile of every image is staged in shared memory as stored (uint8), all its
+//              table lookups in flight together, then all its pixel fetches
 //   b5_down    G^l -> G^{l+1}
-//   b5_top     R^{L-1} = blend(G^{L-1})
-//   b5_up      R^l = up(R^{l+1}) + blend(G^l - up(G^{l+1}))         (l = L-2 .. 1)
+//   b5_up      R^l = up(R^{l+1}) + blend(G^l - up(G^{l+1}))         (l = L-1 .. 1; no up at L-1)
 //   b5_fine    level 0 of the write rect: blend(G^0 - up(G^1)) + up(R^1), packed into the canvas
+// b5_up and b5_fine work on 32x8 pixel blocks; the coarser-level pixels their expands read (19x7,
+// reflected at the borders) of every image and of R are staged in shared memory first. Every
+// launch after the first is a programmatic dependent of the one before (griddepcontrol.wait
+// before any global access), so a launch's CTAs are resident as its predecessor drains.
 // Arithmetic order follows the oracle term by term (this file is compiled with -fmad=false).
 #include "hmp_blend.cuh"
 
@@ -26,27 +31,38 @@ namespace {
 constexpr int kB5Tile = 16;                    // output tile edge of the down kernels
 constexpr int kB5Src = 2 * kB5Tile + 3;        // source tile edge: 2x-2 .. 2x+2 of 16 outputs
 constexpr int kB5SrcArea = kB5Src * kB5Src;
+constexpr int kB5Per = (kB5SrcArea + 255) / 256;  // source elements per thread
+constexpr int kUpW = 19, kUpH = 7;             // coarser-level taps of a 32x8 block (any parity)
+constexpr int kUpArea = kUpW * kUpH;
 
+__device__ __forceinline__ void b5_dep_wait() { asm volatile("griddepcontrol.wait;\n" ::: "memory"); }
+
+// Reflect-101 of coordinate m into [0, n). A tap an output reads is at most 2 outside, which
+// these steps settle (the second only for n == 2); staged tiles also hold elements past the
+// level's far edge that no output reads, and those are clamped into the level so that every load
+// stays inside the buffer.
 __device__ __forceinline__ int reflect101(int m, int n) {
   if (n == 1) return 0;
-  // Coordinates here are at most 2 outside [0, n), so this settles in at most two steps.
-  for (int it = 0; it < 4 && (m < 0 || m >= n); ++it) {
-    if (m < 0) m = -m;
-    if (m >= n) m = 2 * n - 2 - m;
-  }
-  return m;
+  if (m < 0) m = -m;
+  if (m >= n) m = 2 * n - 2 - m;
+  if (m < 0) m = -m;
+  return min(max(m, 0), n - 1);
 }
 
 // Down-filter output (ox, oy) of a source tile `t` whose element (p, q) is source pixel
 // (reflect(2*X0 - 2 + p), reflect(2*Y0 - 2 + q)); (tx, ty) = output position in the tile.
-__device__ __forceinline__ float4 down5(const float4* t, int tx, int ty, int ox, int oy, int iw, int ih) {
+__device__ __forceinline__ float4 tile_f4(const float4 v) { return v; }
+__device__ __forceinline__ float4 tile_f4(const uchar4 v) { return to_f4(v); }
+
+template <typename T>
+__device__ __forceinline__ float4 down5(const T* t, int tx, int ty, int ox, int oy, int iw, int ih) {
   const float k5[5] = {1.f, 4.f, 6.f, 4.f, 1.f};
   float sw = 0.f, s0 = 0.f, s1 = 0.f, s2 = 0.f;
 #pragma unroll
   for (int j = 0; j < 5; ++j)
 #pragma unroll
     for (int i = 0; i < 5; ++i) {
-      const float4 p = t[(2 * ty + j) * kB5Src + 2 * tx + i];
+      const float4 p = tile_f4(t[(2 * ty + j) * kB5Src + 2 * tx + i]);
       if (p.w == 0.f) continue;
       const float wgt = (k5[i] * k5[j]) / 256.f;
       sw += wgt;
@@ -60,7 +76,7 @@ __device__ __forceinline__ float4 down5(const float4* t, int tx, int ty, int ox,
 #pragma unroll
     for (int dx = 0; dx < 2; ++dx) {
       if (2 * ox + dx < iw && 2 * oy + dy < ih) {
-        const float a = t[(2 * ty + 2 + dy) * kB5Src + 2 * tx + 2 + dx].w;
+        const float a = tile_f4(t[(2 * ty + 2 + dy) * kB5Src + 2 * tx + 2 + dx]).w;
         if (a > amax) amax = a;
       }
     }
@@ -68,28 +84,28 @@ __device__ __forceinline__ float4 down5(const float4* t, int tx, int ty, int ox,
   return make_float4(0.f, 0.f, 0.f, amax);
 }
 
-// Burt-Adelson expand of a level buffer (lw x lh, frame base `low`) at high-res pixel (x, y).
-template <typename T>
-__device__ __forceinline__ float3 up5(const T* low, int lw, int lh, int x, int y) {
+// Burt-Adelson expand at high-res pixel (x, y) from a staged tile: element (u, v) of `t` is the
+// coarser-level pixel (reflect(U0 + u), reflect(V0 + v)).
+__device__ __forceinline__ float3 up5(const float4* t, int U0, int V0, int x, int y) {
   int tx[3], ty[3];
   float wx[3], wy[3];
   int nx, ny;
   if ((x & 1) == 0) {
     nx = 3;
-    tx[0] = reflect101(x / 2 - 1, lw), tx[1] = reflect101(x / 2, lw), tx[2] = reflect101(x / 2 + 1, lw);
+    tx[0] = (x >> 1) - 1 - U0, tx[1] = tx[0] + 1, tx[2] = tx[0] + 2;
     wx[0] = 1.f, wx[1] = 6.f, wx[2] = 1.f;
   } else {
     nx = 2;
-    tx[0] = reflect101((x - 1) / 2, lw), tx[1] = reflect101((x + 1) / 2, lw), tx[2] = 0;
+    tx[0] = (x >> 1) - U0, tx[1] = tx[0] + 1, tx[2] = tx[0];
     wx[0] = 4.f, wx[1] = 4.f, wx[2] = 0.f;
   }
   if ((y & 1) == 0) {
     ny = 3;
-    ty[0] = reflect101(y / 2 - 1, lh), ty[1] = reflect101(y / 2, lh), ty[2] = reflect101(y / 2 + 1, lh);
+    ty[0] = (y >> 1) - 1 - V0, ty[1] = ty[0] + 1, ty[2] = ty[0] + 2;
     wy[0] = 1.f, wy[1] = 6.f, wy[2] = 1.f;
   } else {
     ny = 2;
-    ty[0] = reflect101((y - 1) / 2, lh), ty[1] = reflect101((y + 1) / 2, lh), ty[2] = 0;
+    ty[0] = (y >> 1) - V0, ty[1] = ty[0] + 1, ty[2] = ty[0];
     wy[0] = 4.f, wy[1] = 4.f, wy[2] = 0.f;
   }
   float sw = 0.f, s0 = 0.f, s1 = 0.f, s2 = 0.f;
@@ -99,7 +115,7 @@ __device__ __forceinline__ float3 up5(const T* low, int lw, int lh, int x, int y
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
       if (i >= nx) break;
-      const float4 p = ldg_level(low + (long long)ty[j] * lw + tx[i]);
+      const float4 p = t[ty[j] * kUpW + tx[i]];
       if (p.w == 0.f) continue;
       const float wgt = (wx[i] * wy[j]) / 64.f;
       sw += wgt;
@@ -112,6 +128,16 @@ __device__ __forceinline__ float3 up5(const T* low, int lw, int lh, int x, int y
   return make_float3(0.f, 0.f, 0.f);
 }
 
+// Stages the coarser-level taps of the 32x8 block at (X0, Y0): element (u, v) = level buffer `low`
+// (lw x lh) at (reflect(U0 + u), reflect(V0 + v)), U0 = X0/2 - 1, V0 = Y0/2 - 1.
+template <typename T>
+__device__ __forceinline__ void stage_up(float4* t, const T* low, int lw, int lh, int U0, int V0) {
+  for (int i = threadIdx.y * 32 + threadIdx.x; i < kUpArea; i += 256) {
+    const int sx = reflect101(U0 + i % kUpW, lw), sy = reflect101(V0 + i / kUpW, lh);
+    t[i] = ldg_level(low + (long long)sy * lw + sx);
+  }
+}
+
 template <int NMAX, typename Store>
 __device__ __forceinline__ const Store* g_of(const PyrArgs& a, int k, int l, int b) {
   const void* p = a.G[0][l];
@@ -121,31 +147,53 @@ __device__ __forceinline__ const Store* g_of(const PyrArgs& a, int k, int l, int
   return static_cast<const Store*>(p) + (long long)b * a.lw[l] * a.lh[l];
 }
 
-// Level 0 -> G^1 for every slot: the source tile is gathered through the slot plane at
-// reflected level-0 coordinates.
+// Level 0 -> G^1 for every slot: the source tiles are gathered through the slot planes at
+// reflected level-0 coordinates, every image's together (the table lookups of all of them in
+// flight, then all the pixel fetches), and kept as stored.
 template <int NMAX, typename Store>
 __global__ void __launch_bounds__(256) b5_down0_kernel(const __grid_constant__ PyrArgs a) {
-  __shared__ float4 t[kB5SrcArea];
+  __shared__ uchar4 t[NMAX][kB5SrcArea];
+  constexpr int kGroup = NMAX <= 3 ? NMAX : 2;  // images whose loads are in flight together
+  b5_dep_wait();
   const int n = a.n, b = blockIdx.z, tid = threadIdx.x;
   const int X0 = blockIdx.x * kB5Tile, Y0 = blockIdx.y * kB5Tile;
   const int iw = a.lw[0], ih = a.lh[0], ow = a.lw[1], oh = a.lh[1];
   const int tx = tid % kB5Tile, ty = tid / kB5Tile, ox = X0 + tx, oy = Y0 + ty;
+  int sx[kB5Per], sy[kB5Per];
 #pragma unroll
-  for (int k = 0; k < NMAX; ++k) {
-    if (k >= n) break;
-    for (int i = tid; i < kB5SrcArea; i += 256) {
-      const int sx = reflect101(2 * X0 - 2 + i % kB5Src, iw), sy = reflect101(2 * Y0 - 2 + i / kB5Src, ih);
-      int own;
-      uint32_t ent;
-      slot_lookup(a.slot[k], k, sx, sy, own, ent);
-      t[i] = to_f4(slot_fetch<NMAX>(a, k, own, ent, b, a.opaque != 0));
-    }
-    __syncthreads();
-    if (ox < ow && oy < oh) {
+  for (int u = 0; u < kB5Per; ++u) {
+    const int i = min(tid + 256 * u, kB5SrcArea - 1);
+    sx[u] = reflect101(2 * X0 - 2 + i % kB5Src, iw);
+    sy[u] = reflect101(2 * Y0 - 2 + i / kB5Src, ih);
+  }
+#pragma unroll
+  for (int k0 = 0; k0 < NMAX; k0 += kGroup) {
+    if (k0 >= n) break;
+    int own[kGroup][kB5Per];
+    uint32_t ent[kGroup][kB5Per];
+#pragma unroll
+    for (int g = 0; g < kGroup; ++g)
+#pragma unroll
+      for (int u = 0; u < kB5Per; ++u) {
+        own[g][u] = 0xFF;
+        ent[g][u] = 0xFFFFFFFFu;
+        if (k0 + g < n && tid + 256 * u < kB5SrcArea) slot_lookup(a.slot[k0 + g], k0 + g, sx[u], sy[u], own[g][u], ent[g][u]);
+      }
+#pragma unroll
+    for (int g = 0; g < kGroup; ++g)
+#pragma unroll
+      for (int u = 0; u < kB5Per; ++u)
+        if (k0 + g < n && tid + 256 * u < kB5SrcArea)
+          t[k0 + g][tid + 256 * u] = slot_fetch<NMAX>(a, k0 + g, own[g][u], ent[g][u], b, a.opaque != 0);
+  }
+  __syncthreads();
+  if (ox < ow && oy < oh) {
+#pragma unroll
+    for (int k = 0; k < NMAX; ++k) {
+      if (k >= n) break;
       Store* G1 = static_cast<Store*>(a.G[k][1]) + (long long)b * ow * oh;
-      store_level(G1 + (long long)oy * ow + ox, down5(t, tx, ty, ox, oy, iw, ih));
+      store_level(G1 + (long long)oy * ow + ox, down5(t[k], tx, ty, ox, oy, iw, ih));
     }
-    __syncthreads();
   }
 }
 
@@ -153,6 +201,7 @@ __global__ void __launch_bounds__(256) b5_down0_kernel(const __grid_constant__ P
 template <int NMAX, typename Store>
 __global__ void __launch_bounds__(256) b5_down_kernel(const __grid_constant__ PyrArgs a, int l) {
   __shared__ float4 t[kB5SrcArea];
+  b5_dep_wait();
   const int n = a.n, b = blockIdx.z, tid = threadIdx.x;
   const int X0 = blockIdx.x * kB5Tile, Y0 = blockIdx.y * kB5Tile;
   const int iw = a.lw[l], ih = a.lh[l], ow = a.lw[l + 1], oh = a.lh[l + 1];
@@ -161,9 +210,13 @@ __global__ void __launch_bounds__(256) b5_down_kernel(const __grid_constant__ Py
   for (int k = 0; k < NMAX; ++k) {
     if (k >= n) break;
     const Store* src = static_cast<const Store*>(a.G[k][l]) + (long long)b * iw * ih;
-    for (int i = tid; i < kB5SrcArea; i += 256) {
-      const int sx = reflect101(2 * X0 - 2 + i % kB5Src, iw), sy = reflect101(2 * Y0 - 2 + i / kB5Src, ih);
-      t[i] = ldg_level(src + (long long)sy * iw + sx);
+#pragma unroll
+    for (int u = 0; u < kB5Per; ++u) {
+      const int i = tid + 256 * u;
+      if (i < kB5SrcArea) {
+        const int sx = reflect101(2 * X0 - 2 + i % kB5Src, iw), sy = reflect101(2 * Y0 - 2 + i / kB5Src, ih);
+        t[i] = ldg_level(src + (long long)sy * iw + sx);
+      }
     }
     __syncthreads();
     if (ox < ow && oy < oh) {
@@ -178,14 +231,26 @@ __global__ void __launch_bounds__(256) b5_down_kernel(const __grid_constant__ Py
 // weights are one-hot; G^l itself at the coarsest level) plus up(R^{l+1}).
 template <int RULE, int NMAX, typename Store>
 __global__ void __launch_bounds__(256) b5_up_kernel(const __grid_constant__ PyrArgs a, int l) {
+  __shared__ float4 tg[NMAX][kUpArea];  // G^{l+1} taps of every image
+  __shared__ float4 tr[kUpArea];        // R^{l+1} taps
+  b5_dep_wait();
   const int n = RULE == kRuleNway ? a.n : NMAX;
   const int K = RULE == kRuleTwo ? 1 : (RULE == kRuleThree ? 3 : a.K);
   const int b = blockIdx.z;
-  const int x = blockIdx.x * 32 + threadIdx.x, y = blockIdx.y * 8 + threadIdx.y;
+  const int X0 = blockIdx.x * 32, Y0 = blockIdx.y * 8;
+  const int x = X0 + threadIdx.x, y = Y0 + threadIdx.y;
   const int lw = a.lw[l], lh = a.lh[l];
-  if (x >= lw || y >= lh) return;
   const bool has_next = l + 1 < a.levels;
   const int lwn = a.lw[has_next ? l + 1 : l], lhn = a.lh[has_next ? l + 1 : l];
+  const int U0 = (X0 >> 1) - 1, V0 = (Y0 >> 1) - 1;
+  if (has_next) {
+#pragma unroll
+    for (int k = 0; k < NMAX; ++k)
+      if (k < n) stage_up(tg[k], g_of<NMAX, Store>(a, k, l + 1, b), lwn, lhn, U0, V0);
+    stage_up(tr, a.Rl[l + 1] + (long long)b * lwn * lhn, lwn, lhn, U0, V0);
+    __syncthreads();
+  }
+  if (x >= lw || y >= lh) return;
   const long long o = (long long)y * lw + x;
   float4 g[NMAX];
   float al[NMAX], m[NMAX];
@@ -203,7 +268,7 @@ __global__ void __launch_bounds__(256) b5_up_kernel(const __grid_constant__ PyrA
     for (int k = 1; k < NMAX; ++k)
       if (k == pk) v = g[k];
     if (has_next) {
-      const float3 up = up5(g_of<NMAX, Store>(a, pk, l + 1, b), lwn, lhn, x, y);
+      const float3 up = up5(tg[pk], U0, V0, x, y);
       v.x = v.x - up.x;
       v.y = v.y - up.y;
       v.z = v.z - up.z;
@@ -213,7 +278,7 @@ __global__ void __launch_bounds__(256) b5_up_kernel(const __grid_constant__ PyrA
 #pragma unroll
     for (int k = 0; k < NMAX; ++k) {
       if (k < n && has_next) {
-        const float3 up = up5(g_of<NMAX, Store>(a, k, l + 1, b), lwn, lhn, x, y);
+        const float3 up = up5(tg[k], U0, V0, x, y);
         g[k].x = g[k].x - up.x;
         g[k].y = g[k].y - up.y;
         g[k].z = g[k].z - up.z;
@@ -222,7 +287,7 @@ __global__ void __launch_bounds__(256) b5_up_kernel(const __grid_constant__ PyrA
     r = blend_level<RULE, NMAX>(n, g, m);
   }
   if (has_next) {
-    const float3 up = up5(a.Rl[l + 1] + (long long)b * lwn * lhn, lwn, lhn, x, y);
+    const float3 up = up5(tr, U0, V0, x, y);
     r.x = up.x + r.x;
     r.y = up.y + r.y;
     r.z = up.z + r.z;
@@ -234,11 +299,21 @@ __global__ void __launch_bounds__(256) b5_up_kernel(const __grid_constant__ PyrA
 // up(R^1), truncating pack into the canvas.
 template <int RULE, int NMAX, typename Store>
 __global__ void __launch_bounds__(256) b5_fine_kernel(const __grid_constant__ PyrArgs a) {
+  __shared__ float4 tg[NMAX][kUpArea];  // G^1 taps of every image
+  __shared__ float4 tr[kUpArea];        // R^1 taps
+  b5_dep_wait();
   const int n = RULE == kRuleNway ? a.n : NMAX;
   const int b = blockIdx.z;
-  const int x = a.wx0 + blockIdx.x * 32 + threadIdx.x, y = a.wy0 + blockIdx.y * 8 + threadIdx.y;
-  if (x >= a.wx1 || y >= a.wy1) return;
+  const int X0 = a.wx0 + blockIdx.x * 32, Y0 = a.wy0 + blockIdx.y * 8;
+  const int x = X0 + threadIdx.x, y = Y0 + threadIdx.y;
   const int lw1 = a.lw[1], lh1 = a.lh[1];
+  const int U0 = (X0 >> 1) - 1, V0 = (Y0 >> 1) - 1;
+#pragma unroll
+  for (int k = 0; k < NMAX; ++k)
+    if (k < n) stage_up(tg[k], g_of<NMAX, Store>(a, k, 1, b), lw1, lh1, U0, V0);
+  stage_up(tr, a.Rl[1] + (long long)b * lw1 * lh1, lw1, lh1, U0, V0);
+  __syncthreads();
+  if (x >= a.wx1 || y >= a.wy1) return;
   const int mv = int(__ldg(a.mask0 + (long long)y * a.mask0_pitch + x));
   uchar4 src[NMAX];
   float al[NMAX];
@@ -258,7 +333,7 @@ __global__ void __launch_bounds__(256) b5_fine_kernel(const __grid_constant__ Py
     for (int k = 1; k < NMAX; ++k)
       if (k == pk) s = src[k];
     float4 v = to_f4(s);
-    const float3 up = up5(g_of<NMAX, Store>(a, pk, 1, b), lw1, lh1, x, y);
+    const float3 up = up5(tg[pk], U0, V0, x, y);
     r = make_float4(v.x - up.x, v.y - up.y, v.z - up.z, blend_alpha<RULE, NMAX>(al, pk));
   } else if (pk == kPickAll) {
     float4 lap[NMAX];
@@ -266,7 +341,7 @@ __global__ void __launch_bounds__(256) b5_fine_kernel(const __grid_constant__ Py
     for (int k = 0; k < NMAX; ++k) {
       float4 v = to_f4(src[k]);
       if (k < n) {
-        const float3 up = up5(g_of<NMAX, Store>(a, k, 1, b), lw1, lh1, x, y);
+        const float3 up = up5(tg[k], U0, V0, x, y);
         v.x = v.x - up.x;
         v.y = v.y - up.y;
         v.z = v.z - up.z;
@@ -275,7 +350,7 @@ __global__ void __launch_bounds__(256) b5_fine_kernel(const __grid_constant__ Py
     }
     r = blend_level0<RULE, NMAX>(n, lap, mv);
   }
-  const float3 up = up5(a.Rl[1] + (long long)b * lw1 * lh1, lw1, lh1, x, y);
+  const float3 up = up5(tr, U0, V0, x, y);
   r.x = up.x + r.x;
   r.y = up.y + r.y;
   r.z = up.z + r.z;
@@ -284,21 +359,36 @@ __global__ void __launch_bounds__(256) b5_fine_kernel(const __grid_constant__ Py
   crow[x + a.cx_off] = pack_rgba(r);
 }
 
+// Launches `k` on `s`; with `pdl` as a programmatic dependent of the kernel before it.
+template <typename Kern, typename... Args>
+void b5_launch(Kern k, dim3 grid, dim3 block, bool pdl, cudaStream_t s, Args... args) {
+  cudaLaunchConfig_t cfg{};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = pdl ? 1 : 0;
+  cudaLaunchKernelEx(&cfg, k, args...);
+}
+
 template <int RULE, int NMAX, typename Store>
 cudaError_t b5_chain(const PyrArgs& a, int batch, cudaStream_t s) {
   const int L = a.levels;
   for (int l = 0; l + 1 < L; ++l) {
     const dim3 grid((a.lw[l + 1] + kB5Tile - 1) / kB5Tile, (a.lh[l + 1] + kB5Tile - 1) / kB5Tile, batch);
     if (l == 0)
-      b5_down0_kernel<NMAX, Store><<<grid, 256, 0, s>>>(a);
+      b5_launch(b5_down0_kernel<NMAX, Store>, grid, dim3(256), false, s, a);
     else
-      b5_down_kernel<NMAX, Store><<<grid, 256, 0, s>>>(a, l);
+      b5_launch(b5_down_kernel<NMAX, Store>, grid, dim3(256), true, s, a, l);
   }
   const dim3 blk(32, 8);
   for (int l = L - 1; l >= 1; --l)
-    b5_up_kernel<RULE, NMAX, Store><<<dim3((a.lw[l] + 31) / 32, (a.lh[l] + 7) / 8, batch), blk, 0, s>>>(a, l);
-  b5_fine_kernel<RULE, NMAX, Store>
-      <<<dim3((a.wx1 - a.wx0 + 31) / 32, (a.wy1 - a.wy0 + 7) / 8, batch), blk, 0, s>>>(a);
+    b5_launch(b5_up_kernel<RULE, NMAX, Store>, dim3((a.lw[l] + 31) / 32, (a.lh[l] + 7) / 8, batch), blk, true, s, a, l);
+  b5_launch(b5_fine_kernel<RULE, NMAX, Store>, dim3((a.wx1 - a.wx0 + 31) / 32, (a.wy1 - a.wy0 + 7) / 8, batch), blk,
+            true, s, a);
   return cudaGetLastError();
 }
 

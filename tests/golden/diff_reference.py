@@ -39,7 +39,9 @@ def main() -> int:
     ap.add_argument("--seed", type=int, default=1)
     ap.add_argument("--rigs", type=int, default=100)
     ap.add_argument("--max-images", type=int, default=5, help="images per rig: 2..max (at most 8)")
-    ap.add_argument("--reference", default=os.environ.get("HM_CUPANO_REFERENCE", "/root/reference"))
+    ap.add_argument("--reference", default=os.environ.get("HM_CUPANO_REFERENCE"),
+                    required="HM_CUPANO_REFERENCE" not in os.environ,
+                    help="the hm-cupano checkout (default: $HM_CUPANO_REFERENCE)")
     args = ap.parse_args()
     mg._install_stubs()
     sys.path.insert(0, args.reference)

@@ -208,7 +208,9 @@ def _known_answer_cases(cupano):
 
 def main() -> None:
     ap = argparse.ArgumentParser()
-    ap.add_argument("--reference", default=os.environ.get("HM_CUPANO_REFERENCE", "/root/reference"))
+    ap.add_argument("--reference", default=os.environ.get("HM_CUPANO_REFERENCE"),
+                    required="HM_CUPANO_REFERENCE" not in os.environ,
+                    help="the hm-cupano checkout (default: $HM_CUPANO_REFERENCE)")
     ap.add_argument("--out", default=str(HERE / "golden.npz"))
     args = ap.parse_args()
     _install_stubs()
