@@ -25,6 +25,10 @@ CASES = [
     ("pano3_2704x1520_to_6000x1800", 3, 4, 0.25, True, 1),
     ("panon8_2000x1500_to_9000x2400", 1, 5, 0.25, True, 1),
     ("panon8_2000x1500_to_9000x2400", 1, 2, 0.25, False, 1),
+    # 7 levels of small rigs: the coarsest levels are a few pixels across, narrower than the
+    # filter's staged tiles
+    ("pano2_1280x720_to_2200x800", 2, 7, 0.25, True, 1),
+    ("panon8_2000x1500_to_9000x2400", 1, 7, 0.125, True, 1),
 ]
 
 
