@@ -5,7 +5,8 @@
 // configuration id, device input frames and a device canvas. A dispatcher thread owns the GPU
 // side: it admits pending requests against the HBM budget (hmp_admission.h), keeps stitchers
 // resident per configuration (tables, seam, pyramid scratch), launches each admitted request on
-// a free stream slot, and watches the slots' completion events. Requests that arrive while others
+// a stream slot with room (each runs one request and holds the next queued behind it), and
+// watches the requests' completion events. Requests that arrive while others
 // are on the GPU start as soon as a slot and an instance are free, so their work overlaps on the
 // device. Latency = observed completion - submission, host steady clock.
 #include <cuda_runtime.h>
@@ -59,7 +60,12 @@ struct InFlight {
   Request req;
   int slot = -1;
   int instance = -1;
+  int event = -1;  // its completion event
 };
+
+// Requests a stream slot holds: one running and the next queued behind it on the same stream, so
+// that the slot's next request is already on the GPU when the running one completes.
+constexpr int kSlotDepth = 2;
 
 }  // namespace
 
@@ -70,8 +76,9 @@ struct hmp_server {
   std::vector<ConfigEntry> configs;
   std::vector<hmp_stitcher*> stitchers;  // indexed like the policy's instances
   std::vector<cudaStream_t> streams;
-  std::vector<cudaEvent_t> events;
-  std::vector<char> slot_busy;
+  std::vector<cudaEvent_t> events;  // kSlotDepth per slot
+  std::vector<char> event_busy;
+  std::vector<int> slot_count;      // requests in flight on the slot
 
   std::mutex mu;
   std::condition_variable cv_work, cv_done;
@@ -123,14 +130,15 @@ struct hmp_server {
     // Completions.
     const Clock::time_point now = Clock::now();
     for (size_t i = 0; i < inflight.size();) {
-      const cudaError_t q = cudaEventQuery(events[inflight[i].slot]);
+      const cudaError_t q = cudaEventQuery(events[inflight[i].event]);
       if (q == cudaErrorNotReady) {
         ++i;
         continue;
       }
       InFlight f = std::move(inflight[i]);
       inflight.erase(inflight.begin() + long(i));
-      slot_busy[f.slot] = 0;
+      --slot_count[f.slot];
+      event_busy[f.event] = 0;
       policy.release(f.instance);
       hmp_status s = q == cudaSuccess ? mk(HMP_OK, "") : mk(int(q), cudaGetErrorString(q));
       if (s.code == HMP_OK) s = hmp_stitcher_status(stitchers[f.instance]);
@@ -139,12 +147,9 @@ struct hmp_server {
     }
     // Admission, in arrival order, skipping requests that must wait.
     for (auto it = queue.begin(); it != queue.end();) {
-      int slot = -1;
-      for (size_t k = 0; k < slot_busy.size(); ++k)
-        if (!slot_busy[k]) {
-          slot = int(k);
-          break;
-        }
+      int slot = -1;  // the least loaded slot with room: an empty one first
+      for (size_t k = 0; k < slot_count.size(); ++k)
+        if (slot_count[k] < kSlotDepth && (slot < 0 || slot_count[k] < slot_count[slot])) slot = int(k);
       if (slot < 0) break;
       ConfigEntry& c = configs[it->config];
       if (c.bytes > policy.budget()) {
@@ -217,12 +222,16 @@ struct hmp_server {
         worked = true;
         continue;
       }
-      cudaEventRecord(events[slot], streams[slot]);
-      slot_busy[slot] = 1;
+      int ev = slot * kSlotDepth;
+      while (event_busy[ev]) ++ev;  // the slot has fewer than kSlotDepth requests in flight
+      cudaEventRecord(events[ev], streams[slot]);
+      event_busy[ev] = 1;
+      ++slot_count[slot];
       InFlight f;
       f.req = std::move(*it);
       f.slot = slot;
       f.instance = inst;
+      f.event = ev;
       inflight.push_back(std::move(f));
       it = queue.erase(it);
       worked = true;
@@ -244,11 +253,17 @@ struct hmp_server {
       std::unique_lock<std::mutex> lk(mu);
       if (stop && pending.empty() && queue.empty() && inflight.empty()) break;
       if (!worked) {
-        // Idle or waiting on the GPU: poll in-flight events every 20 us, else sleep until work.
-        if (inflight.empty() && pending.empty() && queue.empty())
+        // Idle: sleep until work arrives. Waiting on the GPU: poll the in-flight events again
+        // after yielding the core, not after a timed sleep (a 20 us wait sleeps 50 us or more
+        // with the kernel's timer slack, and every slot that drains meanwhile idles the GPU).
+        if (inflight.empty() && pending.empty() && queue.empty()) {
           cv_work.wait_for(lk, std::chrono::milliseconds(5));
-        else
+        } else if (!inflight.empty()) {
+          lk.unlock();
+          std::this_thread::yield();
+        } else {
           cv_work.wait_for(lk, std::chrono::microseconds(20));
+        }
       }
     }
   }
@@ -281,16 +296,18 @@ HMP_API hmp_status hmp_server_create(const hmp_server_options* opt, hmp_server**
     e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
     if (e != cudaSuccess) break;
     s->streams.push_back(st);
-    e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
-    if (e != cudaSuccess) break;
-    s->events.push_back(ev);
+    for (int d = 0; d < kSlotDepth && e == cudaSuccess; ++d) {
+      e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
+      if (e == cudaSuccess) s->events.push_back(ev);
+    }
   }
   if (e != cudaSuccess) {
     const hmp_status r = mk(int(e), cudaGetErrorString(e));
     delete s;
     return r;
   }
-  s->slot_busy.assign(opt->slots, 0);
+  s->slot_count.assign(opt->slots, 0);
+  s->event_busy.assign(size_t(opt->slots) * kSlotDepth, 0);
   s->worker = std::thread([s] { s->run(); });
   *out = s;
   return mk(HMP_OK, "");

@@ -22,6 +22,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdint>
 #include <cstdio>
 #include <new>
 
@@ -205,19 +206,143 @@ __global__ void __launch_bounds__(256) flow_kernel(const float* __restrict__ pre
   flow[f] = make_float2(dx, dy);
 }
 
-// The global motion: the flow summed in feature order (as the reference's host loop), its mean and
-// the rounded translation.
-__global__ void motion_kernel(const float2* flow, int cap, Motion* m) {
-  const int n = min(m->corners, cap);
-  float sx = 0.f, sy = 0.f;
-  for (int f = 0; f < n; ++f) {
-    sx += flow[f].x;
-    sy += flow[f].y;
+// Lucas-Kanade per feature for the reference's default 15-pixel window, the same taps and sums in
+// the same order as flow_kernel, loaded by rows: a row of the window is a few aligned 16-byte
+// chunks (frames 16-byte aligned, checked on the host) instead of one 4-byte load per value, and
+// the three rows of `prev` the gradients read slide down the window in registers. A warp's
+// features sit at scattered places, so each load instruction touches about one cache line per
+// lane; loading four values per instruction cuts those wavefronts about five-fold.
+// v[c] = frame[L + c] for c < N (0 outside [0, total)).
+template <int N>
+__device__ __forceinline__ void load_row(const float* __restrict__ frame, long long total, long long L, float (&v)[N]) {
+  constexpr int NC = (N + 6) / 4;  // chunks covering an offset of up to 3 plus N values
+  const long long a0 = L & ~3LL;
+  const int off = int(L - a0);
+  float c4[NC * 4];
+#pragma unroll
+  for (int k = 0; k < NC; ++k) {
+    const long long c = a0 + 4 * k;
+    if (c >= 0 && c + 3 < total) {
+      const float4 q = __ldg(reinterpret_cast<const float4*>(frame + c));
+      c4[4 * k] = q.x, c4[4 * k + 1] = q.y, c4[4 * k + 2] = q.z, c4[4 * k + 3] = q.w;
+    } else {
+#pragma unroll
+      for (int e = 0; e < 4; ++e) c4[4 * k + e] = (c + e >= 0 && c + e < total) ? __ldg(frame + c + e) : 0.f;
+    }
   }
-  m->dx = n > 0 ? sx / float(n) : 0.f;
-  m->dy = n > 0 ? sy / float(n) : 0.f;
-  m->sx = shift_of(m->dx);
-  m->sy = shift_of(m->dy);
+#pragma unroll
+  for (int c = 0; c < N; ++c)
+    v[c] = off == 0 ? c4[c] : off == 1 ? c4[c + 1] : off == 2 ? c4[c + 2] : c4[c + 3];
+}
+
+template <int W>
+__global__ void __launch_bounds__(256) flow_rows_kernel(const float* __restrict__ prev, const float* __restrict__ next,
+                                                        const int2* xy, const Motion* m, int cap, int w, int h,
+                                                        float2* flow) {
+  constexpr int HALF = W / 2;
+  const int f = blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= min(m->corners, cap)) return;
+  const int2 p = xy[f];
+  const long long total = (long long)w * h;
+  float dx = 0.f, dy = 0.f;
+  for (int iter = 0; iter < 10; ++iter) {
+    float sxx = 0.f, syy = 0.f, sxy = 0.f, stx = 0.f, sty = 0.f;
+    const int rdx = shift_of(dx), rdy = shift_of(dy);
+    // up, mid, dn: prev rows y-1, y, y+1 at columns p.x - HALF - 1 .. p.x + HALF + 1
+    float up[W + 2], mid[W + 2], dn[W + 2];
+    load_row(prev, total, (long long)(p.y - HALF - 1) * w + (p.x - HALF - 1), up);
+    load_row(prev, total, (long long)(p.y - HALF) * w + (p.x - HALF - 1), mid);
+    for (int j = -HALF; j <= HALF; ++j) {
+      const int y = p.y + j, yn = y + rdy;
+      load_row(prev, total, (long long)(y + 1) * w + (p.x - HALF - 1), dn);
+      float nx[W];  // next row yn at columns p.x + rdx - HALF ..
+      load_row(next, total, (long long)yn * w + (p.x + rdx - HALF), nx);
+      const bool row_ok = y >= 1 && y < h - 1 && yn >= 0 && yn < h - 1;
+#pragma unroll
+      for (int i = 0; i < W; ++i) {
+        const int x = p.x - HALF + i, xn = x + rdx;
+        if (!row_ok || x < 1 || x >= w - 1 || xn < 0 || xn >= w - 1) continue;
+        const float ix = (mid[i + 2] - mid[i]) * 0.5f;
+        const float iy = (dn[i + 1] - up[i + 1]) * 0.5f;
+        const float it = nx[i] - mid[i + 1];
+        sxx += ix * ix;
+        syy += iy * iy;
+        sxy += ix * iy;
+        stx += ix * it;
+        sty += iy * it;
+      }
+#pragma unroll
+      for (int c = 0; c < W + 2; ++c) {
+        up[c] = mid[c];
+        mid[c] = dn[c];
+      }
+    }
+    const float det = sxx * syy - sxy * sxy;
+    if (fabsf(det) < 1e-6f) break;
+    const float ddx = (-syy * stx + sxy * sty) / det;
+    const float ddy = (sxy * stx - sxx * sty) / det;
+    dx += ddx;
+    dy += ddy;
+    if (sqrtf(ddx * ddx + ddy * ddy) < 0.01f) break;
+  }
+  flow[f] = make_float2(dx, dy);
+}
+
+// The global motion: the flow summed in feature order (as the reference's host loop), its mean and
+// the rounded translation. The sum is one dependent chain of additions, so one thread makes it;
+// the CTA's other threads stage the flow in shared memory ahead of it (double-buffered chunks,
+// coalesced), so that the chain waits on shared-memory loads, not on global-memory latency.
+constexpr int kMotionThreads = 1024, kMotionChunk = 2048;  // 2 x 16 KB of float2
+
+__global__ void __launch_bounds__(kMotionThreads) motion_kernel(const float2* __restrict__ flow, int cap, Motion* m) {
+  __shared__ float4 buf[2][kMotionChunk / 2];  // float2 pairs
+  const int n = min(m->corners, cap);
+  const int chunks = (n + kMotionChunk - 1) / kMotionChunk;
+  const float4* f4 = reinterpret_cast<const float4*>(flow);  // flow is 16-byte aligned (cudaMalloc)
+  const auto stage = [&](int c) {
+    const int base = c * kMotionChunk;
+    for (int i = threadIdx.x; i < kMotionChunk / 2; i += kMotionThreads) {
+      const int e = base + 2 * i;  // feature index of the pair's first element
+      float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (e + 1 < n) {
+        v = __ldg(f4 + (e >> 1));
+      } else if (e < n) {
+        const float2 q = __ldg(flow + e);
+        v.x = q.x, v.y = q.y;
+      }
+      buf[c & 1][i] = v;
+    }
+  };
+  float sx = 0.f, sy = 0.f;
+  if (chunks > 0) stage(0);
+  __syncthreads();
+  for (int c = 0; c < chunks; ++c) {
+    if (c + 1 < chunks) stage(c + 1);
+    if (threadIdx.x == 0) {
+      const int cnt = min(kMotionChunk, n - c * kMotionChunk);
+      const float4* b = buf[c & 1];
+      int i = 0;
+#pragma unroll 8
+      for (; 2 * i + 1 < cnt; ++i) {
+        const float4 v = b[i];
+        sx += v.x;
+        sy += v.y;
+        sx += v.z;
+        sy += v.w;
+      }
+      if (2 * i < cnt) {
+        sx += b[i].x;
+        sy += b[i].y;
+      }
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    m->dx = n > 0 ? sx / float(n) : 0.f;
+    m->dy = n > 0 ? sy / float(n) : 0.f;
+    m->sx = shift_of(m->dx);
+    m->sy = shift_of(m->dy);
+  }
 }
 
 __global__ void __launch_bounds__(256) warp_kernel(const float* __restrict__ in, float* __restrict__ out, int w, int h,
@@ -330,9 +455,13 @@ HMP_API hmp_status hmp_stabilizer_flow(hmp_stabilizer* st, const float* prev, co
   if (s.code) return s;
   if (window_size < 1 || window_size > 255) return status_of(HMP_ERR_INVALID_VALUE, "window_size must be in 1..255");
   const cudaStream_t cs = static_cast<cudaStream_t>(stream);
-  flow_kernel<<<(std::max(st->cap, 1) + 255) / 256, 256, 0, cs>>>(prev, next, st->xy, st->motion, st->cap, st->w,
-                                                                   st->h, window_size, st->flow);
-  motion_kernel<<<1, 1, 0, cs>>>(st->flow, st->cap, st->motion);
+  const unsigned blocks = unsigned((std::max(st->cap, 1) + 255) / 256);
+  const bool aligned = ((reinterpret_cast<uintptr_t>(prev) | reinterpret_cast<uintptr_t>(next)) & 15u) == 0;
+  if (window_size == 15 && aligned)
+    flow_rows_kernel<15><<<blocks, 256, 0, cs>>>(prev, next, st->xy, st->motion, st->cap, st->w, st->h, st->flow);
+  else
+    flow_kernel<<<blocks, 256, 0, cs>>>(prev, next, st->xy, st->motion, st->cap, st->w, st->h, window_size, st->flow);
+  motion_kernel<<<1, kMotionThreads, 0, cs>>>(st->flow, st->cap, st->motion);
   const cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? status_of(HMP_OK, "") : cuda_failure(e, "flow launch");
 }

@@ -333,7 +333,7 @@ typedef struct hmp_server hmp_server;
 
 typedef struct hmp_server_options {
   size_t hbm_budget_bytes;      /* device bytes resident stitchers may hold together */
-  int slots;                    /* requests on the GPU at once, one stream each (1..64) */
+  int slots;                    /* streams (1..64): each runs one request and queues the next */
   int max_instances_per_config; /* resident stitchers per configuration (one request each at a time) */
 } hmp_server_options;
 

@@ -178,3 +178,22 @@ def test_graph_capture_replays_identically(oracle_lib):
     g.replay()
     torch.cuda.synchronize()
     _check(st, oracle_lib.Stabilize().run(prev2, nxt2), out)
+
+
+def test_unaligned_frames(oracle_lib):
+    """Frames 4 bytes off a 16-byte boundary take the scalar flow kernel; the result is the same."""
+    import torch
+
+    import hmpano
+
+    h, w = 90, 130
+    prev, nxt = moving_pair(h, w, (2, 1), seed=31)
+    ref = oracle_lib.Stabilize().run(prev, nxt)
+    bufs = [torch.zeros(h * w + 1, dtype=torch.float32, device="cuda") for _ in range(3)]
+    p, n, out = (b[1:].view(h, w) for b in bufs)
+    p.copy_(_dev(prev))
+    n.copy_(_dev(nxt))
+    assert p.data_ptr() % 16 == 4
+    st = hmpano.Stabilizer(w, h)
+    st.run(p, n, out)
+    _check(st, ref, out)
