@@ -253,16 +253,7 @@ __global__ void __launch_bounds__(kSegPixels) resolve_plane_kernel(const __grid_
   if (in) res[(long long)y * raw.map_pitch + x] = (s_code != kSegMixed && r < kOffSkip) ? (r & kOffMask) : r;
 }
 
-// Copy-block mode: clears the alpha flag at the start of a call. A kernel rather than a memset,
-// which the driver may queue on a copy engine behind the caller's host transfers.
-__global__ void flag_reset_kernel(int* flag) { *flag = 0; }
-
 }  // namespace
-
-cudaError_t launch_flag_reset(int* flag, cudaStream_t stream) {
-  flag_reset_kernel<<<1, 1, 0, stream>>>(flag);
-  return cudaGetLastError();
-}
 
 cudaError_t launch_resolve_plane(const PlaneDev& raw, uint32_t* res, uint8_t* seg_owner, int seg_pitch, const SrcSet& S,
                                  int n, bool opaque, const SkipMap& skip, cudaStream_t stream) {

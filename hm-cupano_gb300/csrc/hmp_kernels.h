@@ -69,10 +69,12 @@ struct PyrArgs {
   int* alpha_flag;
   const uint8_t* support_mark;
   int sm_pitch, sm_shift;
-  // Fallback launches: every CTA returns at once unless *gate != 0 (a copy block's source pixels
+  // Fallback launches: every CTA returns at once unless gate[0] != 0 (a copy block's source pixels
   // held alpha 0, so the whole write rect is recomputed); then the launch's CTAs walk the dense
-  // grid of fb_nx x fb_ny tiles of fb_batch frames with a grid stride. nullptr: no gate.
-  const int* gate;
+  // grid of fb_nx x fb_ny tiles of fb_batch frames with a grid stride, and the last CTA of the
+  // last fallback launch (pyr_fine's) to finish clears gate[0] (gate[1] counts them), so the flag
+  // is 0 again when the next call's kernels start. nullptr: no gate.
+  int* gate;
   int fb_nx, fb_ny, fb_batch;
   CanvasDev C;
   int wx0, wy0, wx1, wy1;  // write rect, blend coordinates, end exclusive
@@ -134,8 +136,6 @@ cudaError_t launch_resolve_plane(const PlaneDev& raw, uint32_t* res, uint8_t* se
 
 // copy_blocks: the plane holds copy-block skips (kOffSkip) or the call checks source alpha.
 cudaError_t launch_canvas_gather(const GatherArgs& a, bool copy_blocks, cudaStream_t stream);
-// Copy-block mode: zeroes the alpha flag (one thread).
-cudaError_t launch_flag_reset(int* flag, cudaStream_t stream);
 
 // Gaussian levels 1..L-1 of every slot; grid = tiles over the blend region x batch.
 cudaError_t launch_pyr_down(const PyrArgs& a, int storage, dim3 grid, cudaStream_t stream);

@@ -101,6 +101,27 @@ __device__ __forceinline__ Store* level_of(const PyrArgs& a, int k, int l, int b
 // kernel has completed and its writes are visible (at once after a normal launch).
 __device__ __forceinline__ void grid_dep_wait() { asm volatile("griddepcontrol.wait;\n" ::: "memory"); }
 
+// The gated fallback launches (copy-block mode) let their dependents start at once: a fallback CTA
+// whose gate is clear only reads it and returns, so the next fallback launch need not wait for the
+// previous one to drain before its own CTAs are placed (they wait for its results, if any, with
+// grid_dep_wait). Only the walking instantiations do this.
+__device__ __forceinline__ void grid_dep_launch() { asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory"); }
+
+// The last fallback launch (pyr_fine's), when its gate was set: every CTA counts itself out once it
+// is done walking, and the last one clears the gate and the count, so that the flag is 0 when the
+// next call's kernels start. Nothing waits: a CTA counts and returns.
+__device__ __forceinline__ void walk_done(const PyrArgs& a) {
+  if (threadIdx.x != 0) return;
+  volatile int* g = a.gate;
+  if (g[0] == 0) return;
+  __threadfence();
+  if (atomicAdd(a.gate + 1, 1) == int(gridDim.x * gridDim.y * gridDim.z) - 1) {
+    g[1] = 0;
+    g[0] = 0;
+    __threadfence();
+  }
+}
+
 // pyr_down in copy-block mode: bit 31 of a listed tile says whether pyr_fine reads the tile's kept
 // level-0 pixels (the tile meets a pyramid block); other listed tiles feed only coarser levels.
 // Dense and walking launches keep every tile's.
@@ -166,6 +187,7 @@ template <int NMAX, typename Store, int TD, bool kListed = false, bool kWalk = f
 __global__ void __launch_bounds__(256) pyr_down_kernel(const __grid_constant__ PyrArgs a) {
   extern __shared__ float4 sm[];
   // One tile, or (kWalk: the gated fallback) a grid-stride walk over the dense tiles.
+  if constexpr (kWalk) grid_dep_launch();
   for (int w = 0;; ++w) {
     int tx, ty, b;
     if (!cta_tile<(NMAX >= 3 || kListed), kWalk>(a, w, tx, ty, b)) return;
@@ -362,6 +384,7 @@ template <typename Store, int TD, bool kWalk = false>
 __global__ void __launch_bounds__(256) pyr_down_n_kernel(const __grid_constant__ PyrArgs a) {
   extern __shared__ float4 sm[];
   // One tile, or (kWalk: the gated fallback) a grid-stride walk over the dense tiles.
+  if constexpr (kWalk) grid_dep_launch();
   for (int w = 0;; ++w) {
     int tx, ty, b;
     if (!cta_tile<true, kWalk>(a, w, tx, ty, b)) return;
@@ -562,6 +585,7 @@ template <int RULE, int NMAX, typename Store, int T1, bool kListed = false, bool
 __global__ void __launch_bounds__(256) pyr_coarse_kernel(const __grid_constant__ PyrArgs a) {
   extern __shared__ float4 sm[];
   // One tile, or (kWalk: the gated fallback) a grid-stride walk over the dense tiles.
+  if constexpr (kWalk) grid_dep_launch();
   for (int w = 0;; ++w) {
     int tx, ty, b;
     if (!cta_tile<(RULE != kRuleTwo || kListed), kWalk>(a, w, tx, ty, b)) return;
@@ -787,6 +811,7 @@ template <typename Store, int T1, bool kWalk = false>
 __global__ void __launch_bounds__(256) pyr_coarse_n_kernel(const __grid_constant__ PyrArgs a) {
   extern __shared__ float4 sm[];
   // One tile, or (kWalk: the gated fallback) a grid-stride walk over the dense tiles.
+  if constexpr (kWalk) grid_dep_launch();
   for (int w = 0;; ++w) {
     int tx, ty, b;
     if (!cta_tile<true, kWalk>(a, w, tx, ty, b)) return;
@@ -996,9 +1021,13 @@ template <int RULE, int NMAX, typename Store, bool P0M, bool kListed = false, bo
 __global__ void __launch_bounds__(256) pyr_fine_kernel(const __grid_constant__ PyrArgs a) {
   extern __shared__ float4 fsm[];  // R^1 tile, then G^1 tiles of slots 0..n-1 (Store)
   // One tile, or (kWalk: the gated fallback) a grid-stride walk over the dense tiles.
+  if constexpr (kWalk) grid_dep_launch();
   for (int w = 0;; ++w) {
     int tx, ty, b;
-    if (!cta_tile<(RULE != kRuleTwo || kListed), kWalk>(a, w, tx, ty, b)) return;
+    if (!cta_tile<(RULE != kRuleTwo || kListed), kWalk>(a, w, tx, ty, b)) {
+      if constexpr (kWalk) walk_done(a);
+      return;
+    }
     if (kWalk && w) __syncthreads();  // the previous tile is done with shared memory
     const int n = RULE == kRuleNway ? a.n : NMAX;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -1167,9 +1196,13 @@ template <typename Store, bool kWalk = false>
 __global__ void __launch_bounds__(256) pyr_fine_n_kernel(const __grid_constant__ PyrArgs a) {
   extern __shared__ float4 fsm[];
   // One tile, or (kWalk: the gated fallback) a grid-stride walk over the dense tiles.
+  if constexpr (kWalk) grid_dep_launch();
   for (int w = 0;; ++w) {
     int tx, ty, b;
-    if (!cta_tile<true, kWalk>(a, w, tx, ty, b)) return;
+    if (!cta_tile<true, kWalk>(a, w, tx, ty, b)) {
+      if constexpr (kWalk) walk_done(a);
+      return;
+    }
     if (kWalk && w) __syncthreads();  // the previous tile is done with shared memory
     grid_dep_wait();  // R^1 of pyr_coarse; G^1 and level 0 of pyr_down
     const int n = a.n, cap = a.fine_cap;

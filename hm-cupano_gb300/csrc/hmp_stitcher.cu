@@ -527,10 +527,11 @@ struct hmp_stitcher {
     // The pyramid-block map, then the flag (4-byte aligned; allocations are 256-byte aligned).
     const size_t flag_off = (c.pyramid_block.size() + 3) / 4 * 4;
     void* m = nullptr;
-    if (e == cudaSuccess) e = alloc(&m, flag_off + sizeof(int));
+    if (e == cudaSuccess) e = alloc(&m, flag_off + 2 * sizeof(int));
     if (e == cudaSuccess)
       e = cudaMemcpy(m, c.pyramid_block.data(), c.pyramid_block.size(), cudaMemcpyHostToDevice);
-    if (e == cudaSuccess) e = cudaMemset(static_cast<char*>(m) + flag_off, 0, sizeof(int));
+    // The flag and the fallback's CTA count start at 0; the fallback clears both whenever it ran.
+    if (e == cudaSuccess) e = cudaMemset(static_cast<char*>(m) + flag_off, 0, 2 * sizeof(int));
     if (e != cudaSuccess) return cuda_status(e, "copy-block upload");
     n_fine = int(c.fine_list.size());
     n_coarse = int(c.coarse_list.size());
@@ -567,7 +568,7 @@ struct hmp_stitcher {
   // Kernels one process() launches in copy-block mode: the flag reset, the listed pyramid kernels,
   // the gather and the three gated fallbacks.
   int copy_launches() const {
-    return 1 + (n_down[tile_down == 64 ? 1 : 0] > 0) + (n_coarse > 0) + (n_fine > 0) + 1 + 3;
+    return (n_down[tile_down == 64 ? 1 : 0] > 0) + (n_coarse > 0) + (n_fine > 0) + 1 + 3;
   }
 
   // Compulsory bytes per process(): outside the write rect, 4 (table) + 1 (seam) + a source and
@@ -973,10 +974,6 @@ struct hmp_stitcher {
       if (timing && tnext < kTimingSlots) ++tnext;
       if (e != cudaSuccess) return cuda_status(e, "canvas_gather launch");
       return ok_status();
-    }
-    if (copy) {
-      e = hmp::launch_flag_reset(alpha_flag, s);
-      if (e != cudaSuccess) return cuda_status(e, "copy-block flag reset");
     }
     // Fork: the pyramid goes to the high-priority stream `aux` when the canvas gather also
     // runs; the gather is launched on the caller stream after the pyramid kernels.
