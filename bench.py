@@ -548,9 +548,9 @@ def main() -> None:
         "kernel_ms": {k: round(v[0] / max(v[1], 1), 5) for k, v in ktimes.items()},
         "kernel_ms_serialized": {k: round(v[0] / max(v[1], 1), 5) for k, v in ktimes_serial.items()},
         # Kernels launched in the headline timed region (every rank): each process() launches
-        # exactly launches_per_process of this library's kernels (here 7: pyr_down, pyr_coarse,
-        # pyr_fine over their work lists, canvas_gather, and the three gated fallbacks, which
-        # return at once unless a copy block's source alpha was 0).
+        # exactly launches_per_process of this library's kernels (here 5: pyr_down, pyr_coarse,
+        # pyr_fine over their work lists, canvas_gather, and the copy-block fallback's one-thread
+        # gate, which returns at once unless a copy block's source alpha was 0).
         "gpu_launches": world * args.steps * int(info["launches_per_process"]),
         "e2e": e2e,
         "clocks": dict(sampler.summary(), window_s=round(t_region1 - t_region0, 3),

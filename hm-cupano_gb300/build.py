@@ -38,8 +38,13 @@ UNITS = {
     "hmp_generic.cu": ["-fmad=false"],
     "hmp_batch.cpp": [],
     "hmp_stabilize.cu": ["-fmad=false"],
+    # Device-side (tail) launches need relocatable device code; only this unit has it, since it
+    # raises the pyramid kernels' registers (it holds its own copies of them for the fallback).
+    "hmp_fallback.cu": ["-fmad=false", "-rdc=true"],
 }
-HEADERS = ["hmp_plan.h", "hmp_copyplan.h", "hmp_device.cuh", "hmp_kernels.h", "hmp_blend.cuh", "hmp_admission.h"]
+RDC_UNITS = [u for u, extra in UNITS.items() if "-rdc=true" in extra]
+HEADERS = ["hmp_plan.h", "hmp_copyplan.h", "hmp_device.cuh", "hmp_kernels.h", "hmp_blend.cuh", "hmp_admission.h",
+           "hmp_pyramid_kernels.cuh"]
 
 
 def nvcc() -> str:
@@ -87,8 +92,16 @@ def build(force: bool = False, verbose: bool = False) -> Path:
         raise RuntimeError(f"nvcc failed for {[u for u, _ in failed]}")
     objs = [str(BUILD / (u + ".o")) for u in UNITS]
     if jobs or force or not LIB.exists():
+        # Device link of the relocatable units (with the device runtime), then the shared library.
+        dlink = str(BUILD / "device_link.o")
+        cmd = [cc, *ARCH, "-Xcompiler", "-fPIC", "-dlink", "-o", dlink,
+               *[str(BUILD / (u + ".o")) for u in RDC_UNITS], "-lcudadevrt"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            print(r.stderr, file=sys.stderr)
+            raise RuntimeError("device link failed")
         tmp = str(LIB) + ".tmp"
-        cmd = [cc, *ARCH, "-shared", "-o", tmp, *objs]
+        cmd = [cc, *ARCH, "-shared", "-o", tmp, *objs, dlink, "-lcudadevrt"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             print(r.stderr, file=sys.stderr)

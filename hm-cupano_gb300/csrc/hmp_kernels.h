@@ -120,6 +120,12 @@ int generic_launches(int levels, bool canvas);
 
 // One-time attribute setup (dynamic shared memory limits). Call before capture.
 cudaError_t kernels_init();
+// Copy-block fallback (hmp_fallback.cu): one single-thread launch after the frame's other kernels;
+// when the alpha flag (a.gate[0]) is set it clears it and tail-launches the dense pyramid chain
+// over the given dense grids. fallback_init sets the shared-memory limits of its kernels.
+cudaError_t fallback_init();
+cudaError_t launch_fallback_gate(const PyrArgs& a, int rule, int storage, int tile_down, int tile_coarse, dim3 down,
+                                 dim3 coarse, dim3 fine, size_t coarse_smem, cudaStream_t stream);
 
 // Resolves a plane's packed entries (raw.map) into offsets for the frames S (res: raw's layout).
 // opaque: the soft-seam rule for entries outside their source.

@@ -160,7 +160,7 @@ struct hmp_stitcher {
   int copy_blocks = 0, empty_blocks = 0, pyramid_blocks = 0;
   long long pyramid_pixels = 0;
   cudaStream_t aux = nullptr;
-  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_gather = nullptr;
   double m0_bytes = 0;
   int launches = 0;
   hmp::SrcSet last_src{};  // frames of the last process(), for the pyramid dump
@@ -183,6 +183,7 @@ struct hmp_stitcher {
     for (cudaEvent_t e : tev) cudaEventDestroy(e);
     if (ev_fork) cudaEventDestroy(ev_fork);
     if (ev_join) cudaEventDestroy(ev_join);
+    if (ev_gather) cudaEventDestroy(ev_gather);
     if (aux) cudaStreamDestroy(aux);
     for (void* p : allocations) cudaFree(p);
   }
@@ -475,6 +476,7 @@ struct hmp_stitcher {
       e = cudaStreamCreateWithPriority(&aux, cudaStreamNonBlocking, greatest);
       if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming);
       if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev_join, cudaEventDisableTiming);
+      if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev_gather, cudaEventDisableTiming);
       if (e != cudaSuccess) return cuda_status(e, "stream setup");
     }
     // The uploads and clears ran on the legacy default stream; wait for them only, so that a
@@ -568,7 +570,7 @@ struct hmp_stitcher {
   // Kernels one process() launches in copy-block mode: the flag reset, the listed pyramid kernels,
   // the gather and the three gated fallbacks.
   int copy_launches() const {
-    return (n_down[tile_down == 64 ? 1 : 0] > 0) + (n_coarse > 0) + (n_fine > 0) + 1 + 3;
+    return (n_down[tile_down == 64 ? 1 : 0] > 0) + (n_coarse > 0) + (n_fine > 0) + 1 + 1;
   }
 
   // Compulsory bytes per process(): outside the write rect, 4 (table) + 1 (seam) + a source and
@@ -1077,24 +1079,46 @@ struct hmp_stitcher {
     }
     hmp_status cst = chain(a, copy, ps, true);
     if (cst.code != HMP_OK) return cst;
+    // Copy-block fallback, after the gather wrote the copy blocks: it recomputes the whole write
+    // rect densely if a copy block's source pixels held alpha 0, and clears the flag. Outside a
+    // stream capture it is one thread (hmp_fallback.cu) that returns at once unless the flag is
+    // set, then tail-launches the dense chain; with the gather forked it runs on the pyramid
+    // stream after pyr_fine and the gather, so the caller stream's join follows it directly.
+    // In a CUDA graph the gate's device-side launches did not run (the graph replay test of copy
+    // blocks on alpha-0 frames caught it), so a captured call keeps three gated launches whose
+    // CTAs walk the dense tiles when the flag is set; the last one clears it.
+    cudaStreamCaptureStatus capture = cudaStreamCaptureStatusNone;
+    if (copy) {
+      e = cudaStreamIsCapturing(s, &capture);
+      if (e != cudaSuccess) return failed(e, "stream capture query");
+    }
+    const bool gate = copy && capture == cudaStreamCaptureStatusNone;
+    hmp::PyrArgs f = a;
+    f.gate = alpha_flag;
     if (gather) {
       tbegin(0, s);
       e = hmp::launch_canvas_gather(ga, copy_plan, s);
       tend(0, s);
       if (e != cudaSuccess) return failed(e, "canvas_gather launch");
     }
+    if (gate && fork) {
+      e = cudaEventRecord(ev_gather, s);
+      if (e == cudaSuccess) e = cudaStreamWaitEvent(aux, ev_gather, 0);
+      if (e == cudaSuccess)
+        e = hmp::launch_fallback_gate(f, p.rule, p.storage, tile_down, tile_coarse, dgrid, cgrid, fgrid, coarse_smem,
+                                      aux);
+      if (e != cudaSuccess) return failed(e, "copy-block fallback launch");
+    }
     if (fork) {
       e = cudaEventRecord(ev_join, aux);
       if (e == cudaSuccess) e = cudaStreamWaitEvent(s, ev_join, 0);
       if (e != cudaSuccess) return cuda_status(e, "stream join");
     }
-    if (copy) {
-      // The fallback: the dense chain on the caller stream, every CTA returning at once unless a
-      // copy block's source pixels held alpha 0 (then it recomputes the whole write rect, copy
-      // blocks included, after the gather wrote them).
-      hmp::PyrArgs f = a;
+    if (gate && !fork) {
+      e = hmp::launch_fallback_gate(f, p.rule, p.storage, tile_down, tile_coarse, dgrid, cgrid, fgrid, coarse_smem, s);
+      if (e != cudaSuccess) return cuda_status(e, "copy-block fallback launch");
+    } else if (copy && !gate) {
       f.alpha_flag = nullptr;
-      f.gate = alpha_flag;
       cst = chain(f, false, s, false);
       if (cst.code != HMP_OK) return cst;
     }
