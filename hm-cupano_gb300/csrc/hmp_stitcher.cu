@@ -285,12 +285,14 @@ struct hmp_stitcher {
     return best;
   }
 
-  // Default cap on pyr_down's CTAs per SM. Two images, 64-pixel tiles: 4. Its 40 KB of shared
+  // Default cap on pyr_down's CTAs per SM, 64-pixel tiles. Two images: 4. Its 40 KB of shared
   // memory and ~48 registers would let five share an SM, and five measured slower beside the
   // canvas gather (8500x3300 at L=6: 0.103 -> 0.090 ms per frame with the cap; three would do as
-  // well, two is slower); packed five to an SM the one-wave kernel bunches onto fewer SMs. Other
-  // configurations are held to three or fewer by their shared memory already.
-  int default_residency() const { return plan.n == 2 && tile_down == 64 ? 4 : 0; }
+  // well, two is slower); packed five to an SM the one-wave kernel bunches onto fewer SMs. Four
+  // or more images (the N-way kernel): 4 as well (eight-image 9000x2400 at L=6: 0.2057 -> 0.1971
+  // ms per frame FP32, 0.2015 -> 0.1955 FP16; 3 and 5 no better than none). Three images: no cap
+  // (2 to 5 measured no better).
+  int default_residency() const { return (plan.n == 2 || plan.n >= 4) && tile_down == 64 ? 4 : 0; }
 
   // pyr_coarse's shared memory: the N-way kernel holds `coarse_cap` slots and no mask values.
   size_t coarse_smem_for(int t1) const {
