@@ -137,6 +137,36 @@ def test_alpha_zero_runs_the_fallback(oracle_lib, workload, kind, levels, scale,
     _exact(gpu_stitch(st, fr), o.run(fr), "clean frame after a fallback")
 
 
+@pytest.mark.parametrize("workload,kind,levels,scale,storage,tile_down", [
+    ("pano3_2704x1520_to_6000x1800", 3, 6, 0.25, "f16", 64),
+    ("panon8_2000x1500_to_9000x2400", 1, 6, 0.25, "f16", 64),
+    ("pano2_5120x2880_to_8500x3300", 2, 6, 0.5, "f32", 32),
+    ("pano2_5120x2880_to_8500x3300", 2, 6, 0.5, "f16", 32),
+])
+def test_alpha_zero_fallback_storage_and_tiles(oracle_lib, workload, kind, levels, scale, storage, tile_down):
+    """The fallback's dense chain in the other instantiations it launches: FP16 level storage
+    (against the FP64 oracle within the FP16 tolerance) and 32-pixel down tiles."""
+    from hmpano import synth
+
+    rig = synth.workload_rig(workload, seed=47, kind=kind, scale=scale)
+    st = make_stitcher(kind, masks_for_rig(rig), levels, storage=storage)
+    st.set_tiles(tile_down)
+    o = oracle_lib.Stitch.from_rig(rig, levels)
+    rng = np.random.default_rng(9)
+    fr = synth.rig_frames(rig, seed=6)
+    for k in range(rig.n):
+        ys = rng.integers(0, rig.src_h[k], 16)
+        xs = rng.integers(0, rig.src_w[k], 16)
+        fr[k][:, ys, xs, 3] = 0
+    for what, frames in (("alpha 0", fr), ("clean frame after a fallback", synth.rig_frames(rig, seed=7))):
+        out = gpu_stitch(st, frames)
+        if storage == "f32":
+            _exact(out, o.run(frames), what)
+        else:
+            mx, mean = lsb_stats(out, o.run(frames, "f64"))
+            assert mx <= 1 and mean <= 0.05, (what, mx, mean)
+
+
 def test_frames_smaller_than_the_tables(oracle_lib):
     """Frames cropped below the tables' coordinates: entries past the frames read as fills, so the
     copy blocks do not apply and the call runs the full pyramid."""
