@@ -153,11 +153,11 @@ class Plan:
         return [c[last % 2][-1] for c in self.canvases]
 
 
-def autotune(job: Job, batches=(1, 2, 4, 8), tiles=(32, 64), residencies=(0, 4), reps: int = 3,
+def autotune(job: Job, batches=(1, 2, 4, 8, 16), tiles=(32, 64), residencies=(0, 4), reps: int = 3,
              use_cache: bool = True) -> dict:
     """Time every frames-per-call candidate with every pyramid down-tile edge per stream kind
-    (two-image and three-image streams choose theirs separately; two-image streams with 64-pixel
-    tiles also try each cap on the down kernel's CTAs per SM); keep and cache the fastest."""
+    (two-image and three-image streams choose theirs separately; with 64-pixel tiles each also
+    tries each cap on the down kernel's CTAs per SM); keep and cache the fastest."""
     key = job.signature()
     cache = {}
     if use_cache and CACHE.exists():
@@ -172,7 +172,7 @@ def autotune(job: Job, batches=(1, 2, 4, 8), tiles=(32, 64), residencies=(0, 4),
     def options(kind):
         out = []
         for tile in tiles:
-            for res in (residencies if kind == 2 and tile == 64 else (0,)):
+            for res in (residencies if tile == 64 else (0,)):
                 out.append((tile, res))
         return out
 
