@@ -161,3 +161,19 @@ def test_stabilizer_abi_rejects_bad_arguments_before_any_device_work():
     assert lib.hmp_stabilizer_get_response(None, None, 0, None).code == 1
     assert lib.hmp_stabilizer_set_features(None, None, 0, None).code == 1
     lib.hmp_stabilizer_destroy(None)
+
+
+def test_oracle_warp_rounds_extreme_motion_like_the_gpu(oracle_lib):
+    """The warp's shift is the motion rounded as the GPU's float-to-int conversion does it:
+    NaN shifts nothing, a shift past the frame leaves only zero fill (clamped at 2^24)."""
+    from oracle.oracle import _ptr
+    import ctypes as C
+
+    L = oracle_lib.lib()
+    img = texture(20, 30, seed=3)
+    out = np.full_like(img, -1.0)
+    for dx, dy, want in [(float("nan"), 0.0, img), (0.0, float("nan"), img),
+                         (1e30, 0.0, np.zeros_like(img)), (-1e30, 2.0, np.zeros_like(img)),
+                         (0.4, -0.4, img)]:
+        L.hmpo_stab_warp(_ptr(img, C.c_float), 30, 20, dx, dy, _ptr(out, C.c_float))
+        assert np.array_equal(out, want), (dx, dy)
