@@ -271,10 +271,11 @@ HMP_API hmp_status hmp_stitcher_set_down_residency(hmp_stitcher* st, int ctas_pe
  * over the remaining blocks and the tiles their reconstruction reads. Two conditions are checked
  * per call, and the full pyramid runs when either fails: the frames must contain every table
  * entry the copy blocks read (host check), and every source pixel behind a copy block must have
- * alpha != 0 (device check; a failure runs the whole write rect through the pyramid in three
- * extra launches that otherwise return at once). Results are identical either way; off forces
- * the full pyramid every call. Applies to RGBA8 stitchers of 3..8 images with the box filter and
- * two or more levels. */
+ * alpha != 0 (device check; a failure runs the whole write rect through the pyramid, launched
+ * from one single-thread kernel that otherwise returns at once, or under stream capture from three
+ * gated launches). Results are identical either way; off forces the full pyramid every call.
+ * Applies to RGBA8 stitchers with the box filter and two or more levels: 3..8 images, and two
+ * images whose minimised blend strip lines up with the canvas. */
 HMP_API hmp_status hmp_stitcher_set_copy_blocks(hmp_stitcher* st, int enable);
 
 /* Enable (1) or disable (0) per-kernel event timing; enabling clears the accumulated times.
