@@ -22,6 +22,7 @@
 #include <string>
 #include <thread>
 #include <unordered_map>
+#include <unordered_set>
 #include <vector>
 
 #include "hmp_admission.h"
@@ -84,6 +85,7 @@ struct hmp_server {
   std::condition_variable cv_work, cv_done;
   std::deque<Request> pending;            // submitted, not yet taken by the dispatcher
   std::unordered_map<long long, hmp_status> done;
+  std::unordered_multiset<long long> waited_ids;  // requests a hmp_server_wait call waits for
   long long next_id = 1;
   long long submitted = 0, completed = 0, failed = 0, created = 0, evicted = 0, outstanding = 0;
   int max_in_flight = 0;
@@ -114,7 +116,10 @@ struct hmp_server {
     } else {
       ++failed;
     }
-    cv_done.notify_all();
+    // Wake waiters only when one of them can return: drains once nothing is outstanding, a wait
+    // once its request is done. Waking every waiter on every completion had them contend for `mu`
+    // with this thread at each of thousands of completions a second.
+    if (outstanding == 0 || waited_ids.count(r.id) > 0) cv_done.notify_all();
   }
 
   // One dispatcher step; returns true if it did any work.
@@ -379,8 +384,10 @@ HMP_API hmp_status hmp_server_submit(hmp_server* s, int config_id, const hmp_ima
 HMP_API hmp_status hmp_server_wait(hmp_server* s, long long request_id, int timeout_ms) {
   if (!s) return mk(HMP_ERR_INVALID_VALUE, "server is null");
   std::unique_lock<std::mutex> lk(s->mu);
+  const auto w = s->waited_ids.insert(request_id);
   const bool ok = s->cv_done.wait_for(lk, std::chrono::milliseconds(std::max(0, timeout_ms)),
                                       [&] { return s->done.count(request_id) > 0; });
+  s->waited_ids.erase(w);
   if (!ok) return mk(HMP_ERR_TIMEOUT, "request did not finish within the timeout");
   const hmp_status r = s->done[request_id];
   s->done.erase(request_id);
