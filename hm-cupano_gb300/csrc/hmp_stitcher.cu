@@ -148,6 +148,7 @@ struct hmp_stitcher {
   // recompute everything when a copy block's source pixels hold alpha 0.
   bool copy_plan = false;  // planned for this configuration
   bool copy_on = true;     // hmp_stitcher_set_copy_blocks
+  bool copy_opaque = false;  // mode 2: frames promised opaque, no alpha checks and no fallback
   const uint32_t* fine_list = nullptr;
   const uint32_t* coarse_list = nullptr;
   const uint32_t* down_list[2] = {};  // tile_down 32, 64 (nullptr where that tile is not allowed)
@@ -572,7 +573,7 @@ struct hmp_stitcher {
   // Kernels one process() launches in copy-block mode: the flag reset, the listed pyramid kernels,
   // the gather and the three gated fallbacks.
   int copy_launches() const {
-    return (n_down[tile_down == 64 ? 1 : 0] > 0) + (n_coarse > 0) + (n_fine > 0) + 1 + 1;
+    return (n_down[tile_down == 64 ? 1 : 0] > 0) + (n_coarse > 0) + (n_fine > 0) + 1 + (copy_opaque ? 0 : 1);
   }
 
   // Compulsory bytes per process(): outside the write rect, 4 (table) + 1 (seam) + a source and
@@ -954,8 +955,9 @@ struct hmp_stitcher {
       ga.seg_pitch = seg_pitch;
       if (copy) {
         // The gather writes the copy blocks too (the pyramid blocks' entries are skips) and checks
-        // the alpha of every source pixel it reads over the blend region.
-        ga.alpha_flag = alpha_flag;
+        // the alpha of every source pixel it reads over the blend region (unless the caller
+        // promised opaque frames).
+        ga.alpha_flag = copy_opaque ? nullptr : alpha_flag;
         ga.chk_x0 = p.blend.x;
         ga.chk_y0 = p.blend.y;
         ga.chk_x1 = p.blend.x + p.blend.w;
@@ -1074,7 +1076,7 @@ struct hmp_stitcher {
       return ok_status();
     };
     if (copy) {  // pyr_fine checks the pyramid-block pixels inside copy blocks' supports
-      a.alpha_flag = alpha_flag;
+      a.alpha_flag = copy_opaque ? nullptr : alpha_flag;
       a.support_mark = support_mark;
       a.sm_pitch = sm_pitch;
       a.sm_shift = sm_shift;
@@ -1089,12 +1091,15 @@ struct hmp_stitcher {
     // In a CUDA graph the gate's device-side launches did not run (the graph replay test of copy
     // blocks on alpha-0 frames caught it), so a captured call keeps three gated launches whose
     // CTAs walk the dense tiles when the flag is set; the last one clears it.
+    // With frames promised opaque (hmp_stitcher_set_copy_blocks mode 2) nothing is checked and no
+    // fallback is launched.
+    const bool checked = copy && !copy_opaque;
     cudaStreamCaptureStatus capture = cudaStreamCaptureStatusNone;
-    if (copy) {
+    if (checked) {
       e = cudaStreamIsCapturing(s, &capture);
       if (e != cudaSuccess) return failed(e, "stream capture query");
     }
-    const bool gate = copy && capture == cudaStreamCaptureStatusNone;
+    const bool gate = checked && capture == cudaStreamCaptureStatusNone;
     hmp::PyrArgs f = a;
     f.gate = alpha_flag;
     if (gather) {
@@ -1119,7 +1124,7 @@ struct hmp_stitcher {
     if (gate && !fork) {
       e = hmp::launch_fallback_gate(f, p.rule, p.storage, tile_down, tile_coarse, dgrid, cgrid, fgrid, coarse_smem, s);
       if (e != cudaSuccess) return cuda_status(e, "copy-block fallback launch");
-    } else if (copy && !gate) {
+    } else if (checked && !gate) {
       f.alpha_flag = nullptr;
       cst = chain(f, false, s, false);
       if (cst.code != HMP_OK) return cst;
@@ -1246,7 +1251,9 @@ HMP_API hmp_status hmp_stitcher_set_down_residency(hmp_stitcher* st, int ctas_pe
 HMP_API hmp_status hmp_stitcher_set_copy_blocks(hmp_stitcher* st, int enable) {
   if (!st) return make_status(HMP_ERR_INVALID_VALUE, "stitcher is null");
   if (st->status.code != HMP_OK) return st->status;
+  if (enable < 0 || enable > 2) return make_status(HMP_ERR_INVALID_VALUE, "copy-block mode must be 0, 1 or 2");
   st->copy_on = enable != 0;
+  st->copy_opaque = enable == 2;
   return ok_status();
 }
 

@@ -523,9 +523,12 @@ class _Stitcher:
         if not s.ok():
             raise CudaStatusError(s)
 
-    def set_copy_blocks(self, enable: bool) -> None:
-        """Copy blocks on (default) or off (tuning and tests only: both give the same bits)."""
-        s = _status(_lib.lib().hmp_stitcher_set_copy_blocks(self._handle, 1 if enable else 0))
+    def set_copy_blocks(self, enable: bool, opaque_frames: bool = False) -> None:
+        """Copy blocks on (default) or off (both give the same bits). ``opaque_frames``: the caller
+        promises every source pixel has alpha != 0 (camera and video frames), which drops the
+        per-call alpha check and its fallback launch."""
+        mode = (2 if opaque_frames else 1) if enable else 0
+        s = _status(_lib.lib().hmp_stitcher_set_copy_blocks(self._handle, mode))
         if not s.ok():
             raise CudaStatusError(s)
 

@@ -4,7 +4,9 @@
   storage, with the 5-tap Binomial5 filter, and as a hard seam (0 levels);
 * the eight-image rig (8 x 2000x1500 -> 9000x2400, 45-degree steps) at 6 levels, FP32 and FP16;
 * the three-image stream of the batched workload (3 x 2704x1520 -> 6000x1800) at 6 levels, FP32
-  and FP16.
+  and FP16;
+* the headline frame with copy blocks for frames promised opaque (no per-call alpha check and no
+  fallback launch).
 
 Each variant: one stitcher, batch 1, two rotating frame/canvas sets (every set is larger than the
 129 MB L2), warm-up calls, then CUDA events around `steps` process() calls on one stream.
@@ -30,7 +32,11 @@ VARIANTS = [
     ("panon8_l6_f16", "panon8_2000x1500_to_9000x2400", 1, 6, "f16", "refbox"),
     ("pano3_l6_f32", "pano3_2704x1520_to_6000x1800", 3, 6, "f32", "refbox"),
     ("pano3_l6_f16", "pano3_2704x1520_to_6000x1800", 3, 6, "f16", "refbox"),
+    ("pano2_l6_f32_opaque", "pano2_5120x2880_to_8500x3300", 2, 6, "f32", "refbox"),
 ]
+# Variants run with copy blocks for frames promised opaque (hmp_stitcher_set_copy_blocks mode 2:
+# no per-call alpha check, no fallback launch); the synthetic frames are opaque (alpha 255).
+OPAQUE = {"pano2_l6_f32_opaque"}
 
 
 def masks_for(kind: int, rig):
@@ -97,10 +103,13 @@ def run(device, steps: int, peak_gbs: float, warmup: int = 5, only=None) -> dict
         st = stitcher(kind, masks, levels, storage=storage, filter=filt)
         if not st.status.ok():
             raise pano.CudaStatusError(st.status)
+        if name in OPAQUE:
+            st.set_copy_blocks(True, opaque_frames=True)
         ms = time_frames(st, sets, steps, warmup, device)
         info = st.info()
         mpix = rig.canvas_w * rig.canvas_h / 1e6
         out[name] = {"workload": workload, "levels": levels, "storage": storage, "filter": filt,
+                     "copy_blocks": "opaque frames" if name in OPAQUE else "checked",
                      "ms_per_frame": round(ms, 5), "fps": round(1e3 / ms, 1), "mpix_s": round(mpix / ms * 1e3, 1),
                      "m0_bytes": int(info["m0_bytes"]),
                      "hbm_frac_frame": round(info["m0_bytes"] / (ms / 1e3) / (peak_gbs * 1e9), 4),

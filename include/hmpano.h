@@ -262,7 +262,8 @@ typedef struct hmp_kernel_timing {
  * No counterpart in the reference. */
 HMP_API hmp_status hmp_stitcher_set_down_residency(hmp_stitcher* st, int ctas_per_sm);
 
-/* Copy blocks: on (1, the default) or off (0). No counterpart in the reference.
+/* Copy blocks: on (1, the default), off (0), or on for frames the caller promises are opaque (2).
+ * No counterpart in the reference.
  * Three-image and N-image blend regions cover most of the canvas, but wherever the seam mask is
  * one image's at every level of a pixel's reconstruction and that image is valid there, the
  * pyramid's result is that image's pixel exactly (the box filter and bilinear upsample keep every
@@ -275,7 +276,10 @@ HMP_API hmp_status hmp_stitcher_set_down_residency(hmp_stitcher* st, int ctas_pe
  * from one single-thread kernel that otherwise returns at once, or under stream capture from three
  * gated launches). Results are identical either way; off forces the full pyramid every call.
  * Applies to RGBA8 stitchers with the box filter and two or more levels: 3..8 images, and two
- * images whose minimised blend strip lines up with the canvas. */
+ * images whose minimised blend strip lines up with the canvas. Mode 2 drops the device check and
+ * its fallback (one launch fewer per call): for frames whose source pixels all have alpha != 0
+ * (camera and video frames, alpha 255); a source pixel with alpha 0 behind a copy block then gives
+ * that block the source pixel where the reference's pyramid would blend it out. */
 HMP_API hmp_status hmp_stitcher_set_copy_blocks(hmp_stitcher* st, int enable);
 
 /* Enable (1) or disable (0) per-kernel event timing; enabling clears the accumulated times.

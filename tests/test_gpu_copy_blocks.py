@@ -208,3 +208,30 @@ def test_graph_replay_with_copy_blocks(oracle_lib):
         g.replay()
         torch.cuda.synchronize()
         _exact(canvas.cpu().numpy(), o.run(fr), f"graph replay, seed {seed}")
+
+
+@pytest.mark.parametrize("workload,kind,levels,scale", [
+    ("pano2_5120x2880_to_8500x3300", 2, 6, 0.5),
+    ("pano3_2704x1520_to_6000x1800", 3, 6, 0.25),
+    ("panon8_2000x1500_to_9000x2400", 1, 6, 0.25),
+])
+def test_opaque_frames_mode(oracle_lib, workload, kind, levels, scale):
+    """Copy blocks for frames promised opaque (mode 2): no alpha check and no fallback launch, and
+    on opaque frames the same bits as the oracle; modes switch per call."""
+    from hmpano import _lib, synth
+
+    rig = synth.workload_rig(workload, seed=53, kind=kind, scale=scale)
+    st = make_stitcher(kind, masks_for_rig(rig), levels)
+    o = oracle_lib.Stitch.from_rig(rig, levels)
+    checked = st.info()["launches_per_process"]
+    st.set_copy_blocks(True, opaque_frames=True)
+    assert st.info()["launches_per_process"] == checked - 1
+    for seed in (12, 13):
+        fr = synth.rig_frames(rig, seed=seed)
+        _exact(gpu_stitch(st, fr), o.run(fr), f"opaque frames, seed {seed}")
+    st.set_copy_blocks(True)
+    fr = synth.rig_frames(rig, seed=14)
+    _exact(gpu_stitch(st, fr), o.run(fr), "checked mode after opaque mode")
+    for bad in (-1, 3):
+        s = _lib.lib().hmp_stitcher_set_copy_blocks(st._handle, bad)
+        assert s.code == 1, bad
