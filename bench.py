@@ -171,13 +171,42 @@ def pad_steps(step, stream, seconds: float) -> int:
     return n
 
 
+def _concurrent_copies_s(dev, h_in, d_in, d_out, h_out) -> float:
+    """Best of 5 (CUDA events) of one host-to-device copy and one device-to-host copy issued on
+    two streams at once, in seconds."""
+    import torch
+
+    s_up, s_dn = torch.cuda.Stream(dev), torch.cuda.Stream(dev)
+    best = float("inf")
+    for _ in range(5):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        fork, done = torch.cuda.Event(), torch.cuda.Event()
+        e0.record(s_up)
+        fork.record(s_up)
+        s_dn.wait_event(fork)
+        with torch.cuda.stream(s_up):
+            d_in.copy_(h_in, non_blocking=True)
+        with torch.cuda.stream(s_dn):
+            h_out.copy_(d_out, non_blocking=True)
+        done.record(s_dn)
+        s_up.wait_event(done)
+        e1.record(s_up)
+        torch.cuda.synchronize(dev)
+        best = min(best, e0.elapsed_time(e1) / 1e3)
+    return best
+
+
 def host_link(dev, nbytes: int = 256 << 20) -> dict:
     """Pinned host <-> device copy bandwidth (GB/s, best of 5, CUDA events), the bound of the
-    end-to-end number, whose every step copies its frames in and its canvas out."""
+    end-to-end number, whose every step copies its frames in and its canvas out: each direction
+    alone, and each direction while the other runs (`both`; the link carries less per direction
+    then, so this, not the one-way figures, bounds a pipeline that overlaps the two)."""
     import torch
 
     h = torch.empty(nbytes, dtype=torch.uint8).pin_memory()
+    h2 = torch.empty(nbytes, dtype=torch.uint8).pin_memory()
     d = torch.empty(nbytes, dtype=torch.uint8, device=dev)
+    d2 = torch.empty(nbytes, dtype=torch.uint8, device=dev)
     s = torch.cuda.Stream(dev)
     out = {}
     for name, dst, src in (("h2d", d, h), ("d2h", h, d)):
@@ -191,7 +220,20 @@ def host_link(dev, nbytes: int = 256 << 20) -> dict:
             torch.cuda.synchronize(dev)
             best = min(best, e0.elapsed_time(e1) / 1e3)
         out[name] = round(nbytes / best / 1e9, 1)
+    out["both"] = round(nbytes / _concurrent_copies_s(dev, h, d, d2, h2) / 1e9, 1)
     return out
+
+
+def step_copy_floor_ms(dev, in_bytes: int, out_bytes: int) -> float:
+    """The copies of one end-to-end step alone: `in_bytes` host to device while `out_bytes` go
+    device to host (ms, best of 5), the floor for a step whose copies overlap."""
+    import torch
+
+    h_in = torch.empty(in_bytes, dtype=torch.uint8).pin_memory()
+    h_out = torch.empty(out_bytes, dtype=torch.uint8).pin_memory()
+    d_in = torch.empty(in_bytes, dtype=torch.uint8, device=dev)
+    d_out = torch.empty(out_bytes, dtype=torch.uint8, device=dev)
+    return _concurrent_copies_s(dev, h_in, d_in, d_out, h_out) * 1e3
 
 
 def _masks(rig):
@@ -478,11 +520,10 @@ def main() -> None:
                "d2h_bytes_per_step": int(B * W * H * 4), "ms_per_step": round(ms_e2e, 4), "steps": k_e2e,
                "fps": round(world * B * 1e3 / ms_e2e, 1), "pipeline": "3 streams x 3 buffer sets",
                "output_check": ok}
-        # Its bound: the copies alone at the measured pinned copy bandwidth (the two directions
-        # overlap, so the floor is the slower of them).
+        # Its bound: the step's copies alone, both directions at once as the pipeline runs them
+        # (a direction carries less while the other runs, so the one-way rates understate it).
         link = host_link(dev)
-        floor_ms = max(e2e["h2d_bytes_per_step"] / (link["h2d"] * 1e9),
-                       e2e["d2h_bytes_per_step"] / (link["d2h"] * 1e9)) * 1e3
+        floor_ms = step_copy_floor_ms(dev, e2e["h2d_bytes_per_step"], e2e["d2h_bytes_per_step"])
         e2e["host_link_gbs"] = link
         e2e["copy_floor_ms_per_step"] = round(floor_ms, 4)
         e2e["frac_of_copy_floor"] = round(floor_ms / ms_e2e, 3)
