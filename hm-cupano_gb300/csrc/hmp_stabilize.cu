@@ -107,26 +107,44 @@ __device__ __forceinline__ bool is_corner(const float* resp, int w, int h, float
   return true;
 }
 
-// A warp per row: its corner count.
-__global__ void __launch_bounds__(256) corner_count_kernel(const float* resp, int w, int h, float thr, int* row_count) {
-  const int lane = threadIdx.x & 31, y = blockIdx.x * 8 + (threadIdx.x >> 5);
-  if (y >= h) return;
+// Corners are counted and emitted by segments: kCornerSeg pixels of one row, a warp each. Rows
+// split into segments give the count and emit passes many more warps than rows (a 3840-pixel row
+// is 8 segments), and the segments' raster order keeps the corners in raster order.
+constexpr int kCornerSeg = 512;
+constexpr int kScanPerThread = 8;  // segment counts per thread in each pass of the scan
+
+__host__ __device__ inline int corner_segments_per_row(int w) { return (w + kCornerSeg - 1) / kCornerSeg; }
+
+// A warp per segment: its corner count.
+__global__ void __launch_bounds__(256) corner_count_kernel(const float* resp, int w, int h, float thr, int segs,
+                                                           int* seg_count) {
+  const int lane = threadIdx.x & 31, g = blockIdx.x * 8 + (threadIdx.x >> 5);
+  if (g >= segs) return;
+  const int spr = corner_segments_per_row(w), y = g / spr, xs = (g - y * spr) * kCornerSeg;
+  const int xe = min(xs + kCornerSeg, w);
   int c = 0;
-  for (int x0 = 0; x0 < w; x0 += 32) c += __popc(__ballot_sync(0xFFFFFFFFu, is_corner(resp, w, h, thr, x0 + lane, y)));
-  if (lane == 0) row_count[y] = c;
+  for (int x0 = xs; x0 < xe; x0 += 32) c += __popc(__ballot_sync(0xFFFFFFFFu, is_corner(resp, w, h, thr, x0 + lane, y)));
+  if (lane == 0) seg_count[g] = c;
 }
 
-// One CTA: row offsets (exclusive scan of the counts, in chunks of 1024 rows) and the total.
-__global__ void __launch_bounds__(1024) corner_scan_kernel(const int* row_count, int h, int* row_off, Motion* m) {
+// One CTA: segment offsets (exclusive scan of the counts, kScanPerThread consecutive counts per
+// thread, 1024 threads a pass) and the total.
+__global__ void __launch_bounds__(1024) corner_scan_kernel(const int* seg_count, int segs, int* seg_off, Motion* m) {
   __shared__ int warp_sum[32];
   __shared__ int carry;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   if (threadIdx.x == 0) carry = 0;
   __syncthreads();
-  for (int base = 0; base < h; base += 1024) {
-    const int y = base + threadIdx.x;
-    const int v = y < h ? row_count[y] : 0;
-    int s = v;  // inclusive scan within the warp
+  for (int base = 0; base < segs; base += 1024 * kScanPerThread) {
+    const int i0 = base + threadIdx.x * kScanPerThread;
+    int v[kScanPerThread];
+    int t = 0;
+#pragma unroll
+    for (int e = 0; e < kScanPerThread; ++e) {
+      v[e] = i0 + e < segs ? seg_count[i0 + e] : 0;
+      t += v[e];
+    }
+    int s = t;  // inclusive scan of the threads' totals within the warp
 #pragma unroll
     for (int d = 1; d < 32; d <<= 1) {
       const int u = __shfl_up_sync(0xFFFFFFFFu, s, d);
@@ -144,22 +162,28 @@ __global__ void __launch_bounds__(1024) corner_scan_kernel(const int* row_count,
       warp_sum[lane] = ws;  // inclusive over warps
     }
     __syncthreads();
-    const int before = carry + (wid > 0 ? warp_sum[wid - 1] : 0) + s - v;
-    if (y < h) row_off[y] = before;
+    int before = carry + (wid > 0 ? warp_sum[wid - 1] : 0) + s - t;
+#pragma unroll
+    for (int e = 0; e < kScanPerThread; ++e) {
+      if (i0 + e < segs) seg_off[i0 + e] = before;
+      before += v[e];
+    }
     __syncthreads();
-    if (threadIdx.x == 1023) carry = before + v;
+    if (threadIdx.x == 1023) carry = before;  // this pass's total added
     __syncthreads();
   }
   if (threadIdx.x == 0) m->corners = carry;
 }
 
-// A warp per row: its corners, in x order, at the row's offset (those within the capacity).
-__global__ void __launch_bounds__(256) corner_emit_kernel(const float* resp, int w, int h, float thr,
-                                                          const int* row_off, int2* xy, int cap) {
-  const int lane = threadIdx.x & 31, y = blockIdx.x * 8 + (threadIdx.x >> 5);
-  if (y >= h) return;
-  int at = row_off[y];
-  for (int x0 = 0; x0 < w; x0 += 32) {
+// A warp per segment: its corners, in x order, at the segment's offset (those within the capacity).
+__global__ void __launch_bounds__(256) corner_emit_kernel(const float* resp, int w, int h, float thr, int segs,
+                                                          const int* seg_off, int2* xy, int cap) {
+  const int lane = threadIdx.x & 31, g = blockIdx.x * 8 + (threadIdx.x >> 5);
+  if (g >= segs) return;
+  const int spr = corner_segments_per_row(w), y = g / spr, xs = (g - y * spr) * kCornerSeg;
+  const int xe = min(xs + kCornerSeg, w);
+  int at = seg_off[g];
+  for (int x0 = xs; x0 < xe; x0 += 32) {
     const bool c = is_corner(resp, w, h, thr, x0 + lane, y);
     const unsigned bits = __ballot_sync(0xFFFFFFFFu, c);
     const int pos = at + __popc(bits & ((1u << lane) - 1u));
@@ -377,14 +401,15 @@ hmp_status cuda_failure(cudaError_t e, const char* what) {
 struct hmp_stabilizer {
   int w = 0, h = 0, cap = 0, device = -1;
   float* resp = nullptr;
-  int* row_count = nullptr;
-  int* row_off = nullptr;
+  int segs = 0;  // corner segments (rows x corner_segments_per_row)
+  int* seg_count = nullptr;
+  int* seg_off = nullptr;
   int2* xy = nullptr;
   float2* flow = nullptr;
   Motion* motion = nullptr;
   float* temp = nullptr;  // an in-place warp's output before the copy back
   ~hmp_stabilizer() {
-    for (void* p : {static_cast<void*>(resp), static_cast<void*>(row_count), static_cast<void*>(row_off),
+    for (void* p : {static_cast<void*>(resp), static_cast<void*>(seg_count), static_cast<void*>(seg_off),
                     static_cast<void*>(xy), static_cast<void*>(flow), static_cast<void*>(motion),
                     static_cast<void*>(temp)})
       if (p) cudaFree(p);
@@ -412,11 +437,12 @@ HMP_API hmp_status hmp_stabilizer_create(int width, int height, int max_features
   st->w = width;
   st->h = height;
   st->cap = int(max_features == 0 ? interior : std::min<long long>(max_features, interior));
+  st->segs = height * corner_segments_per_row(width);
   cudaError_t e = cudaGetDevice(&st->device);
   const size_t px = size_t(width) * height;
   if (e == cudaSuccess) e = cudaMalloc(&st->resp, px * sizeof(float));
-  if (e == cudaSuccess) e = cudaMalloc(&st->row_count, size_t(height) * sizeof(int));
-  if (e == cudaSuccess) e = cudaMalloc(&st->row_off, size_t(height) * sizeof(int));
+  if (e == cudaSuccess) e = cudaMalloc(&st->seg_count, size_t(st->segs) * sizeof(int));
+  if (e == cudaSuccess) e = cudaMalloc(&st->seg_off, size_t(st->segs) * sizeof(int));
   if (e == cudaSuccess) e = cudaMalloc(&st->xy, size_t(std::max(st->cap, 1)) * sizeof(int2));
   if (e == cudaSuccess) e = cudaMalloc(&st->flow, size_t(std::max(st->cap, 1)) * sizeof(float2));
   if (e == cudaSuccess) e = cudaMalloc(&st->motion, sizeof(Motion));
@@ -440,10 +466,11 @@ HMP_API hmp_status hmp_stabilizer_corners(hmp_stabilizer* st, const float* img, 
   const cudaStream_t cs = static_cast<cudaStream_t>(stream);
   const dim3 tiles((st->w + kTX - 1) / kTX, (st->h + kTY - 1) / kTY);
   harris_kernel<<<tiles, dim3(kTX, kTY), 0, cs>>>(img, st->w, st->h, k, st->resp);
-  const int rows = (st->h + 7) / 8;
-  corner_count_kernel<<<rows, 256, 0, cs>>>(st->resp, st->w, st->h, threshold, st->row_count);
-  corner_scan_kernel<<<1, 1024, 0, cs>>>(st->row_count, st->h, st->row_off, st->motion);
-  corner_emit_kernel<<<rows, 256, 0, cs>>>(st->resp, st->w, st->h, threshold, st->row_off, st->xy, st->cap);
+  const int seg_blocks = (st->segs + 7) / 8;
+  corner_count_kernel<<<seg_blocks, 256, 0, cs>>>(st->resp, st->w, st->h, threshold, st->segs, st->seg_count);
+  corner_scan_kernel<<<1, 1024, 0, cs>>>(st->seg_count, st->segs, st->seg_off, st->motion);
+  corner_emit_kernel<<<seg_blocks, 256, 0, cs>>>(st->resp, st->w, st->h, threshold, st->segs, st->seg_off, st->xy,
+                                                 st->cap);
   const cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? status_of(HMP_OK, "") : cuda_failure(e, "corner launch");
 }
