@@ -201,6 +201,9 @@ def test_c_abi_rejects_bad_arguments_before_any_device_work(lib):
     assert lib.hmp_stitcher_get_info(None, C.byref(info)).code == 1
     assert lib.hmp_stitcher_process(None, None, 0, None, None).code == 1
     assert lib.hmp_stitcher_set_tiles(None, 64, 32).code == 1
+    for mode in (0, 1, 2):
+        assert lib.hmp_stitcher_set_copy_blocks(None, mode).code == 1
+    assert lib.hmp_stitcher_set_down_residency(None, 4).code == 1
     assert lib.hmp_stitcher_status(None).code == 1
     assert lib.hmp_stitcher_canvas_width(None) == 0
     lib.hmp_stitcher_destroy(None)  # no-op
@@ -387,3 +390,31 @@ def test_c_abi_header_is_plain_c(tmp_path):
         r = subprocess.run([cc, std, "-Wall", "-Wextra", "-pedantic", "-Werror", "-I", str(REPO / "include"),
                             "-fsyntax-only", str(src)], capture_output=True, text=True)
         assert r.returncode == 0, r.stderr
+
+
+def test_copy_block_modes_from_the_python_mirror(monkeypatch):
+    """set_copy_blocks(enable, opaque_frames) passes the C ABI's mode: 0 off, 1 on (checked),
+    2 on for frames promised opaque; opaque_frames without enable stays off. A recording stand-in
+    for the library takes the call, so no stitcher (and no GPU) is needed."""
+    from hmpano import _lib, pano
+
+    calls = []
+
+    class FakeLib:
+        def hmp_stitcher_set_copy_blocks(self, handle, mode):
+            calls.append(mode)
+            return _lib.Status(0, b"")
+
+        def hmp_stitcher_destroy(self, handle):
+            pass
+
+    monkeypatch.setattr(_lib, "lib", lambda: FakeLib())
+    st = object.__new__(pano._Stitcher)
+    st._handle = C.c_void_p(1)  # never dereferenced: only the stand-in sees it
+    try:
+        for enable, opaque in ((False, False), (True, False), (True, True), (False, True)):
+            st.set_copy_blocks(enable, opaque_frames=opaque)
+        st.set_copy_blocks(True)
+    finally:
+        st._handle = C.c_void_p()  # so that no later destructor hands it to the real library
+    assert calls == [0, 1, 2, 0, 1]
